@@ -1,0 +1,306 @@
+#!/usr/bin/env python
+"""Headline benchmark: time to FP64 relres <= 1e-12 on the N=32768 Gaussian RBF system.
+
+One step = one complete solve of the headline system from x = 0 to the FP64
+relative residual tolerance (factorization / FP32 copy included, assembly
+excluded), with A already resident in HBM.  Prints ONE JSON line.
+
+Extra keys:
+  fp64_gpu_baseline  the plain FP64 GPU solve of the same system (FP64 LU of
+                     the vendor library + FP64 refinement), timed once
+  roofline           the dominant kernel class, timed live with CUDA events
+  cpu_baseline       SciPy FP64 LU on the host cores at a bounded sample N,
+                     scaled by (N / n_sample)^3
+  e2e                the same solve through the public API with host inputs
+                     (pinned host -> device copy and x back to the host timed)
+
+--impl reference runs the reference's CPU path (SciPy FP64 LU, the oracle)
+instead, on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+HEADLINE_METRIC = "time to FP64 relres<=1e-12, mixed-precision GMRES-IR vs plain FP64 GPU solve (N=32768 Gaussian RBF)"
+UNIT = "s"
+FALLBACK_HBM = 6800.0
+FALLBACK_BF16 = 1900.0
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", FALLBACK_HBM)), float(d.get("bf16_tflops", FALLBACK_BF16)), \
+            float(d.get("bf16_tflops_sustained", FALLBACK_BF16)), "measured"
+    return FALLBACK_HBM, FALLBACK_BF16, 1700.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sms.sort()
+        med = sms[len(sms) // 2] if sms else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def cpu_lu_sample(n_sample: int, repeats: int, config: str = "HEADLINE"):
+    """SciPy FP64 LU solve timed in a child process with all host threads."""
+    try:
+        threads = len(os.sched_getaffinity(0))
+    except AttributeError:
+        threads = os.cpu_count() or 1
+    env = dict(os.environ, OPENBLAS_NUM_THREADS=str(threads), OMP_NUM_THREADS=str(threads),
+               MKL_NUM_THREADS=str(threads))
+    out = subprocess.run([sys.executable, "-m", "oracle.cpu_baseline", "--n", str(n_sample), "--repeats",
+                          str(repeats), "--config", config], cwd=str(ROOT), env=env, capture_output=True, text=True,
+                         timeout=1800)
+    if out.returncode != 0:
+        raise RuntimeError(out.stderr[-2000:])
+    d = json.loads(out.stdout.strip().splitlines()[-1])
+    d["threads"] = threads
+    return d
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path (SciPy FP64 LU) on rank 0."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    n_full = args.n
+    ns = args.cpu_sample_n
+    scale = (n_full / ns) ** 3
+    d = cpu_lu_sample(ns, args.warmup + args.steps)
+    secs = d["seconds"][args.warmup:] or d["seconds"]
+    per = sum(secs) / len(secs) * scale
+    line = {
+        "impl": "reference", "metric": HEADLINE_METRIC, "value": per, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded NumPy)",
+        "config": {"workload": f"HEADLINE Gaussian RBF N={n_full}, eps=40, nugget 1e-2, SciPy FP64 LU + refinement",
+                   "sample_n": ns},
+        "cpu_baseline": {"value": per, "unit": UNIT, "cores": d["threads"], "kind": "port",
+                         "sample": f"scipy lu_factor/lu_solve FP64 at N={ns} (x{scale:.1f} O(N^3) scaling to "
+                                   f"N={n_full}); relres {d['relres']:.2e}"},
+        "e2e": {"value": per, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--n", type=int, default=32768)
+    ap.add_argument("--cpu-sample-n", type=int, default=8192)
+    ap.add_argument("--no-fp64-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    from mpdok_gb300 import _native as NV
+    from mpdok_gb300 import configs
+    from mpdok_gb300.solvers import MixedSolver, fp64_gpu_solve
+    from mpdok_gb300.rbf_kernel import assemble
+
+    sysm = configs.headline(n=args.n)
+    n = sysm.n
+    b = torch.from_numpy(np.asarray(sysm.b)).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    A = assemble(sysm.coords, gamma=sysm.gamma, reg=sysm.reg, kernel=sysm.kernel, dtype=torch.float64)
+    torch.cuda.synchronize()
+    t_asm = time.perf_counter() - t0
+
+    solver = MixedSolver()
+    for _ in range(args.warmup):
+        x, info = solver.solve(A, b, tol=sysm.tol)
+    torch.cuda.synchronize()
+    barrier()
+
+    NV.profile_enable(True)
+    l0 = NV.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    infos = []
+    for _ in range(args.steps):
+        x, info = solver.solve(A, b, tol=sysm.tol)
+        infos.append(info)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ck = clocks.stop()
+    launches = NV.launch_count() - l0
+    total_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    per_s = total_ms / 1e3 / args.steps
+    prof = {}
+    for name, cls in (("gemv_f32", NV.PROF_GEMV_F32), ("gemv_f64", NV.PROF_GEMV_F64), ("lu_gemm", NV.PROF_LU_GEMM),
+                      ("trsv", NV.PROF_TRSV), ("lu_panel", NV.PROF_LU_PANEL)):
+        ms, cnt, work = NV.profile_query(cls)
+        prof[name] = (ms, cnt, work)
+    NV.profile_enable(False)
+
+    hbm, bf16, bf16s, peak_kind = _peaks()
+    # dominant kernel class by device time
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    name, (ms, cnt, work) = dom
+    if name == "lu_gemm":
+        achieved = work / (ms / 1e3) / 1e12
+        roof = {"kernel": name, "bound": "tensor", "achieved": achieved, "peak": bf16s, "unit": "TFLOP/s",
+                "frac": achieved / bf16s, "traffic": None, "launches_timed": cnt,
+                "avg_launch_ms": ms / max(1, cnt), "peak_source": f"{peak_kind} bf16 sustained"}
+    else:
+        achieved = work / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "launches_timed": cnt,
+                "avg_launch_ms": ms / max(1, cnt), "peak_source": f"{peak_kind} hbm copy"}
+    share = {k: v[0] / max(1e-9, total_ms) for k, v in prof.items()}
+
+    # accuracy of the timed solves
+    xs = x
+    relres = infos[-1]["relres"]
+
+    fp64 = None
+    if not args.no_fp64_baseline and rank == 0:
+        fp64 = fp64_gpu_solve(A, b, tol=sysm.tol)
+        err = float(torch.linalg.norm(xs - fp64["x"]) / torch.linalg.norm(fp64["x"]))
+        fp64 = {"seconds": fp64["seconds"], "relres": fp64["relres"], "method": fp64["method"],
+                "mixed_err_vs_fp64_lu": err, "speedup_mixed_vs_fp64": fp64["seconds"] / per_s}
+
+    e2e = None
+    if not args.no_e2e:
+        A_host = torch.empty_strided((n, n), (1, n), dtype=torch.float64, pin_memory=True)
+        A_host.copy_(A.cpu())
+        b_host = torch.from_numpy(np.asarray(sysm.b)).pin_memory()
+        times = []
+        for i in range(max(1, min(args.steps, 3)) + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            xe, _ = solver.solve(A_host, b_host, tol=sysm.tol)
+            xh = xe.cpu()
+            torch.cuda.synchronize()
+            if i > 0:
+                times.append(time.perf_counter() - t0)
+        del A_host
+        e2e = {"value": sum(times) / len(times), "unit": UNIT, "h2d_bytes_per_step": 8 * n * n + 8 * n,
+               "d2h_bytes_per_step": 8 * n, "api": "mpdok_gb300.solvers.MixedSolver.solve(host A, host b)"}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        try:
+            d = cpu_lu_sample(args.cpu_sample_n, 1)
+            scale = (n / args.cpu_sample_n) ** 3
+            cpu = {"value": d["seconds"][0] * scale, "unit": UNIT, "cores": d["threads"], "kind": "port",
+                   "sample": f"scipy lu_factor/lu_solve FP64 + refinement at N={args.cpu_sample_n}, "
+                             f"{d['seconds'][0]:.2f} s measured, x{scale:.1f} O(N^3) scaling to N={n}"}
+        except Exception as e:  # noqa: BLE001
+            cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {e}"}
+
+    line = {
+        "metric": HEADLINE_METRIC, "value": per_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per_s * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded NumPy, HEADLINE system)",
+        "config": {"workload": f"HEADLINE: Gaussian RBF N={n}, 2-D stratified jitter seed 2, eps=40 (gamma=1600), "
+                               f"nugget 1e-2, b~N(0,1); tol 1e-12; one step = one full solve (A in HBM)",
+                   "l2": "inputs larger than L2 (A64 8.6 GB, A32 4.3 GB)", "parallelism": f"replicas x{world}",
+                   "solver": solver.describe(), "assembly_s": t_asm},
+        "relres": relres, "solve_info": infos[-1], "fp64_gpu_baseline": fp64,
+        "roofline": roof, "kernel_time_share": share, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": launches, "clocks": ck,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,175 @@
+/*
+ * mpdok_gb300 — C ABI of the GB300-native dense-operator Krylov solvers.
+ *
+ * Two layers are exported:
+ *
+ *  1. The reference's own ctypes ABI (the symbols MPDOK's mpdok_ops.py binds
+ *     to mpdok.so / lu_ir.so).  Same names, argument order, argument meaning
+ *     and out-parameter conventions: device (or managed) pointers, A in
+ *     column-major (Fortran) order, void return, status through int*
+ *     out-parameters, the caller synchronises the null stream afterwards.
+ *     Like the reference these keep one process-wide saved factorization.
+ *
+ *  2. The handle-free mpdok_* API: explicit cudaStream_t, caller-owned
+ *     workspace sized by *_workspace_size(), int status return
+ *     (0 ok, <0 error, >0 numerical information), no hidden globals.
+ *
+ * All compute runs in hand-written sm_103a kernels; nothing here falls back
+ * to the CPU.
+ */
+#ifndef MPDOK_GB300_H
+#define MPDOK_GB300_H
+
+#include <stddef.h>
+#include <cuda_runtime.h>
+
+#if defined(__GNUC__)
+#define MPDOK_API __attribute__((visibility("default")))
+#else
+#define MPDOK_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  MPDOK_OK = 0,
+  MPDOK_ERR_INVALID_ARG = -1,
+  MPDOK_ERR_CUDA = -2,
+  MPDOK_ERR_ALLOC = -3,
+  MPDOK_ERR_NOT_FACTORED = -4,
+  MPDOK_ERR_TIMEOUT = -5,     /* a bounded device-side wait gave up */
+  MPDOK_ERR_UNSUPPORTED = -6,
+  MPDOK_ERR_IO = -7,
+  MPDOK_ERR_NONFINITE = -8    /* NaN / Inf met in a residual or pivot */
+};
+
+/* element types */
+enum { MPDOK_F64 = 0, MPDOK_F32 = 1, MPDOK_BF16 = 2, MPDOK_F16 = 3 };
+/* radial basis functions: Gaussian exp(-gamma r^2), multiquadric sqrt(1 + gamma r^2) */
+enum { MPDOK_KERNEL_GAUSSIAN = 0, MPDOK_KERNEL_MQ = 1 };
+
+#define MPDOK_HISTORY_MAX 256
+
+/* Per-solve report: outer FP64 relative residual history and counters. */
+typedef struct mpdok_solve_info {
+  int converged;          /* 1 when the FP64 relative residual fell below tol */
+  int outer_iters;        /* outer refinement steps (or restarts / CG checks) */
+  int inner_iters;        /* total inner matvecs */
+  int stagnated;          /* 1 when the 1 % stagnation rule stopped the solve */
+  double relres;          /* final FP64 ||b - A x|| / ||b|| */
+  double bnorm;           /* ||b|| */
+  int n_history;          /* entries used in history[] */
+  int hist_iter[MPDOK_HISTORY_MAX];   /* iteration index of each entry */
+  double history[MPDOK_HISTORY_MAX];  /* FP64 relative residual of each entry */
+} mpdok_solve_info;
+
+MPDOK_API int mpdok_version(void);
+MPDOK_API const char* mpdok_status_string(int status);
+/* Message of the last error raised on the calling host thread. */
+MPDOK_API const char* mpdok_last_error(void);
+
+/* ------------------------------------------------------------ assembly
+ * out(i, j) = phi(||rows_i - cols_j||) + reg * [i + diag_offset == j]
+ * rows: (n_rows, dim) and cols: (n_cols, dim) FP64, row-major (C order).
+ * out: column-major with leading dimension ld (col_major != 0) or row-major.
+ * Replaces rbf_kernel.py:158-227 (build_rbf_kernel) and mpdok_ooc.py:39-46
+ * (_build_fp32_tile).  FP64 output computes in FP64; FP32/BF16/FP16 in FP32. */
+MPDOK_API int mpdok_rbf_assemble(const double* rows, long long n_rows, const double* cols, long long n_cols,
+                       int dim, int kernel, double gamma, double reg, long long diag_offset,
+                       int out_dtype, void* out, long long ld, int col_major, cudaStream_t stream);
+
+/* Elementwise type conversion of n contiguous elements (the FP64 -> FP32
+ * copy of A that py_gmres_ir makes, mpdok_ops.py:329-333 / dense_krylov.py:47). */
+MPDOK_API int mpdok_convert(const void* src, int src_dtype, void* dst, int dst_dtype, long long n, cudaStream_t stream);
+
+/* ---------------------------------------------------------------- GEMV
+ * Y = alpha * op(A) X + beta * Y, A column-major (m x n, lda), op = A or A^T.
+ * X / Y are FP64 when A is FP64 and FP32 otherwise; nrhs columns.
+ * Replaces cp.matmul(A_fp32, x) (dense_krylov.py:61-63). */
+MPDOK_API size_t mpdok_gemv_workspace_size(int a_dtype, long long m, long long n, int nrhs, int trans);
+MPDOK_API int mpdok_gemv(int a_dtype, int trans, const void* A, long long lda, long long m, long long n,
+               const void* X, long long ldx, int nrhs, void* Y, long long ldy, double alpha, double beta,
+               void* work, size_t work_bytes, cudaStream_t stream);
+
+/* r = b - A x in FP64 and *rnorm2 = ||r||^2 (device scalar); workspace as
+ * mpdok_gemv_workspace_size(MPDOK_F64, n, n, 1, 0).
+ * Replaces DenseLinearOperator.residual_norm (dense_krylov.py:65-79). */
+MPDOK_API int mpdok_residual(const double* A, long long lda, long long n, const double* b, const double* x,
+                   double* r, double* rnorm2, void* work, size_t work_bytes, cudaStream_t stream);
+
+/* ------------------------------------------------------- Krylov drivers
+ * All vectors are device pointers; A32 is the FP32 copy of A (column-major,
+ * lda32), A64 the FP64 matrix used for residuals.  The solve stays on the
+ * device; the host reads one scalar per outer step. */
+MPDOK_API size_t mpdok_krylov_workspace_size(long long n, int restart);
+
+/* GMRES-IR, the algorithm of mpdok_ooc.py:315-373 with the inner solve of
+ * mpdok_ooc.py:231-311 (Arnoldi, two-pass classical Gram-Schmidt, FP64
+ * Givens rotations, early stop |g_{k+1}|/beta < inner_tol), which the
+ * reference labels as its port of the native py_gmres_ir.
+ * x holds the initial guess on entry and the FP64 solution on exit.
+ * a32_ready != 0 skips the FP64 -> FP32 conversion into A32. */
+MPDOK_API int mpdok_gmres_ir(const double* A64, long long lda, float* A32, long long lda32, int a32_ready,
+                   long long n, const double* b, double* x, double tol, int maxiter_outer, int restart,
+                   double inner_tol, void* work, size_t work_bytes, mpdok_solve_info* info,
+                   cudaStream_t stream);
+
+/* Restarted FP32 GMRES(m) of dense_krylov.py:212-331 (single Gram-Schmidt
+ * pass, FP64 residual check at each restart, 1 % stagnation stop).
+ * x: FP64 initial guess in, FP64 (promoted FP32 iterate) out. */
+MPDOK_API int mpdok_gmres(const float* A32, long long lda32, const double* A64, long long lda, long long n,
+                const double* b, double* x, double tol, int maxiter, int restart, void* work,
+                size_t work_bytes, mpdok_solve_info* info, cudaStream_t stream);
+
+/* GMRES-IR of dense_krylov.py:338-421: FP64 residual, inner restarted FP32
+ * GMRES (tol 1e-6, maxiter_inner), FP64 update, final residual. */
+MPDOK_API int mpdok_dense_gmres_ir(const float* A32, long long lda32, const double* A64, long long lda, long long n,
+                         const double* b, double* x, double tol, int maxiter_outer, int restart,
+                         int maxiter_inner, void* work, size_t work_bytes, mpdok_solve_info* info,
+                         cudaStream_t stream);
+
+/* FP32 conjugate gradients of dense_krylov.py:119-205 (FP64 residual check
+ * every check_every iterations, 1 % stagnation stop). */
+MPDOK_API int mpdok_cg(const float* A32, long long lda32, const double* A64, long long lda, long long n,
+             const double* b, double* x, double tol, int maxiter, int check_every, void* work,
+             size_t work_bytes, mpdok_solve_info* info, cudaStream_t stream);
+
+/* --------------------------------------------------------- instrumentation
+ * mpdok_launch_count: kernels launched by this library since load.
+ * mpdok_profile_enable(1) clears and starts per-launch CUDA-event timing of
+ * the kernel classes below (on the launching stream); mpdok_profile_query
+ * sums, after the work has completed, the device time, the number of
+ * launches and the algorithmic work (bytes or flops) of one class. */
+enum {
+  MPDOK_PROF_GEMV_F32 = 0,   /* stored FP32 / 16-bit GEMV stage (bytes)  */
+  MPDOK_PROF_GEMV_F64 = 1,   /* stored FP64 GEMV stage (bytes)           */
+  MPDOK_PROF_ASSEMBLE = 2,   /* RBF assembly (bytes written)             */
+  MPDOK_PROF_LU_GEMM = 3,    /* LU trailing-update GEMM (flops)          */
+  MPDOK_PROF_TRSV = 4,       /* triangular solves (bytes)                */
+  MPDOK_PROF_MATFREE = 5,    /* matrix-free evaluate-and-multiply (entries) */
+  MPDOK_PROF_OOC_COPY = 6,   /* host -> device tile copies (bytes)       */
+  MPDOK_PROF_LU_PANEL = 7    /* LU panel factorization (flops)           */
+};
+MPDOK_API long long mpdok_launch_count(void);
+MPDOK_API int mpdok_profile_enable(int on);
+MPDOK_API int mpdok_profile_query(int kernel_class, double* total_ms, long long* launches, double* work);
+
+/* ------------------------------------------- reference ctypes ABI (mpdok.so)
+ * mpdok_ops.py:362-373: A (N x N FP64, Fortran order), b, x (FP64, x is the
+ * output and starts as zeros), A_fp32 caller-owned FP32 scratch (N x N,
+ * Fortran order) that receives the FP32 copy of A; converged_out = 1 / 0. */
+MPDOK_API void py_gmres_ir(double* A, double* b, double* x, float* A_fp32, int N, double tol, int maxiter_outer,
+                 int restart, int* converged_out);
+/* mpdok_ops.py:375-382: (N, N) FP64 managed allocation, kept until
+ * py_free_managed(). */
+MPDOK_API void py_alloc_managed(int N, void** ptr_out);
+MPDOK_API void py_free_managed(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPDOK_GB300_H */

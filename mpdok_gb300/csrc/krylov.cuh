@@ -1,0 +1,61 @@
+// Device-resident Krylov machinery shared by the GMRES / CG / LU-IR drivers.
+#pragma once
+#include "gemv.cuh"
+
+namespace mpdok {
+
+// Device scalars of one solve (one cache line each group).
+struct KScal {
+  double nrm2;      // target of the last ordered reduction
+  double beta;      // ||rhs|| of the current Arnoldi cycle
+  double rs;        // CG: r.r
+  double alpha;     // CG step
+  double betacg;    // CG direction update
+  double aux;       // spare reduction target
+  int done;         // cycle finished: early stop, breakdown or stop request
+  int m_used;       // Arnoldi steps completed in the current cycle
+  int breakdown;    // |w| <= 1e-12 met
+  int nonfinite;    // NaN / Inf seen in a device scalar
+};
+
+// Workspace carve-up for a Krylov solve of size n with restart m.
+struct KWs {
+  long long n = 0, ldv = 0;
+  int m = 0;
+  float *V = nullptr, *w = nullptr, *x32 = nullptr, *b32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+  double *r64 = nullptr, *x64t = nullptr, *e64 = nullptr;
+  double *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr, *h2 = nullptr;
+  double* parts = nullptr;
+  unsigned* tickets = nullptr;  // 8 independent tickets
+  KScal* sc = nullptr;
+  void* gw = nullptr;
+  size_t gbytes = 0;
+  int nblk = 1;       // blocks of the row-chunked vector kernels
+  long long ch = 256; // rows per block of those kernels
+  size_t total = 0;
+};
+
+KWs krylov_layout(long long n, int m, void* base);
+
+// Preconditioner hook for right-preconditioned cycles: z = M^{-1} v.
+struct Precond {
+  int (*apply)(void* ctx, const float* v, float* z, cudaStream_t s, const int* skip) = nullptr;
+  void* ctx = nullptr;
+  float* z = nullptr;  // n floats of scratch for M^{-1} v
+};
+
+// One Arnoldi cycle (up to m steps) on the FP32 operator A32 with the
+// unnormalised start vector already in V[:,0] and ws.sc->nrm2 = ||V[:,0]||^2
+// set by cycle_setup.  reorth = 1 or 2 Gram-Schmidt passes.  Early stop when
+// |g_{k+1}| / beta < tol_rel (tol_rel <= 0 disables it).  The correction
+// V y (or M^{-1} V y when preconditioned) is added to x32 or x64.
+int arnoldi_cycle(const KWs& ws, const float* A32, long long lda32, int m, int reorth, double tol_rel,
+                  const Precond* pc, float* x32, double* x64, cudaStream_t s);
+
+// V[:,0] = (float) src64 and sc->nrm2, beta, flags for a new cycle.
+int cycle_start_from_f64(const KWs& ws, const double* src64, cudaStream_t s);
+
+int read_scal(const KWs& ws, KScal* host, cudaStream_t s);
+int norm2_f64(const KWs& ws, const double* x, long long n, double* out_dev, cudaStream_t s);
+
+}  // namespace mpdok

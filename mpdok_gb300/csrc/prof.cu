@@ -1,0 +1,99 @@
+// Launch counter and opt-in CUDA-event timing of kernel classes.
+//
+// Timing is per launch, on the stream the kernel is launched on, so a caller
+// can time the dominant kernel inside a larger timed region (the bench's
+// roofline figure) without a profiler.
+#include "common.cuh"
+
+#include <atomic>
+#include <mutex>
+#include <vector>
+
+namespace mpdok {
+
+static std::atomic<long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+struct ProfRec {
+  cudaEvent_t a = nullptr, b = nullptr;
+  int cls = 0;
+  double work = 0.0;
+  bool closed = false;
+};
+
+static std::mutex g_pmu;
+static bool g_prof_on = false;
+static std::vector<ProfRec> g_recs;
+static std::vector<cudaEvent_t> g_pool;
+
+static cudaEvent_t get_event() {
+  if (!g_pool.empty()) {
+    cudaEvent_t e = g_pool.back();
+    g_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+int prof_start(int cls, cudaStream_t s) {
+  if (!g_prof_on) return -1;
+  std::lock_guard<std::mutex> lk(g_pmu);
+  if (g_recs.size() >= (1u << 20)) return -1;
+  ProfRec r;
+  r.cls = cls;
+  r.a = get_event();
+  r.b = get_event();
+  if (!r.a || !r.b) return -1;
+  cudaEventRecord(r.a, s);
+  g_recs.push_back(r);
+  return (int)g_recs.size() - 1;
+}
+
+void prof_stop(int slot, cudaStream_t s, double work) {
+  if (slot < 0) return;
+  std::lock_guard<std::mutex> lk(g_pmu);
+  if ((size_t)slot >= g_recs.size()) return;
+  cudaEventRecord(g_recs[slot].b, s);
+  g_recs[slot].work = work;
+  g_recs[slot].closed = true;
+}
+
+}  // namespace mpdok
+
+using namespace mpdok;
+
+extern "C" long long mpdok_launch_count(void) { return launch_count(); }
+
+extern "C" int mpdok_profile_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_pmu);
+  for (auto& r : g_recs) {
+    if (r.a) g_pool.push_back(r.a);
+    if (r.b) g_pool.push_back(r.b);
+  }
+  g_recs.clear();
+  g_prof_on = on != 0;
+  return MPDOK_OK;
+}
+
+extern "C" int mpdok_profile_query(int cls, double* total_ms, long long* launches, double* work) {
+  std::lock_guard<std::mutex> lk(g_pmu);
+  double t = 0.0, w = 0.0;
+  long long n = 0;
+  for (auto& r : g_recs) {
+    if (r.cls != cls || !r.closed) continue;
+    float ms = 0.f;
+    cudaError_t e = cudaEventElapsedTime(&ms, r.a, r.b);
+    if (e != cudaSuccess) return cuda_status(e, "mpdok_profile_query");
+    t += ms;
+    w += r.work;
+    ++n;
+  }
+  if (total_ms) *total_ms = t;
+  if (launches) *launches = n;
+  if (work) *work = w;
+  return MPDOK_OK;
+}

@@ -1,0 +1,83 @@
+"""High-level mixed-precision solve used by the benchmark and the examples.
+
+``MixedSolver.solve(A, b)`` takes an (N, N) FP64 matrix (CUDA tensor in
+column-major order, or host memory, which is uploaded) and returns
+``(x, info)`` with x an FP64 CUDA tensor at the FP64 relative-residual
+tolerance.  ``fp64_gpu_solve`` is the plain FP64 GPU reference solve used for
+comparison (vendor FP64 LU through PyTorch, FP64 refinement with this
+library's residual kernel); it is a baseline, never used by the product path.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+
+import torch
+
+from . import _native as N
+from ._device import Workspace, as_fortran, as_vector, fortran_empty, ptr, stream_handle
+
+
+def _info_dict(info: N.SolveInfo) -> dict:
+    return {"converged": bool(info.converged), "outer_iters": int(info.outer_iters),
+            "inner_iters": int(info.inner_iters), "relres": float(info.relres),
+            "history": info.history_list()}
+
+
+class MixedSolver:
+    """FP64-accurate solve with FP32 Krylov work on the GPU (GMRES-IR)."""
+
+    def __init__(self, restart: int = 30, maxiter_outer: int = 60, inner_tol: float = 1e-6):
+        self.restart = restart
+        self.maxiter_outer = maxiter_outer
+        self.inner_tol = inner_tol
+        self._ws = Workspace()
+        self._a32 = None
+
+    def describe(self) -> str:
+        return (f"GMRES-IR: FP32 A copy + FP32 GMRES({self.restart}) inner (CGS2, FP64 Givens, inner tol "
+                f"{self.inner_tol:g}), FP64 residual/update")
+
+    def solve(self, A, b, tol: float = 1e-12):
+        A64 = as_fortran(A, torch.float64)
+        b64 = as_vector(b, torch.float64)
+        n = A64.shape[0]
+        if self._a32 is None or self._a32.shape[0] != n:
+            self._a32 = fortran_empty(n, n, torch.float32)
+        x = torch.zeros(n, dtype=torch.float64, device=b64.device)
+        lib = N.load()
+        w = self._ws.get(lib.mpdok_krylov_workspace_size(n, self.restart))
+        info = N.SolveInfo()
+        N.check(lib.mpdok_gmres_ir(ptr(A64), n, ptr(self._a32), n, 0, n, ptr(b64), ptr(x), float(tol),
+                                   self.maxiter_outer, self.restart, self.inner_tol, ptr(w), w.numel(),
+                                   ctypes.byref(info), stream_handle()), "gmres_ir")
+        return x, _info_dict(info)
+
+
+def fp64_gpu_solve(A, b, tol: float = 1e-12, max_refine: int = 3):
+    """Plain FP64 GPU solve: vendor FP64 LU (torch.linalg.lu_factor) + FP64 refinement."""
+    A64 = as_fortran(A, torch.float64)
+    b64 = as_vector(b, torch.float64)
+    n = A64.shape[0]
+    lib = N.load()
+    ws = Workspace()
+    w = ws.get(lib.mpdok_gemv_workspace_size(N.F64, n, n, 1, 0))
+    r = torch.empty_like(b64)
+    nrm2 = torch.empty(1, dtype=torch.float64, device=b64.device)
+    bn = float(torch.linalg.norm(b64))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    LU, piv = torch.linalg.lu_factor(A64)
+    x = torch.linalg.lu_solve(LU, piv, b64.reshape(-1, 1)).reshape(-1)
+    rel = float("inf")
+    for _ in range(max_refine + 1):
+        N.check(lib.mpdok_residual(ptr(A64), n, n, ptr(b64), ptr(x), ptr(r), ptr(nrm2), ptr(w), w.numel(),
+                                   stream_handle()), "residual")
+        rel = float(nrm2.item()) ** 0.5 / bn
+        if rel <= tol:
+            break
+        x = x + torch.linalg.lu_solve(LU, piv, r.reshape(-1, 1)).reshape(-1)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    del LU, piv
+    return {"x": x, "seconds": secs, "relres": rel, "method": "torch.linalg.lu_factor FP64 + FP64 refinement"}
