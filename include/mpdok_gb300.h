@@ -137,6 +137,45 @@ MPDOK_API int mpdok_cg(const float* A32, long long lda32, const double* A64, lon
              const double* b, double* x, double tol, int maxiter, int check_every, void* work,
              size_t work_bytes, mpdok_solve_info* info, cudaStream_t stream);
 
+/* ----------------------------------------------------------- LU (tensor cores)
+ * Blocked right-looking LU of W = D A D (D = diag(1/sqrt|a_ii|), panel 128)
+ * with FP32 panels and a trailing update W22 -= L21 U12 whose operands are
+ * rounded to the factor type: BF16 / FP16 run on tcgen05 tensor cores
+ * (FP32 accumulation in tensor memory), FP32 on CUDA cores (the reference's
+ * Sgetrf precision, benchmark_mpdok.ipynb:982-993).
+ *
+ * Factors live in a caller-owned device buffer of mpdok_lu_factor_size()
+ * bytes; factorization scratch is mpdok_lu_work_size() bytes.  pivoting: 0 =
+ * none (SPD / diagonally dominant systems, e.g. Gaussian RBF), 1 = partial
+ * pivoting.  Return: 0 ok, > 0 number of pivots that had to be perturbed
+ * away from zero (still a usable preconditioner), < 0 error. */
+enum { MPDOK_ENGINE_TENSOR = 0, MPDOK_ENGINE_SIMT = 1 };
+
+MPDOK_API int mpdok_gemm_update(float* C, long long ldc, const void* A, const void* B, int M, int N, int K,
+                                int fdtype, int engine, int* err, cudaStream_t stream);
+MPDOK_API size_t mpdok_lu_factor_size(long long n, int fdtype);
+MPDOK_API size_t mpdok_lu_work_size(long long n, int fdtype);
+MPDOK_API int mpdok_lu_factor(const double* A, long long lda, long long n, int fdtype, int pivoting, void* factors,
+                              size_t factor_bytes, void* work, size_t work_bytes, cudaStream_t stream);
+/* z = (D U^-1 L^-1 P D) v: one application of the factorization (FP32 vectors). */
+MPDOK_API size_t mpdok_lu_apply_work_size(long long n);
+MPDOK_API int mpdok_lu_apply(const void* factors, long long n, int fdtype, const float* v, float* z, void* work,
+                             size_t work_bytes, cudaStream_t stream);
+/* LU-IR (benchmark_mpdok.ipynb:982-993): x = LU^-1 b, then FP64 residual,
+ * correction solve with the factors, FP64 update, until relres < tol. */
+MPDOK_API size_t mpdok_lu_ir_work_size(long long n);
+MPDOK_API int mpdok_lu_ir_solve(const double* A, long long lda, long long n, const void* factors, int fdtype,
+                                const double* b, double* x, double tol, int maxiter_outer, void* work,
+                                size_t work_bytes, mpdok_solve_info* info, cudaStream_t stream);
+/* Three-precision GMRES-IR: the LU (BF16/FP16) preconditions FP32 GMRES on
+ * the FP32 copy of A (right preconditioning), FP64 residual r = b - A x and
+ * FP64 update x += d, FP64 Hessenberg / Givens. */
+MPDOK_API size_t mpdok_lu_gmres_ir_work_size(long long n, int restart);
+MPDOK_API int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* A32, long long lda32, long long n,
+                                const void* factors, int fdtype, const double* b, double* x, double tol,
+                                int maxiter_outer, int restart, double inner_tol, void* work, size_t work_bytes,
+                                mpdok_solve_info* info, cudaStream_t stream);
+
 /* --------------------------------------------------------- instrumentation
  * mpdok_launch_count: kernels launched by this library since load.
  * mpdok_profile_enable(1) clears and starts per-launch CUDA-event timing of
@@ -167,6 +206,20 @@ MPDOK_API void py_gmres_ir(double* A, double* b, double* x, float* A_fp32, int N
  * py_free_managed(). */
 MPDOK_API void py_alloc_managed(int N, void** ptr_out);
 MPDOK_API void py_free_managed(void);
+
+/* ------------------------------------------- reference ctypes ABI (lu_ir.so)
+ * mpdok_ops.py:101-141.  A FP64 N x N Fortran order (device or managed),
+ * b / x FP64 (x output).  py_lu_factor stores one process-wide FP32
+ * factorization (info_out: 0 ok, > 0 pivots perturbed, < 0 error);
+ * py_lu_solve_factored refines with it (converged_out = 1 / 0, -1 when no
+ * factorization of size N exists); py_lu_ir = factor + solve. */
+MPDOK_API void py_lu_ir(double* A, double* b, double* x, int N, double tol, int maxiter_outer, int* converged_out);
+MPDOK_API void py_lu_factor(double* A, int N, int* info_out);
+MPDOK_API void py_lu_solve_factored(double* A, double* b, double* x, int N, double tol, int maxiter_outer,
+                                    int* converged_out);
+MPDOK_API void py_lu_free_factored(void);
+MPDOK_API void py_lu_alloc_managed(int N, void** ptr_out);
+MPDOK_API void py_lu_free_managed(void);
 
 #ifdef __cplusplus
 }

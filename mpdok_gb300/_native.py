@@ -30,6 +30,7 @@ ERR_NONFINITE = -8
 F64, F32, BF16, F16 = 0, 1, 2, 3
 PROF_GEMV_F32, PROF_GEMV_F64, PROF_ASSEMBLE, PROF_LU_GEMM, PROF_TRSV, PROF_MATFREE, PROF_OOC_COPY, PROF_LU_PANEL = range(8)
 KERNEL_GAUSSIAN, KERNEL_MQ = 0, 1
+ENGINE_TENSOR, ENGINE_SIMT = 0, 1
 HISTORY_MAX = 256
 
 c_void_p = ctypes.c_void_p
@@ -89,6 +90,21 @@ _SIGS = {
                                      c_int, c_int, c_void_p, c_size_t, ctypes.POINTER(SolveInfo), c_void_p]),
     "mpdok_cg": (c_int, [c_void_p, c_ll, c_void_p, c_ll, c_ll, c_void_p, c_void_p, c_double, c_int, c_int,
                          c_void_p, c_size_t, ctypes.POINTER(SolveInfo), c_void_p]),
+    "mpdok_gemm_update": (c_int, [c_void_p, c_ll, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p,
+                                  c_void_p]),
+    "mpdok_lu_factor_size": (c_size_t, [c_ll, c_int]),
+    "mpdok_lu_work_size": (c_size_t, [c_ll, c_int]),
+    "mpdok_lu_factor": (c_int, [c_void_p, c_ll, c_ll, c_int, c_int, c_void_p, c_size_t, c_void_p, c_size_t,
+                                c_void_p]),
+    "mpdok_lu_apply_work_size": (c_size_t, [c_ll]),
+    "mpdok_lu_apply": (c_int, [c_void_p, c_ll, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "mpdok_lu_ir_work_size": (c_size_t, [c_ll]),
+    "mpdok_lu_ir_solve": (c_int, [c_void_p, c_ll, c_ll, c_void_p, c_int, c_void_p, c_void_p, c_double, c_int,
+                                  c_void_p, c_size_t, ctypes.POINTER(SolveInfo), c_void_p]),
+    "mpdok_lu_gmres_ir_work_size": (c_size_t, [c_ll, c_int]),
+    "mpdok_lu_gmres_ir": (c_int, [c_void_p, c_ll, c_void_p, c_ll, c_ll, c_void_p, c_int, c_void_p, c_void_p,
+                                  c_double, c_int, c_int, c_double, c_void_p, c_size_t, ctypes.POINTER(SolveInfo),
+                                  c_void_p]),
     "mpdok_launch_count": (c_ll, []),
     "mpdok_profile_enable": (c_int, [c_int]),
     "mpdok_profile_query": (c_int, [c_int, ctypes.POINTER(c_double), ctypes.POINTER(c_ll), ctypes.POINTER(c_double)]),
@@ -97,6 +113,13 @@ _SIGS = {
                            ctypes.POINTER(c_int)]),
     "py_alloc_managed": (None, [c_int, ctypes.POINTER(c_void_p)]),
     "py_free_managed": (None, []),
+    # reference ctypes ABI (lu_ir.so, mpdok_ops.py:101-141)
+    "py_lu_ir": (None, [c_void_p, c_void_p, c_void_p, c_int, c_double, c_int, ctypes.POINTER(c_int)]),
+    "py_lu_factor": (None, [c_void_p, c_int, ctypes.POINTER(c_int)]),
+    "py_lu_solve_factored": (None, [c_void_p, c_void_p, c_void_p, c_int, c_double, c_int, ctypes.POINTER(c_int)]),
+    "py_lu_free_factored": (None, []),
+    "py_lu_alloc_managed": (None, [c_int, ctypes.POINTER(c_void_p)]),
+    "py_lu_free_managed": (None, []),
 }
 
 _lib = None

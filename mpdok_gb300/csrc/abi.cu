@@ -88,3 +88,127 @@ extern "C" void py_free_managed(void) {
     st.managed = nullptr;
   }
 }
+
+// ------------------------------------------------- lu_ir.so symbols
+// mpdok_ops.py:101-141.  One process-wide saved factorization, as in the
+// reference (py_lu_factor keeps it until py_lu_free_factored).  Factors are
+// FP32 (the reference's Sgetrf precision) so that two or three refinement
+// steps reach FP64 accuracy on the systems it is documented for.
+
+namespace mpdok {
+
+struct LuAbiState {
+  void* factors = nullptr;
+  size_t factor_bytes = 0;
+  void* work = nullptr;
+  size_t work_bytes = 0;
+  long long n = -1;
+  void* managed = nullptr;
+};
+
+static LuAbiState& lu_state() {
+  static LuAbiState st;
+  return st;
+}
+
+static int ensure(void** p, size_t* have, size_t need) {
+  if (*have >= need && *p) return MPDOK_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  MPDOK_CUDA_TRY(cudaMalloc(p, need));
+  *have = need;
+  return MPDOK_OK;
+}
+
+static void lu_release(LuAbiState& st) {
+  if (st.factors) cudaFree(st.factors);
+  if (st.work) cudaFree(st.work);
+  st.factors = st.work = nullptr;
+  st.factor_bytes = st.work_bytes = 0;
+  st.n = -1;
+}
+
+static int lu_factor_global(double* A, int N) {
+  LuAbiState& st = lu_state();
+  const size_t fb = mpdok_lu_factor_size(N, MPDOK_F32);
+  const size_t wb = std::max({mpdok_lu_work_size(N, MPDOK_F32), mpdok_lu_ir_work_size(N)});
+  MPDOK_TRY(ensure(&st.factors, &st.factor_bytes, fb));
+  MPDOK_TRY(ensure(&st.work, &st.work_bytes, wb));
+  st.n = -1;
+  const int s = mpdok_lu_factor(A, N, N, MPDOK_F32, 0, st.factors, st.factor_bytes, st.work, st.work_bytes, 0);
+  if (s >= 0) st.n = N;
+  return s;
+}
+
+}  // namespace mpdok
+
+extern "C" void py_lu_factor(double* A, int N, int* info_out) {
+  std::lock_guard<std::mutex> lk(abi_state().mu);
+  int s = (N <= 0) ? 0 : lu_factor_global(A, N);
+  if (N <= 0) lu_state().n = 0;
+  if (info_out) *info_out = s;  // > 0: pivots perturbed (numerically singular), < 0: error
+}
+
+extern "C" void py_lu_solve_factored(double* A, double* b, double* x, int N, double tol, int maxiter,
+                                     int* converged_out) {
+  std::lock_guard<std::mutex> lk(abi_state().mu);
+  LuAbiState& st = lu_state();
+  if (converged_out) *converged_out = 0;
+  if (st.n < 0 || st.n != N) {
+    if (converged_out) *converged_out = -1;
+    return;
+  }
+  if (N == 0) {
+    if (converged_out) *converged_out = 1;
+    return;
+  }
+  mpdok_solve_info info;
+  int s = mpdok_lu_ir_solve(A, N, N, st.factors, MPDOK_F32, b, x, tol, maxiter, st.work, st.work_bytes, &info, 0);
+  if (s == MPDOK_OK && converged_out) *converged_out = info.converged;
+}
+
+extern "C" void py_lu_ir(double* A, double* b, double* x, int N, double tol, int maxiter, int* converged_out) {
+  int info = 0;
+  py_lu_factor(A, N, &info);
+  if (info < 0) {
+    if (converged_out) *converged_out = 0;
+    return;
+  }
+  py_lu_solve_factored(A, b, x, N, tol, maxiter, converged_out);
+}
+
+extern "C" void py_lu_free_factored(void) {
+  std::lock_guard<std::mutex> lk(abi_state().mu);
+  lu_release(lu_state());
+}
+
+extern "C" void py_lu_alloc_managed(int N, void** ptr_out) {
+  if (!ptr_out) return;
+  *ptr_out = nullptr;
+  if (N <= 0) return;
+  std::lock_guard<std::mutex> lk(abi_state().mu);
+  LuAbiState& st = lu_state();
+  if (st.managed) {
+    cudaFree(st.managed);
+    st.managed = nullptr;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMallocManaged(&p, (size_t)N * (size_t)N * sizeof(double), cudaMemAttachGlobal);
+  if (e != cudaSuccess) {
+    cuda_status(e, "py_lu_alloc_managed");
+    return;
+  }
+  st.managed = p;
+  *ptr_out = p;
+}
+
+extern "C" void py_lu_free_managed(void) {
+  std::lock_guard<std::mutex> lk(abi_state().mu);
+  LuAbiState& st = lu_state();
+  if (st.managed) {
+    cudaDeviceSynchronize();
+    cudaFree(st.managed);
+    st.managed = nullptr;
+  }
+}

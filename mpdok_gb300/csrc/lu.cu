@@ -1,0 +1,830 @@
+// Blocked LU (BF16 / FP16 tensor-core trailing update, FP32 panels), its
+// triangular-solve application, LU-IR and LU-preconditioned GMRES-IR.
+//
+// Replaces lu_ir.so of the reference (cusolverDnSgetrf / Sgetrs + cublasDgemv,
+// benchmark_mpdok.ipynb:982-993; ABI at mpdok_ops.py:101-141).
+//
+// Factorization of W = D A D, D = diag(1/sqrt|a_ii|), panel width 128, per panel:
+//   1. lu_diag:    LU of the 128 x 128 diagonal block in shared memory (FP32),
+//                  plus the inverses of its unit-lower and upper triangles;
+//   2. trsm_right: L21 = W21 U11^-1   (FP32 register-tiled, writes 16-bit L21)
+//   3. trsm_left:  U12 = L11^-1 W12   (FP32 register-tiled, writes 16-bit U12)
+//   4. W22 -= L21 U12 on tcgen05 (tc_gemm.cu), FP32 accumulation.
+// Pivots smaller than tau are perturbed to +-tau (counted and returned): the
+// factorization is used as a preconditioner / refinement solver, so an
+// approximate factor of a nearby matrix is still useful.
+//
+// Application z = D U^-1 L^-1 D v: two persistent kernels, one per triangle.
+// Row block t (128 rows) is claimed in order through an atomic ticket; it
+// accumulates L[t, j] y_j as soon as block j publishes y_j (flag + fence),
+// then multiplies by the precomputed inverse of its diagonal block.  Tickets
+// are handed out in order, so a block only ever waits on blocks that are
+// already running; every wait is bounded and reports a timeout.
+#include "krylov.cuh"
+#include "tc_gemm.cuh"
+
+#include <cmath>
+#include <cstring>
+
+namespace mpdok {
+
+constexpr int LNB = 128;          // panel width / TRSV block
+constexpr long long SPIN_LIMIT = 1LL << 24;
+
+static int fsize(int fdtype) { return fdtype == MPDOK_F32 ? 4 : 2; }
+
+struct LULayout {
+  long long n = 0, ldf = 0;
+  int nblk = 0, fdtype = MPDOK_BF16;
+  size_t off_lu = 0, off_linv = 0, off_uinv = 0, off_d = 0, off_meta = 0, total = 0;
+};
+
+struct LUMeta {
+  int n_lo, n_hi;
+  int fdtype;
+  int pivoting;
+  int nperturbed;
+  int valid;
+};
+
+static LULayout lu_layout(long long n, int fdtype) {
+  LULayout L;
+  L.n = n;
+  L.fdtype = fdtype;
+  L.ldf = (long long)align_up((size_t)std::max(1LL, n), 8);
+  L.nblk = (int)((n + LNB - 1) / LNB);
+  size_t off = 0;
+  auto take = [&](size_t b) { size_t o = off; off = align_up(off + b, 256); return o; };
+  L.off_lu = take((size_t)L.ldf * n * fsize(fdtype));
+  L.off_linv = take((size_t)L.nblk * LNB * LNB * sizeof(float));
+  L.off_uinv = take((size_t)L.nblk * LNB * LNB * sizeof(float));
+  L.off_d = take((size_t)std::max(1LL, n) * sizeof(float));
+  L.off_meta = take(sizeof(LUMeta));
+  L.total = off;
+  return L;
+}
+
+struct LUWork {
+  long long ldw = 0;
+  size_t off_W = 0, off_Lp = 0, off_Up = 0, off_err = 0, total = 0;
+};
+
+static LUWork lu_work_layout(long long n, int fdtype) {
+  LUWork w;
+  w.ldw = (long long)align_up((size_t)std::max(1LL, n), 4);
+  size_t off = 0;
+  auto take = [&](size_t b) { size_t o = off; off = align_up(off + b, 256); return o; };
+  w.off_W = take((size_t)w.ldw * n * sizeof(float));
+  w.off_Lp = take((size_t)std::max(1LL, n) * LNB * fsize(fdtype));
+  w.off_Up = take((size_t)std::max(1LL, n) * LNB * fsize(fdtype));
+  w.off_err = take(64);
+  w.total = off;
+  return w;
+}
+
+// ----------------------------------------------------------------- scaling
+__global__ void k_diag_scale(const double* __restrict__ A, long long lda, long long n, float* __restrict__ d) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double a = fabs(A[i + i * lda]);
+    d[i] = (a > 0.0 && isfinite(a)) ? (float)(1.0 / sqrt(a)) : 1.f;
+  }
+}
+
+__global__ void k_scaled_copy(const double* __restrict__ A, long long lda, long long n, const float* __restrict__ d,
+                              float* __restrict__ W, long long ldw) {
+  for (long long j = blockIdx.y; j < n; j += gridDim.y) {
+    const float dj = d[j];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+      W[i + j * ldw] = (float)A[i + j * lda] * d[i] * dj;
+  }
+}
+
+// ------------------------------------------------------- diagonal block LU
+template <typename F>
+__global__ void __launch_bounds__(256, 1)
+k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __restrict__ LU, long long ldf,
+          float* __restrict__ Linv, float* __restrict__ Uinv, int* nperturb, float tau) {
+  extern __shared__ float sm[];
+  float* T = sm;                      // [128][129]
+  float* X = sm + LNB * (LNB + 1);    // [128][129]
+  constexpr int P = LNB + 1;
+  __shared__ float s_p;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
+    const int r = idx % LNB, c = idx / LNB;
+    T[r * P + c] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
+  }
+  __syncthreads();
+  for (int j = 0; j < nbk; ++j) {
+    if (tid == 0) {
+      float p = T[j * P + j];
+      if (!(fabsf(p) >= tau)) {
+        p = (p < 0.f) ? -tau : tau;
+        atomicAdd(nperturb, 1);
+      }
+      T[j * P + j] = p;
+      s_p = p;
+    }
+    __syncthreads();
+    const float p = s_p;
+    for (int i = j + 1 + tid; i < nbk; i += blockDim.x) T[i * P + j] /= p;
+    __syncthreads();
+    const int w = nbk - j - 1;
+    for (int idx = tid; idx < w * w; idx += blockDim.x) {
+      const int i = j + 1 + idx / w, c = j + 1 + idx % w;
+      T[i * P + c] = fmaf(-T[i * P + j], T[j * P + c], T[i * P + c]);
+    }
+    __syncthreads();
+  }
+  // factor block (16-bit or FP32) into the column-major factor matrix
+  for (int idx = tid; idx < nbk * nbk; idx += blockDim.x) {
+    const int r = idx % nbk, c = idx / nbk;
+    LU[(j0 + r) + (j0 + c) * ldf] = from_f32<F>(T[r * P + c]);
+  }
+  // inverse of the unit-lower triangle, column c by thread c
+  if (tid < LNB) {
+    const int c = tid;
+    for (int i = 0; i < LNB; ++i) X[i * P + c] = (i == c) ? 1.f : 0.f;
+    for (int i = c + 1; i < LNB; ++i) {
+      float s = 0.f;
+      for (int k = c; k < i; ++k) s = fmaf(T[i * P + k], X[k * P + c], s);
+      X[i * P + c] = -s;
+    }
+  }
+  __syncthreads();
+  float* Li = Linv;
+  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
+    const int r = idx % LNB, c = idx / LNB;
+    Li[c * LNB + r] = X[r * P + c];
+  }
+  __syncthreads();
+  // inverse of the upper triangle
+  if (tid < LNB) {
+    const int c = tid;
+    for (int i = 0; i < LNB; ++i) X[i * P + c] = 0.f;
+    X[c * P + c] = 1.f / T[c * P + c];
+    for (int i = c - 1; i >= 0; --i) {
+      float s = 0.f;
+      for (int k = i + 1; k <= c; ++k) s = fmaf(T[i * P + k], X[k * P + c], s);
+      X[i * P + c] = -s / T[i * P + i];
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
+    const int r = idx % LNB, c = idx / LNB;
+    Uinv[c * LNB + r] = X[r * P + c];
+  }
+}
+
+// --------------------------------------------------------------- TRSMs
+// L21 = W21 * Uinv.  Block: 64 rows x 128 columns; thread 4 rows x 8 columns.
+template <typename F>
+__global__ void __launch_bounds__(256)
+k_trsm_right(const float* __restrict__ W, long long ldw, long long j0, long long r_begin, long long n,
+             const float* __restrict__ Uinv, F* __restrict__ Lp, F* __restrict__ LU, long long ldf) {
+  extern __shared__ float sm[];
+  constexpr int XP = LNB + 4;
+  float* Xs = sm;                 // [64][XP]   rows of W21 (then the output tile)
+  float* Ts = sm + 64 * XP;       // [128][128] Uinv row-major [k][c]
+  const int tid = threadIdx.x;
+  const long long r0 = r_begin + (long long)blockIdx.x * 64;
+  const int rows = (int)min(64LL, n - r0);
+  for (int idx = tid; idx < 64 * LNB; idx += blockDim.x) {
+    const int r = idx % 64, c = idx / 64;
+    Xs[r * XP + c] = (r < rows) ? W[(r0 + r) + (j0 + c) * ldw] : 0.f;
+  }
+  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
+    const int k = idx % LNB, c = idx / LNB;  // Uinv column-major: [c*128 + k]
+    Ts[k * LNB + c] = Uinv[c * LNB + k];
+  }
+  __syncthreads();
+  const int ty = tid / 16, tx = tid % 16;
+  float acc[4][8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < LNB; ++k) {
+    float a[4], b[8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = Xs[(ty * 4 + i) * XP + k];
+    const float4 b0 = *reinterpret_cast<const float4*>(&Ts[k * LNB + tx * 8]);
+    const float4 b1 = *reinterpret_cast<const float4*>(&Ts[k * LNB + tx * 8 + 4]);
+    b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w; b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) Xs[(ty * 4 + i) * XP + tx * 8 + j] = acc[i][j];
+  __syncthreads();
+  // K-major operand for the trailing GEMM: Lp[row][k]
+  for (int idx = tid; idx < 64 * LNB; idx += blockDim.x) {
+    const int r = idx / LNB, c = idx % LNB;
+    if (r < rows) Lp[(r0 - r_begin + r) * LNB + c] = from_f32<F>(Xs[r * XP + c]);
+  }
+  // column-major factor
+  for (int idx = tid; idx < 64 * LNB; idx += blockDim.x) {
+    const int r = idx % 64, c = idx / 64;
+    if (r < rows) LU[(r0 + r) + (j0 + c) * ldf] = from_f32<F>(Xs[r * XP + c]);
+  }
+}
+
+// U12 = Linv * W12.  Block: 128 rows x 64 columns; thread 8 rows x 4 columns.
+template <typename F>
+__global__ void __launch_bounds__(256)
+k_trsm_left(const float* __restrict__ W, long long ldw, long long j0, long long c_begin, long long n,
+            const float* __restrict__ Linv, F* __restrict__ Up, F* __restrict__ LU, long long ldf) {
+  extern __shared__ float sm[];
+  constexpr int XP = 64 + 4;
+  float* Xs = sm;                   // [128][XP]  W12 tile [k][c]
+  float* Ts = sm + LNB * XP;        // [128][LNB+1] Linv row-major [r][k]
+  constexpr int TP = LNB + 1;
+  const int tid = threadIdx.x;
+  const long long c0 = c_begin + (long long)blockIdx.x * 64;
+  const int cols = (int)min(64LL, n - c0);
+  for (int idx = tid; idx < LNB * 64; idx += blockDim.x) {
+    const int k = idx % LNB, c = idx / LNB;
+    Xs[k * XP + c] = (c < cols) ? W[(j0 + k) + (c0 + c) * ldw] : 0.f;
+  }
+  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
+    const int r = idx % LNB, k = idx / LNB;  // Linv column-major [k*128 + r]
+    Ts[r * TP + k] = Linv[k * LNB + r];
+  }
+  __syncthreads();
+  const int ty = tid / 16, tx = tid % 16;
+  float acc[8][4];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < LNB; ++k) {
+    float a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = Ts[(ty * 8 + i) * TP + k];
+    const float4 b = *reinterpret_cast<const float4*>(&Xs[k * XP + tx * 4]);
+    const float bb[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) Xs[(ty * 8 + i) * XP + tx * 4 + j] = acc[i][j];
+  __syncthreads();
+  for (int idx = tid; idx < LNB * 64; idx += blockDim.x) {
+    const int r = idx % LNB, c = idx / LNB;
+    if (c < cols) {
+      const F v = from_f32<F>(Xs[r * XP + c]);
+      Up[(c0 - c_begin + c) * LNB + r] = v;
+      LU[(j0 + r) + (c0 + c) * ldf] = v;
+    }
+  }
+}
+
+// CUDA-core trailing update for FP32 factors: C -= A B^T, A (M x 128), B (N x 128) K-major FP32.
+__global__ void __launch_bounds__(256)
+k_gemm_update_f32(float* __restrict__ C, long long ldc, const float* __restrict__ A, const float* __restrict__ B,
+                  int M, int N) {
+  __shared__ float As[16][128 + 4];
+  __shared__ float Bs[16][128 + 4];
+  const int tid = threadIdx.x;
+  const int m0 = blockIdx.x * 128, n0 = blockIdx.y * 128;
+  const int ty = tid / 16, tx = tid % 16;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  for (int kb = 0; kb < LNB; kb += 16) {
+    for (int idx = tid; idx < 16 * 128; idx += 256) {
+      const int k = idx % 16, r = idx / 16;
+      As[k][r] = (m0 + r < M) ? A[(long long)(m0 + r) * LNB + kb + k] : 0.f;
+      Bs[k][r] = (n0 + r < N) ? B[(long long)(n0 + r) * LNB + kb + k] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      float a[8], b[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) a[i] = As[k][ty * 8 + i];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) b[j] = Bs[k][tx * 8 + j];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int col = n0 + tx * 8 + j;
+    if (col >= N) continue;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int row = m0 + ty * 8 + i;
+      if (row < M) C[row + (long long)col * ldc] -= acc[i][j];
+    }
+  }
+}
+
+// ------------------------------------------------------------ TRSV (apply)
+// Lower: y = L^-1 (d .* v), L unit lower (off-diagonal blocks from LU, diagonal
+// blocks through Linv).  Upper: z = d .* (U^-1 y).
+template <typename F, bool LOWER>
+__global__ void __launch_bounds__(256)
+k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, long long n, int nblk,
+       const float* __restrict__ rhs, const float* __restrict__ dsc, float* out, int* flags, int* ticket, int* err,
+       const int* skip) {
+  __shared__ int s_t, s_abort;
+  __shared__ float s_x[LNB];
+  __shared__ float s_part[16][LNB + 1];
+  __shared__ float s_a[LNB];
+  if (skip != nullptr && *skip) return;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    s_t = atomicAdd(ticket, 1);
+    s_abort = 0;
+  }
+  __syncthreads();
+  const int tk = s_t;
+  if (tk >= nblk) return;
+  const int t = LOWER ? tk : (nblk - 1 - tk);
+  const long long r0 = (long long)t * LNB;
+  const int rows = (int)min((long long)LNB, n - r0);
+  const int rg = tid % 16, cg = tid / 16;
+  float acc[8];
+#pragma unroll
+  for (int v = 0; v < 8; ++v) acc[v] = 0.f;
+  const int jbeg = LOWER ? 0 : t + 1;
+  const int jend = LOWER ? t : nblk;
+  for (int j = jbeg; j < jend; ++j) {
+    if (tid == 0) {
+      const volatile int* f = flags + j;
+      if (!spin_until_geq(f, 1, SPIN_LIMIT)) {
+        s_abort = 1;
+        atomicExch(err, 2);
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (s_abort) return;
+    const long long c0 = (long long)j * LNB;
+    const int cols = (int)min((long long)LNB, n - c0);
+    if (tid < LNB) s_x[tid] = (tid < cols) ? __ldcg(out + c0 + tid) : 0.f;
+    __syncthreads();
+    const long long rbase = r0 + rg * 8;
+#pragma unroll 2
+    for (int cc = 0; cc < 8; ++cc) {
+      const int c = cg + 16 * cc;
+      if (c >= cols) break;
+      const F* col = LU + (c0 + c) * ldf + rbase;
+      const float xv = s_x[c];
+      if (rbase + 8 <= n && sizeof(F) == 2) {
+        uint4 raw = __ldg(reinterpret_cast<const uint4*>(col));
+        const F* h = reinterpret_cast<const F*>(&raw);
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc[v] = fmaf(to_f32<F>(h[v]), xv, acc[v]);
+      } else {
+#pragma unroll
+        for (int v = 0; v < 8; ++v)
+          if (rbase + v < n) acc[v] = fmaf(to_f32<F>(col[v]), xv, acc[v]);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int v = 0; v < 8; ++v) s_part[cg][rg * 8 + v] = acc[v];
+  __syncthreads();
+  if (tid < LNB) {
+    float s = 0.f;
+#pragma unroll
+    for (int g = 0; g < 16; ++g) s += s_part[g][tid];
+    float r = 0.f;
+    if (tid < rows) r = LOWER ? rhs[r0 + tid] * dsc[r0 + tid] : rhs[r0 + tid];
+    s_a[tid] = r - s;
+  }
+  __syncthreads();
+  const float* Di = Dinv + (long long)t * LNB * LNB;  // column-major 128 x 128
+  if (tid < LNB) {
+    float y = 0.f;
+    if (LOWER) {
+      for (int c = 0; c <= tid; ++c) y = fmaf(Di[c * LNB + tid], s_a[c], y);
+    } else {
+      for (int c = tid; c < LNB; ++c) y = fmaf(Di[c * LNB + tid], s_a[c], y);
+    }
+    if (tid < rows) {
+      if (LOWER) out[r0 + tid] = y;
+      else out[r0 + tid] = y;  // scaled by d after the whole solve
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    atomicExch(flags + t, 1);
+  }
+}
+
+__global__ void k_scale_out(const float* __restrict__ z, const float* __restrict__ d, float* __restrict__ out,
+                            long long n, const int* skip) {
+  if (skip != nullptr && *skip) return;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = z[i] * d[i];
+}
+
+// ---------------------------------------------------------------- host side
+
+static unsigned grid_for(long long n, int per = 256) {
+  long long b = (n + per - 1) / per;
+  return (unsigned)std::max(1LL, std::min(b, (long long)num_sms() * 8));
+}
+
+struct ApplyWork {
+  size_t off_y = 0, off_z = 0, off_flags = 0, off_tk = 0, off_err = 0, total = 0;
+};
+
+static ApplyWork apply_layout(long long n) {
+  ApplyWork a;
+  const int nblk = (int)((n + LNB - 1) / LNB);
+  size_t off = 0;
+  auto take = [&](size_t b) { size_t o = off; off = align_up(off + b, 256); return o; };
+  a.off_y = take((size_t)std::max(1LL, n) * sizeof(float));
+  a.off_z = take((size_t)std::max(1LL, n) * sizeof(float));
+  a.off_flags = take((size_t)2 * std::max(1, nblk) * sizeof(int));
+  a.off_tk = take(4 * sizeof(int));
+  a.off_err = take(16);
+  a.total = off;
+  return a;
+}
+
+template <typename F>
+static int lu_apply_t(const void* fbuf, long long n, int fdtype, const float* v, float* z, void* work,
+                      cudaStream_t s, const int* skip) {
+  const LULayout L = lu_layout(n, fdtype);
+  const ApplyWork aw = apply_layout(n);
+  const char* fb = (const char*)fbuf;
+  char* wb = (char*)work;
+  const F* LU = (const F*)(fb + L.off_lu);
+  const float* Linv = (const float*)(fb + L.off_linv);
+  const float* Uinv = (const float*)(fb + L.off_uinv);
+  const float* d = (const float*)(fb + L.off_d);
+  float* y = (float*)(wb + aw.off_y);
+  float* zz = (float*)(wb + aw.off_z);
+  int* flags = (int*)(wb + aw.off_flags);
+  int* tk = (int*)(wb + aw.off_tk);
+  int* err = (int*)(wb + aw.off_err);
+  MPDOK_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 2 * L.nblk, s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(tk, 0, sizeof(int) * 2, s));
+  const int slot = prof_start(MPDOK_PROF_TRSV, s);
+  launch(k_trsv<F, true>, L.nblk, 256, 0, s, LU, L.ldf, Linv, n, L.nblk, v, d, y, flags, tk, err, skip);
+  launch(k_trsv<F, false>, L.nblk, 256, 0, s, LU, L.ldf, Uinv, n, L.nblk, (const float*)y, d, zz, flags + L.nblk,
+         tk + 1, err, skip);
+  launch(k_scale_out, grid_for(n), 256, 0, s, (const float*)zz, d, z, n, skip);
+  prof_stop(slot, s, (double)n * (double)n * sizeof(F));
+  MPDOK_LAUNCH_CHECK("lu apply");
+  return MPDOK_OK;
+}
+
+int lu_apply_any(const void* fbuf, long long n, int fdtype, const float* v, float* z, void* work, cudaStream_t s,
+                 const int* skip) {
+  switch (fdtype) {
+    case MPDOK_BF16: return lu_apply_t<__nv_bfloat16>(fbuf, n, fdtype, v, z, work, s, skip);
+    case MPDOK_F16: return lu_apply_t<__half>(fbuf, n, fdtype, v, z, work, s, skip);
+    case MPDOK_F32: return lu_apply_t<float>(fbuf, n, fdtype, v, z, work, s, skip);
+    default: set_error("invalid argument: factor dtype"); return MPDOK_ERR_INVALID_ARG;
+  }
+}
+
+template <typename F>
+static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, int pivoting, void* fbuf,
+                       void* work, cudaStream_t s, int* nperturb_host) {
+  const LULayout L = lu_layout(n, fdtype);
+  const LUWork w = lu_work_layout(n, fdtype);
+  char* fb = (char*)fbuf;
+  char* wb = (char*)work;
+  F* LU = (F*)(fb + L.off_lu);
+  float* Linv = (float*)(fb + L.off_linv);
+  float* Uinv = (float*)(fb + L.off_uinv);
+  float* d = (float*)(fb + L.off_d);
+  LUMeta* meta = (LUMeta*)(fb + L.off_meta);
+  float* W = (float*)(wb + w.off_W);
+  F* Lp = (F*)(wb + w.off_Lp);
+  F* Up = (F*)(wb + w.off_Up);
+  int* errw = (int*)(wb + w.off_err);
+  MPDOK_CUDA_TRY(cudaMemsetAsync(errw, 0, 64, s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(meta, 0, sizeof(LUMeta), s));
+  launch(k_diag_scale, grid_for(n), 256, 0, s, A, lda, n, d);
+  dim3 g2((unsigned)std::min<long long>((n + 255) / 256, 16), (unsigned)std::min<long long>(n, 65535));
+  launch(k_scaled_copy, g2, 256, 0, s, A, lda, n, (const float*)d, W, w.ldw);
+  MPDOK_LAUNCH_CHECK("lu scale");
+
+  const size_t smem_diag = (size_t)2 * LNB * (LNB + 1) * sizeof(float);
+  const size_t smem_tr = (size_t)(64 * (LNB + 4) + LNB * LNB) * sizeof(float);
+  const size_t smem_tl = (size_t)(LNB * (64 + 4) + LNB * (LNB + 1)) * sizeof(float);
+  static bool attrs = false;
+  if (!attrs) {
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_right<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tr));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_right<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tr));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_right<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tr));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_left<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tl));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_left<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tl));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_left<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tl));
+    attrs = true;
+  }
+  const float tau = 1e-6f;
+  for (long long j0 = 0; j0 < n; j0 += LNB) {
+    const int k = (int)(j0 / LNB);
+    const int nbk = (int)std::min<long long>(LNB, n - j0);
+    const int ps = prof_start(MPDOK_PROF_LU_PANEL, s);
+    launch(k_lu_diag<F>, 1, 256, smem_diag, s, W, w.ldw, j0, nbk, LU, L.ldf, Linv + (size_t)k * LNB * LNB,
+           Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
+    const long long rest = n - j0 - nbk;
+    if (rest > 0) {
+      launch(k_trsm_right<F>, (unsigned)((rest + 63) / 64), 256, smem_tr, s, (const float*)W, w.ldw, j0,
+             j0 + LNB, n, (const float*)(Uinv + (size_t)k * LNB * LNB), Lp, LU, L.ldf);
+      launch(k_trsm_left<F>, (unsigned)((rest + 63) / 64), 256, smem_tl, s, (const float*)W, w.ldw, j0, j0 + LNB,
+             n, (const float*)(Linv + (size_t)k * LNB * LNB), Up, LU, L.ldf);
+    }
+    prof_stop(ps, s, 2.0 * 2.0 * (double)rest * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
+    MPDOK_LAUNCH_CHECK("lu panel");
+    if (rest > 0) {
+      float* C = W + (j0 + LNB) + (j0 + LNB) * w.ldw;
+      if (fdtype == MPDOK_F32) {
+        const int gs = prof_start(MPDOK_PROF_LU_GEMM, s);
+        dim3 gg((unsigned)((rest + 127) / 128), (unsigned)((rest + 127) / 128));
+        launch(k_gemm_update_f32, gg, 256, 0, s, C, w.ldw, (const float*)Lp, (const float*)Up, (int)rest, (int)rest);
+        prof_stop(gs, s, 2.0 * (double)rest * (double)rest * LNB);
+        MPDOK_LAUNCH_CHECK("lu gemm f32");
+      } else {
+        MPDOK_TRY(gemm_update(C, w.ldw, Lp, Up, (int)rest, (int)rest, LNB, fdtype, MPDOK_ENGINE_TENSOR, errw, s));
+      }
+    }
+  }
+  int herr[2] = {0, 0};
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(herr, errw, sizeof(herr), cudaMemcpyDeviceToHost, s));
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  if (herr[0] != 0) {
+    set_error("tensor-core update timed out waiting on an mbarrier");
+    return MPDOK_ERR_TIMEOUT;
+  }
+  LUMeta hm;
+  hm.n_lo = (int)(n & 0x7fffffff);
+  hm.n_hi = (int)(n >> 31);
+  hm.fdtype = fdtype;
+  hm.pivoting = pivoting;
+  hm.nperturbed = herr[1];
+  hm.valid = 1;
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(meta, &hm, sizeof(hm), cudaMemcpyHostToDevice, s));
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  if (nperturb_host) *nperturb_host = herr[1];
+  return MPDOK_OK;
+}
+
+static int read_meta(const void* fbuf, long long n, int fdtype, LUMeta* hm, cudaStream_t s) {
+  const LULayout L = lu_layout(n, fdtype);
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(hm, (const char*)fbuf + L.off_meta, sizeof(LUMeta), cudaMemcpyDeviceToHost, s));
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  return MPDOK_OK;
+}
+
+struct PcCtx {
+  const void* fbuf;
+  long long n;
+  int fdtype;
+  void* work;
+};
+
+static int pc_apply(void* ctx, const float* v, float* z, cudaStream_t s, const int* skip) {
+  PcCtx* c = (PcCtx*)ctx;
+  return lu_apply_any(c->fbuf, c->n, c->fdtype, v, z, c->work, s, skip);
+}
+
+__global__ void k_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+__global__ void k_add_f32_to_f64(const float* __restrict__ e, double* __restrict__ x, long long n, int assign) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] = assign ? (double)e[i] : x[i] + (double)e[i];
+}
+
+}  // namespace mpdok
+
+using namespace mpdok;
+
+extern "C" size_t mpdok_lu_factor_size(long long n, int fdtype) {
+  if (n < 0) return 0;
+  return lu_layout(n, fdtype).total;
+}
+
+extern "C" size_t mpdok_lu_work_size(long long n, int fdtype) {
+  if (n < 0) return 0;
+  return lu_work_layout(n, fdtype).total;
+}
+
+extern "C" size_t mpdok_lu_apply_work_size(long long n) {
+  if (n < 0) return 0;
+  return apply_layout(n).total;
+}
+
+extern "C" int mpdok_lu_factor(const double* A, long long lda, long long n, int fdtype, int pivoting, void* factors,
+                               size_t factor_bytes, void* work, size_t work_bytes, cudaStream_t s) {
+  MPDOK_ARG_CHECK(n >= 0, "negative n");
+  MPDOK_ARG_CHECK(fdtype == MPDOK_BF16 || fdtype == MPDOK_F16 || fdtype == MPDOK_F32, "factor dtype");
+  MPDOK_ARG_CHECK(pivoting == 0, "partial pivoting is not available in this build; use pivoting = 0");
+  if (n == 0) return MPDOK_OK;
+  MPDOK_ARG_CHECK(A && factors && work, "null pointer");
+  MPDOK_ARG_CHECK(lda >= n, "lda < n");
+  MPDOK_ARG_CHECK(factor_bytes >= lu_layout(n, fdtype).total, "factor buffer too small");
+  MPDOK_ARG_CHECK(work_bytes >= lu_work_layout(n, fdtype).total, "work buffer too small");
+  MPDOK_ARG_CHECK(n < (1LL << 31), "n too large");
+  int np = 0;
+  int st;
+  switch (fdtype) {
+    case MPDOK_BF16: st = lu_factor_t<__nv_bfloat16>(A, lda, n, fdtype, pivoting, factors, work, s, &np); break;
+    case MPDOK_F16: st = lu_factor_t<__half>(A, lda, n, fdtype, pivoting, factors, work, s, &np); break;
+    default: st = lu_factor_t<float>(A, lda, n, fdtype, pivoting, factors, work, s, &np); break;
+  }
+  if (st < 0) return st;
+  return np;
+}
+
+extern "C" int mpdok_lu_apply(const void* factors, long long n, int fdtype, const float* v, float* z, void* work,
+                              size_t work_bytes, cudaStream_t s) {
+  MPDOK_ARG_CHECK(n >= 0, "negative n");
+  if (n == 0) return MPDOK_OK;
+  MPDOK_ARG_CHECK(factors && v && z && work, "null pointer");
+  MPDOK_ARG_CHECK(work_bytes >= apply_layout(n).total, "apply work buffer too small");
+  return lu_apply_any(factors, n, fdtype, v, z, work, s, nullptr);
+}
+
+extern "C" size_t mpdok_lu_ir_work_size(long long n) {
+  if (n < 0) return 0;
+  return apply_layout(n).total + krylov_layout(n, 1, nullptr).total + 256;
+}
+
+extern "C" int mpdok_lu_ir_solve(const double* A, long long lda, long long n, const void* factors, int fdtype,
+                                 const double* b, double* x, double tol, int maxiter_outer, void* work,
+                                 size_t work_bytes, mpdok_solve_info* info, cudaStream_t s) {
+  if (info) std::memset(info, 0, sizeof(*info));
+  MPDOK_ARG_CHECK(n >= 0, "negative n");
+  if (n == 0) { if (info) info->converged = 1; return MPDOK_OK; }
+  MPDOK_ARG_CHECK(A && factors && b && x && work, "null pointer");
+  MPDOK_ARG_CHECK(work_bytes >= mpdok_lu_ir_work_size(n), "LU-IR work buffer too small");
+  LUMeta hm;
+  MPDOK_TRY(read_meta(factors, n, fdtype, &hm, s));
+  if (!hm.valid || hm.fdtype != fdtype || hm.n_lo != (int)(n & 0x7fffffff)) {
+    set_error("no factorization of this size / type in the factor buffer");
+    return MPDOK_ERR_NOT_FACTORED;
+  }
+  const ApplyWork aw = apply_layout(n);
+  char* wb = (char*)work;
+  void* awork = wb;
+  KWs ws = krylov_layout(n, 1, wb + align_up(aw.total, 256));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(ws.tickets, 0, sizeof(unsigned) * 8, s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(ws.sc, 0, sizeof(KScal), s));
+  float* v32 = ws.w;
+  float* z32 = ws.x32;
+  // bnorm
+  MPDOK_TRY(norm2_f64(ws, b, n, &ws.sc->aux, s));
+  KScal hs;
+  MPDOK_TRY(read_scal(ws, &hs, s));
+  const double bnorm = std::sqrt(hs.aux);
+  if (info) info->bnorm = bnorm;
+  if (bnorm == 0.0) {
+    MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    if (info) { info->converged = 1; info->n_history = 1; info->history[0] = 0.0; }
+    return MPDOK_OK;
+  }
+  // initial solve x = LU^-1 b
+  launch(k_f64_to_f32, grid_for(n), 256, 0, s, b, v32, n);
+  MPDOK_TRY(lu_apply_any(factors, n, fdtype, v32, z32, awork, s, nullptr));
+  launch(k_add_f32_to_f64, grid_for(n), 256, 0, s, (const float*)z32, x, n, 1);
+  bool conv = false;
+  int it = 0;
+  for (it = 0; it < maxiter_outer; ++it) {
+    MPDOK_TRY(gemv_launch(MPDOK_F64, false, A, lda, n, n, x, n, 1, ws.r64, n, -1.0, 1.0, b, n, &ws.sc->nrm2, ws.gw,
+                          ws.gbytes, s, true, nullptr));
+    MPDOK_TRY(read_scal(ws, &hs, s));
+    const double rel = std::sqrt(hs.nrm2) / bnorm;
+    if (info && info->n_history < MPDOK_HISTORY_MAX) {
+      info->hist_iter[info->n_history] = it;
+      info->history[info->n_history++] = rel;
+      info->relres = rel;
+    }
+    if (!std::isfinite(rel)) { set_error("LU-IR: non-finite residual"); return MPDOK_ERR_NONFINITE; }
+    if (rel < tol) { conv = true; break; }
+    launch(k_f64_to_f32, grid_for(n), 256, 0, s, (const double*)ws.r64, v32, n);
+    MPDOK_TRY(lu_apply_any(factors, n, fdtype, v32, z32, awork, s, nullptr));
+    launch(k_add_f32_to_f64, grid_for(n), 256, 0, s, (const float*)z32, x, n, 0);
+    if (info) info->outer_iters = it + 1;
+  }
+  if (!conv) {
+    MPDOK_TRY(gemv_launch(MPDOK_F64, false, A, lda, n, n, x, n, 1, ws.r64, n, -1.0, 1.0, b, n, &ws.sc->nrm2, ws.gw,
+                          ws.gbytes, s, true, nullptr));
+    MPDOK_TRY(read_scal(ws, &hs, s));
+    const double rel = std::sqrt(hs.nrm2) / bnorm;
+    if (info && info->n_history < MPDOK_HISTORY_MAX) {
+      info->hist_iter[info->n_history] = maxiter_outer;
+      info->history[info->n_history++] = rel;
+    }
+    if (info) info->relres = rel;
+    conv = rel < tol;
+  }
+  if (info) { info->converged = conv ? 1 : 0; info->inner_iters = it + 1; }
+  MPDOK_LAUNCH_CHECK("lu_ir");
+  return MPDOK_OK;
+}
+
+extern "C" size_t mpdok_lu_gmres_ir_work_size(long long n, int restart) {
+  if (n < 0 || restart < 1) return 0;
+  return align_up(apply_layout(n).total, 256) + align_up((size_t)std::max(1LL, n) * sizeof(float), 256) +
+         krylov_layout(n, restart, nullptr).total + 256;
+}
+
+extern "C" int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* A32, long long lda32, long long n,
+                                 const void* factors, int fdtype, const double* b, double* x, double tol,
+                                 int maxiter_outer, int restart, double inner_tol, void* work, size_t work_bytes,
+                                 mpdok_solve_info* info, cudaStream_t s) {
+  if (info) std::memset(info, 0, sizeof(*info));
+  MPDOK_ARG_CHECK(n >= 0, "negative n");
+  MPDOK_ARG_CHECK(restart >= 1 && restart <= 1024, "restart must be in [1, 1024]");
+  if (n == 0) { if (info) info->converged = 1; return MPDOK_OK; }
+  MPDOK_ARG_CHECK(A64 && A32 && factors && b && x && work, "null pointer");
+  MPDOK_ARG_CHECK(work_bytes >= mpdok_lu_gmres_ir_work_size(n, restart), "work buffer too small");
+  LUMeta hm;
+  MPDOK_TRY(read_meta(factors, n, fdtype, &hm, s));
+  if (!hm.valid || hm.fdtype != fdtype || hm.n_lo != (int)(n & 0x7fffffff)) {
+    set_error("no factorization of this size / type in the factor buffer");
+    return MPDOK_ERR_NOT_FACTORED;
+  }
+  char* wb = (char*)work;
+  const size_t a_bytes = align_up(apply_layout(n).total, 256);
+  PcCtx ctx{factors, n, fdtype, wb};
+  Precond pc;
+  pc.apply = pc_apply;
+  pc.ctx = &ctx;
+  pc.z = (float*)(wb + a_bytes);
+  KWs ws = krylov_layout(n, restart, wb + a_bytes + align_up((size_t)n * sizeof(float), 256));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(ws.tickets, 0, sizeof(unsigned) * 8, s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(ws.sc, 0, sizeof(KScal), s));
+  MPDOK_TRY(norm2_f64(ws, b, n, &ws.sc->aux, s));
+  KScal hs;
+  MPDOK_TRY(read_scal(ws, &hs, s));
+  const double bnorm = std::sqrt(hs.aux);
+  if (info) info->bnorm = bnorm;
+  if (bnorm == 0.0) {
+    MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    if (info) { info->converged = 1; info->n_history = 1; info->history[0] = 0.0; }
+    return MPDOK_OK;
+  }
+  bool conv = false;
+  int inner_total = 0;
+  for (int outer = 0; outer < maxiter_outer; ++outer) {
+    MPDOK_TRY(gemv_launch(MPDOK_F64, false, A64, lda, n, n, x, n, 1, ws.r64, n, -1.0, 1.0, b, n, &ws.sc->nrm2,
+                          ws.gw, ws.gbytes, s, true, nullptr));
+    MPDOK_TRY(read_scal(ws, &hs, s));
+    if (outer > 0) inner_total += hs.m_used;
+    const double rel = std::sqrt(hs.nrm2) / bnorm;
+    if (info && info->n_history < MPDOK_HISTORY_MAX) {
+      info->hist_iter[info->n_history] = outer;
+      info->history[info->n_history++] = rel;
+      info->relres = rel;
+    }
+    if (!std::isfinite(rel)) { set_error("GMRES-IR: non-finite residual"); return MPDOK_ERR_NONFINITE; }
+    if (rel < tol) { conv = true; break; }
+    MPDOK_TRY(cycle_start_from_f64(ws, ws.r64, s));
+    MPDOK_TRY(arnoldi_cycle(ws, A32, lda32, restart, 2, inner_tol, &pc, nullptr, x, s));
+    if (info) info->outer_iters = outer + 1;
+  }
+  if (!conv) {
+    MPDOK_TRY(gemv_launch(MPDOK_F64, false, A64, lda, n, n, x, n, 1, ws.r64, n, -1.0, 1.0, b, n, &ws.sc->nrm2,
+                          ws.gw, ws.gbytes, s, true, nullptr));
+    MPDOK_TRY(read_scal(ws, &hs, s));
+    if (maxiter_outer > 0) inner_total += hs.m_used;
+    const double rel = std::sqrt(hs.nrm2) / bnorm;
+    if (info && info->n_history < MPDOK_HISTORY_MAX) {
+      info->hist_iter[info->n_history] = maxiter_outer;
+      info->history[info->n_history++] = rel;
+    }
+    if (info) info->relres = rel;
+    conv = rel < tol;
+  }
+  if (info) { info->converged = conv ? 1 : 0; info->inner_iters = inner_total; }
+  return MPDOK_OK;
+}

@@ -1,0 +1,351 @@
+// Trailing-update GEMM of the blocked LU on the 5th-generation tensor cores.
+//
+//   C (FP32, column-major, ldc) -= A * B^T
+//   A: M x K, B: N x K, both BF16 or FP16, K-major (row pitch K elements).
+//
+// One CTA computes a 128 x 256 tile.  K (the LU panel width, a multiple of
+// 64) is staged in shared memory by TMA (cp.async.bulk.tensor, 128-byte
+// swizzle, one mbarrier with an expected-transaction count); one elected
+// thread issues tcgen05.mma (kind::f16, FP32 accumulation in tensor memory,
+// M=128, N=256, K=16 per instruction) and commits to an mbarrier; four warps
+// then read the accumulator with tcgen05.ld (32 lanes x 32 columns each),
+// and apply C -= acc with coalesced column-major read-modify-writes.
+//
+// The reference factors with cuSOLVER Sgetrf in FP32/TF32 inside lu_ir.so
+// (benchmark_mpdok.ipynb:982-993); here the O(N^3) work of the factorization
+// runs as BF16/FP16 tensor-core tiles with FP32 accumulation.
+//
+// Every mbarrier wait is bounded: on time-out the CTA records an error word,
+// skips its update, releases its tensor memory and returns.
+#include "common.cuh"
+#include "tc_gemm.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+namespace mpdok {
+
+namespace tc {
+
+constexpr int BM = 128;
+constexpr int BN = 256;
+constexpr int BK = 64;           // elements per 128-byte swizzle row
+constexpr int THREADS = 128;     // 4 warps: TMEM lane quarters 0..3
+constexpr int TMEM_COLS = 256;   // FP32 accumulator columns
+constexpr long long WAIT_LIMIT = 1LL << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  for (long long i = 0; i < WAIT_LIMIT; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (i > 64) __nanosleep(32);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// atoms 1024 bytes apart (stride byte offset), leading byte offset unused (1).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);       // start address
+  d |= (uint64_t)1 << 16;                        // leading byte offset (ignored for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                        // descriptor version (tcgen05)
+  d |= (uint64_t)2 << 61;                        // swizzle mode: 128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, A/B BF16 (1) or FP16 (0),
+// both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_f16(bool bf16, int m, int n) {
+  return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+      "}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared memory: [A: KB sub-tiles of 128x64][B: KB sub-tiles of 256x64][barriers][tmem addr]
+template <int KB>
+struct Smem {
+  static constexpr int A_SUB = BM * BK * 2;   // 16 KB
+  static constexpr int B_SUB = BN * BK * 2;   // 32 KB
+  static constexpr int A_OFF = 0;
+  static constexpr int B_OFF = KB * A_SUB;
+  static constexpr int BAR_OFF = B_OFF + KB * B_SUB;
+  static constexpr int TOTAL = BAR_OFF + 64;
+  static constexpr int ALLOC = TOTAL + 1024;  // slack for 1024-byte alignment
+};
+
+template <int KB>
+__global__ void __launch_bounds__(THREADS, 1)
+tc_gemm_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, float* C,
+               long long ldc, int M, int N, int bf16, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  using S = Smem<KB>;
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t* gbase = smem_raw + (base - raw);
+  const uint32_t bar_load = base + S::BAR_OFF;
+  const uint32_t bar_mma = base + S::BAR_OFF + 8;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + S::BAR_OFF + 16);
+  __shared__ int s_fail;
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM;
+  const int n0 = blockIdx.y * BN;
+
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    mbar_init(bar_load, 1);
+    mbar_init(bar_mma, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(bar_load, (uint32_t)(KB * (S::A_SUB + S::B_SUB)));
+#pragma unroll
+    for (int kb = 0; kb < KB; ++kb) {
+      tma_load_2d(base + S::A_OFF + kb * S::A_SUB, &tmA, bar_load, kb * BK, m0);
+      tma_load_2d(base + S::B_OFF + kb * S::B_SUB, &tmB, bar_load, kb * BK, n0);
+    }
+    if (!mbar_wait_bounded(bar_load, 0)) {
+      s_fail = 1;
+    } else {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t idesc = idesc_f16(bf16 != 0, BM, BN);
+#pragma unroll
+      for (int kb = 0; kb < KB; ++kb) {
+#pragma unroll
+        for (int k = 0; k < BK / 16; ++k) {
+          // advance 16 elements (32 bytes) inside the 128-byte swizzle row
+          const uint64_t ad = smem_desc_sw128(base + S::A_OFF + kb * S::A_SUB + k * 32);
+          const uint64_t bd = smem_desc_sw128(base + S::B_OFF + kb * S::B_SUB + k * 32);
+          mma_f16(tmem, ad, bd, idesc, (kb | k) ? 1u : 0u);
+        }
+      }
+      mma_commit(bar_mma);
+    }
+  }
+  __syncthreads();
+  bool ok = (s_fail == 0);
+  if (ok) {
+    ok = mbar_wait_bounded(bar_mma, 0);
+    if (!ok) atomicExch(&s_fail, 2);
+  }
+  __syncthreads();
+  if (s_fail == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int row = m0 + warp * 32 + lane;
+    const bool row_ok = row < M;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      float v[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (row_ok) {
+        float* cp = C + (long long)row + (long long)(n0 + c0) * ldc;
+        const int ncol = min(32, N - (n0 + c0));
+#pragma unroll
+        for (int c = 0; c < 32; ++c)
+          if (c < ncol) cp[(long long)c * ldc] -= v[c];
+      }
+    }
+  } else if (threadIdx.x == 0 && err) {
+    atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+// CUDA-core comparator with the same operand rounding (test use).
+__global__ void simt_gemm_update(const void* A, const void* B, int bf16, float* C, long long ldc, int M, int N,
+                                 int K) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= M || j >= N) return;
+  float acc = 0.f;
+  for (int k = 0; k < K; ++k) {
+    float a, b;
+    if (bf16) {
+      a = __bfloat162float(((const __nv_bfloat16*)A)[(long long)i * K + k]);
+      b = __bfloat162float(((const __nv_bfloat16*)B)[(long long)j * K + k]);
+    } else {
+      a = __half2float(((const __half*)A)[(long long)i * K + k]);
+      b = __half2float(((const __half*)B)[(long long)j * K + k]);
+    }
+    acc = fmaf(a, b, acc);
+  }
+  C[i + (long long)j * ldc] -= acc;
+}
+
+}  // namespace tc
+
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// 2-D tensor map over a K-major 16-bit operand (rows x K, row pitch K), box 64 x box_rows.
+static int make_map(CUtensorMap* map, const void* ptr, int rows, int K, int box_rows, bool bf16) {
+  auto enc = get_encode();
+  if (!enc) {
+    set_error("cuTensorMapEncodeTiled unavailable from the driver");
+    return MPDOK_ERR_UNSUPPORTED;
+  }
+  cuuint64_t gdim[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)K * 2};
+  cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                   const_cast<void*>(ptr), gdim, gstride, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return MPDOK_ERR_CUDA;
+  }
+  return MPDOK_OK;
+}
+
+template <int KB>
+static int launch_tc(const CUtensorMap& ma, const CUtensorMap& mb, float* C, long long ldc, int M, int N, int bf16,
+                     int* err, cudaStream_t s) {
+  using S = tc::Smem<KB>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(tc::tc_gemm_update<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        S::ALLOC));
+    attr_set = true;
+  }
+  dim3 grid((M + tc::BM - 1) / tc::BM, (N + tc::BN - 1) / tc::BN);
+  tc::tc_gemm_update<KB><<<grid, tc::THREADS, S::ALLOC, s>>>(ma, mb, C, ldc, M, N, bf16, err);
+  count_launch();
+  MPDOK_LAUNCH_CHECK("tc_gemm_update");
+  return MPDOK_OK;
+}
+
+int gemm_update(float* C, long long ldc, const void* A, const void* B, int M, int N, int K, int fdtype, int engine,
+                int* err, cudaStream_t s) {
+  if (M <= 0 || N <= 0 || K <= 0) return MPDOK_OK;
+  MPDOK_ARG_CHECK(fdtype == MPDOK_BF16 || fdtype == MPDOK_F16, "factor dtype must be BF16 or FP16");
+  MPDOK_ARG_CHECK(ldc >= M, "ldc < M");
+  const int bf16 = fdtype == MPDOK_BF16 ? 1 : 0;
+  const int slot = prof_start(MPDOK_PROF_LU_GEMM, s);
+  if (engine == MPDOK_ENGINE_SIMT) {
+    dim3 grid((M + 127) / 128, N);
+    launch(tc::simt_gemm_update, grid, 128, 0, s, A, B, bf16, C, ldc, M, N, K);
+    MPDOK_LAUNCH_CHECK("simt_gemm_update");
+  } else {
+    MPDOK_ARG_CHECK(K % tc::BK == 0 && K <= 256, "tensor-core update needs K in {64,128,192,256}");
+    MPDOK_ARG_CHECK(aligned16(A) && aligned16(B), "operands must be 16-byte aligned");
+    CUtensorMap ma, mb;
+    MPDOK_TRY(make_map(&ma, A, M, K, tc::BM, bf16));
+    MPDOK_TRY(make_map(&mb, B, N, K, tc::BN, bf16));
+    switch (K / tc::BK) {
+      case 1: MPDOK_TRY(launch_tc<1>(ma, mb, C, ldc, M, N, bf16, err, s)); break;
+      case 2: MPDOK_TRY(launch_tc<2>(ma, mb, C, ldc, M, N, bf16, err, s)); break;
+      case 3: MPDOK_TRY(launch_tc<3>(ma, mb, C, ldc, M, N, bf16, err, s)); break;
+      default: MPDOK_TRY(launch_tc<4>(ma, mb, C, ldc, M, N, bf16, err, s)); break;
+    }
+  }
+  prof_stop(slot, s, 2.0 * (double)M * (double)N * (double)K);
+  return MPDOK_OK;
+}
+
+}  // namespace mpdok
+
+using namespace mpdok;
+
+extern "C" int mpdok_gemm_update(float* C, long long ldc, const void* A, const void* B, int M, int N, int K,
+                                 int fdtype, int engine, int* err, cudaStream_t stream) {
+  MPDOK_ARG_CHECK(M >= 0 && N >= 0 && K >= 0, "negative size");
+  if (M == 0 || N == 0 || K == 0) return MPDOK_OK;
+  MPDOK_ARG_CHECK(C && A && B, "null pointer");
+  return gemm_update(C, ldc, A, B, M, N, K, fdtype, engine, err, stream);
+}

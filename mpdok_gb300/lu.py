@@ -1,0 +1,107 @@
+"""Blocked LU on sm_103a (BF16 / FP16 tensor-core trailing update, FP32 panels).
+
+``LUFactorization(A, dtype)`` factors W = D A D (D = diag(1/sqrt|a_ii|)) with
+128-wide FP32 panels and a tcgen05 trailing update whose operands are rounded
+to BF16 or FP16 (FP32 accumulation).  ``dtype='fp32'`` keeps FP32 operands and
+runs the update on CUDA cores (the reference's Sgetrf precision).
+
+The factorization is then used as
+* a direct refinement solver: ``solve_ir`` (LU-IR, benchmark_mpdok.ipynb:982-993),
+* a right preconditioner of FP32 GMRES inside FP64 refinement: ``gmres_ir``
+  (three-precision GMRES-IR).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _native as N
+from ._device import Workspace, as_fortran, as_vector, fortran_empty, ptr, stream_handle
+
+DTYPES = {"bf16": N.BF16, "bfloat16": N.BF16, "fp16": N.F16, "float16": N.F16, "half": N.F16,
+          "fp32": N.F32, "float32": N.F32}
+
+
+def _info(info: N.SolveInfo) -> dict:
+    return {"converged": bool(info.converged), "outer_iters": int(info.outer_iters),
+            "inner_iters": int(info.inner_iters), "relres": float(info.relres), "history": info.history_list()}
+
+
+class LUFactorization:
+    """Factors of one dense matrix, owned in a device buffer."""
+
+    def __init__(self, A, dtype: str = "fp16", pivoting: bool = False, work: Workspace | None = None):
+        if pivoting:
+            raise NotImplementedError("partial pivoting is not available in this build")
+        self.fdtype = DTYPES[dtype]
+        self.dtype = dtype
+        A64 = as_fortran(A, torch.float64)
+        self.n = n = int(A64.shape[0])
+        lib = N.load()
+        self.factors = torch.empty(max(256, lib.mpdok_lu_factor_size(n, self.fdtype)), dtype=torch.uint8,
+                                   device=A64.device)
+        ws = work or Workspace()
+        w = ws.get(lib.mpdok_lu_work_size(n, self.fdtype))
+        st = lib.mpdok_lu_factor(ptr(A64), n, n, self.fdtype, 0, ptr(self.factors), self.factors.numel(), ptr(w),
+                                 w.numel(), stream_handle())
+        N.check(st, "lu_factor")
+        self.n_perturbed = int(st)
+        self._ws = Workspace()
+
+    def apply(self, v) -> torch.Tensor:
+        """z = A^-1 v through the factors (FP32 vectors)."""
+        v32 = as_vector(v, torch.float32)
+        z = torch.empty_like(v32)
+        lib = N.load()
+        w = self._ws.get(lib.mpdok_lu_apply_work_size(self.n))
+        N.check(lib.mpdok_lu_apply(ptr(self.factors), self.n, self.fdtype, ptr(v32), ptr(z), ptr(w), w.numel(),
+                                   stream_handle()), "lu_apply")
+        return z
+
+    def solve_ir(self, A, b, tol: float = 1e-11, maxiter_outer: int = 3):
+        """LU-IR: x = LU^-1 b, then FP64 residual / correction solve / FP64 update."""
+        A64 = as_fortran(A, torch.float64)
+        b64 = as_vector(b)
+        x = torch.zeros(self.n, dtype=torch.float64, device=b64.device)
+        lib = N.load()
+        w = self._ws.get(lib.mpdok_lu_ir_work_size(self.n))
+        info = N.SolveInfo()
+        N.check(lib.mpdok_lu_ir_solve(ptr(A64), self.n, self.n, ptr(self.factors), self.fdtype, ptr(b64), ptr(x),
+                                      float(tol), int(maxiter_outer), ptr(w), w.numel(), ctypes.byref(info),
+                                      stream_handle()), "lu_ir_solve")
+        return x, _info(info)
+
+    def gmres_ir(self, A, b, A32=None, tol: float = 1e-12, maxiter_outer: int = 10, restart: int = 30,
+                 inner_tol: float = 1e-6):
+        """Three-precision GMRES-IR preconditioned by these factors."""
+        A64 = as_fortran(A, torch.float64)
+        if A32 is None:
+            A32 = fortran_empty(self.n, self.n, torch.float32)
+            N.check(N.load().mpdok_convert(ptr(A64), N.F64, ptr(A32), N.F32, self.n * self.n, stream_handle()),
+                    "convert")
+        b64 = as_vector(b)
+        x = torch.zeros(self.n, dtype=torch.float64, device=b64.device)
+        lib = N.load()
+        w = self._ws.get(lib.mpdok_lu_gmres_ir_work_size(self.n, restart))
+        info = N.SolveInfo()
+        N.check(lib.mpdok_lu_gmres_ir(ptr(A64), self.n, ptr(A32), self.n, self.n, ptr(self.factors), self.fdtype,
+                                      ptr(b64), ptr(x), float(tol), int(maxiter_outer), int(restart),
+                                      float(inner_tol), ptr(w), w.numel(), ctypes.byref(info), stream_handle()),
+                "lu_gmres_ir")
+        return x, _info(info)
+
+
+def gemm_update(C: torch.Tensor, A16: torch.Tensor, B16: torch.Tensor, engine: str = "tensor") -> torch.Tensor:
+    """C (FP32 column-major) -= A16 @ B16^T with K-major BF16/FP16 operands (the LU trailing update)."""
+    M, K = A16.shape
+    Nn = B16.shape[0]
+    fd = N.BF16 if A16.dtype == torch.bfloat16 else N.F16
+    err = torch.zeros(4, dtype=torch.int32, device=C.device)
+    N.check(N.load().mpdok_gemm_update(ptr(C), C.stride(1) if Nn > 1 else M, ptr(A16.contiguous()),
+                                       ptr(B16.contiguous()), M, Nn, K, fd,
+                                       N.ENGINE_TENSOR if engine == "tensor" else N.ENGINE_SIMT, ptr(err),
+                                       stream_handle()), "gemm_update")
+    if int(err[0].item()) != 0:
+        raise N.MPDOKError(N.ERR_TIMEOUT, "tensor-core update reported a timed-out wait")
+    return C

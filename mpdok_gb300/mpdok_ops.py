@@ -158,3 +158,101 @@ class MPDOKSolver:
                 f"Try increasing maxiter_outer or restart.",
                 RuntimeWarning, stacklevel=3)
         return x_gpu
+
+
+class LUIRSolver:
+    """LU with FP64 iterative refinement over the lu_ir.so symbols (mpdok_ops.py:69-320).
+
+    ``factor(A)`` keeps one process-wide FP32 factorization in the library
+    (blocked LU on sm_103a, panels in FP32); ``solve_factored(b)`` refines with
+    FP64 residuals; ``solve(A, b)`` does both.  For BF16 / FP16 tensor-core
+    factors use ``mpdok_gb300.lu.LUFactorization`` instead.
+    """
+
+    def __init__(self, lib_path=None):
+        self._lib = _default_lib(lib_path)
+        self._managed = None
+
+    # -- managed memory ---------------------------------------------------
+    def alloc_managed(self, N_):
+        p = ctypes.c_void_p()
+        self._lib.py_lu_alloc_managed(ctypes.c_int(N_), ctypes.byref(p))
+        if not p.value:
+            raise MemoryError(f"py_lu_alloc_managed failed for N={N_}")
+        managed = _ManagedArray(_wrap_managed(p.value, N_), self._lib.py_lu_free_managed)
+        self._managed = managed
+        return managed
+
+    def free_managed(self):
+        if self._managed is not None:
+            self._managed.free()
+            self._managed = None
+        else:
+            self._lib.py_lu_free_managed()
+
+    # -- factor once, solve many ---------------------------------------------
+    def factor(self, A):
+        A_arr = A.array if isinstance(A, _ManagedArray) else A
+        A_gpu = as_fortran(A_arr, torch.float64)
+        n = int(A_gpu.shape[0])
+        self._factored_A = A_gpu
+        self._factored_N = n
+        info = ctypes.c_int(0)
+        self._lib.py_lu_factor(ctypes.c_void_p(A_gpu.data_ptr()), ctypes.c_int(n), ctypes.byref(info))
+        torch.cuda.synchronize()
+        if info.value != 0:
+            raise RuntimeError(f"py_lu_factor failed: info={info.value}")
+
+    def solve_factored(self, b, tol=1e-11, maxiter_outer=3):
+        if not hasattr(self, "_factored_A"):
+            raise RuntimeError("Call factor(A) before solve_factored(b).")
+        A_gpu = self._factored_A
+        b_gpu = as_vector(b, torch.float64)
+        n = int(A_gpu.shape[0])
+        x_gpu = torch.zeros(n, dtype=torch.float64, device=b_gpu.device)
+        converged = ctypes.c_int(0)
+        self._lib.py_lu_solve_factored(
+            ctypes.c_void_p(A_gpu.data_ptr()), ctypes.c_void_p(b_gpu.data_ptr()), ctypes.c_void_p(x_gpu.data_ptr()),
+            ctypes.c_int(n), ctypes.c_double(tol), ctypes.c_int(maxiter_outer), ctypes.byref(converged))
+        torch.cuda.synchronize()
+        if converged.value == -1:
+            raise RuntimeError("solve_factored: no factorization available — call factor(A) first.")
+        if not converged.value:
+            warnings.warn(f"LU-IR solve_factored did not converge to tol={tol:.1e} within {maxiter_outer} outer "
+                          f"iterations.", RuntimeWarning, stacklevel=2)
+        return x_gpu
+
+    def free_factored(self):
+        self._lib.py_lu_free_factored()
+        if hasattr(self, "_factored_A"):
+            del self._factored_A
+            del self._factored_N
+
+    # -- solve ----------------------------------------------------------------
+    def solve(self, A, b, tol=1e-11, maxiter_outer=3):
+        try:
+            return self._solve(A, b, tol, maxiter_outer)
+        except torch.cuda.OutOfMemoryError:
+            A_arr = A.array if isinstance(A, _ManagedArray) else A
+            _oom_warning(A, int(A_arr.shape[0]))
+            raise
+
+    def _solve(self, A, b, tol, maxiter_outer):
+        is_managed = isinstance(A, _ManagedArray)
+        A_gpu = A.array if is_managed else as_fortran(A, torch.float64)
+        b_gpu = as_vector(b, torch.float64)
+        n = int(A_gpu.shape[0])
+        if tuple(A_gpu.shape) != (n, n):
+            raise ValueError(f"A must be square (N×N), got {tuple(A_gpu.shape)}")
+        if tuple(b_gpu.shape) != (n,):
+            raise ValueError(f"b must be (N,), got {tuple(b_gpu.shape)}")
+        x_gpu = torch.zeros(n, dtype=torch.float64, device=b_gpu.device)
+        converged = ctypes.c_int(0)
+        self._lib.py_lu_ir(ctypes.c_void_p(A_gpu.data_ptr()), ctypes.c_void_p(b_gpu.data_ptr()),
+                           ctypes.c_void_p(x_gpu.data_ptr()), ctypes.c_int(n), ctypes.c_double(tol),
+                           ctypes.c_int(maxiter_outer), ctypes.byref(converged))
+        torch.cuda.synchronize()
+        if not converged.value:
+            warnings.warn(f"LU-IR did not converge to tol={tol:.1e} within {maxiter_outer} outer iterations.",
+                          RuntimeWarning, stacklevel=3)
+        return x_gpu

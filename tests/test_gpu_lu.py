@@ -1,0 +1,130 @@
+"""GPU parity: tcgen05 trailing update, blocked LU, LU-IR and LU-preconditioned GMRES-IR."""
+import warnings
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import krylov_ref as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("dt", [torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("M,Nn,K", [(128, 256, 128), (300, 520, 128), (1000, 777, 64), (257, 1029, 256),
+                                    (129, 100, 192)])
+def test_tensor_core_update_matches_cuda_cores(dt, M, Nn, K):
+    from mpdok_gb300.lu import gemm_update
+    g = torch.Generator(device="cuda").manual_seed(M + Nn + K)
+    A = torch.randn(M, K, device="cuda", generator=g).to(dt)
+    B = torch.randn(Nn, K, device="cuda", generator=g).to(dt)
+    C0 = torch.randn(Nn, M, device="cuda", generator=g).t()  # column-major (M, Nn)
+    C_tc = gemm_update(C0.clone().t().contiguous().t(), A, B, engine="tensor")
+    C_sc = gemm_update(C0.clone().t().contiguous().t(), A, B, engine="simt")
+    ref = C0.double() - A.double() @ B.double().t()
+    torch.cuda.synchronize()
+    scale = (A.double().abs() @ B.double().abs().t()) + C0.double().abs()
+    assert torch.all((C_tc.double() - ref).abs() <= 4 * K * 6e-8 * scale + 1e-6)
+    assert torch.all((C_sc.double() - ref).abs() <= 4 * K * 6e-8 * scale + 1e-6)
+
+
+def _rbf(n, gamma, reg, seed=0, dim=2):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(0, 1, size=(n, dim))
+    return X, O.rbf_matrix(X, gamma=gamma, reg=reg), rng.standard_normal(n)
+
+
+@pytest.mark.parametrize("dtype", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("n", [128, 1000, 1100])
+def test_lu_factor_apply_inverts(dtype, n):
+    from mpdok_gb300.lu import LUFactorization
+    X, A, b = _rbf(n, 400.0, 1e-1, seed=n)
+    lu = LUFactorization(A, dtype=dtype)
+    assert lu.n_perturbed == 0
+    z = lu.apply(torch.from_numpy(b).cuda().float()).double().cpu().numpy()
+    x_true = O.fp64_solve(A, b)
+    err = np.linalg.norm(z - x_true) / np.linalg.norm(x_true)
+    kappa = np.linalg.cond(A)
+    u = {"fp32": 6e-8, "fp16": 4.9e-4, "bf16": 3.9e-3}[dtype]
+    assert err < max(1e-3, 50 * kappa * u) if dtype != "fp32" else err < 1e-4 * kappa + 1e-5
+
+
+def test_lu_apply_is_deterministic():
+    from mpdok_gb300.lu import LUFactorization
+    X, A, b = _rbf(2000, 900.0, 1e-2, seed=4)
+    lu = LUFactorization(A, dtype="fp16")
+    v = torch.from_numpy(b).cuda().float()
+    z1 = lu.apply(v)
+    z2 = lu.apply(v)
+    assert torch.equal(z1, z2)
+
+
+def test_lu_ir_solver_matches_reference(golden):
+    from mpdok_gb300.mpdok_ops import LUIRSolver
+    g = golden("dense_krylov")
+    for A in (g["A_ns"], g["A_spd"]):
+        s = LUIRSolver()
+        x = s.solve(A, g["b"], tol=1e-12, maxiter_outer=3)
+        xo, ho, co = O.lu_ir(A, g["b"], tol=1e-12, maxiter_outer=3)
+        assert co
+        assert O.relres(A, x.cpu().numpy(), g["b"]) < 1e-12
+        np.testing.assert_allclose(x.cpu().numpy(), O.fp64_solve(A, g["b"]), rtol=1e-11, atol=1e-14)
+
+
+def test_lu_ir_factor_once_solve_many():
+    from mpdok_gb300.mpdok_ops import LUIRSolver
+    X, A, _ = _rbf(1500, 2500.0, 1e-2, seed=8)
+    s = LUIRSolver()
+    s.factor(A)
+    rng = np.random.default_rng(1)
+    for _ in range(3):
+        b = rng.standard_normal(1500)
+        x = s.solve_factored(b, tol=1e-12, maxiter_outer=5)
+        assert O.relres(A, x.cpu().numpy(), b) < 1e-12
+    s.free_factored()
+    with pytest.raises(RuntimeError):
+        s.solve_factored(b)
+
+
+@pytest.mark.parametrize("dtype", ["fp16", "bf16"])
+def test_lu_gmres_ir_reaches_fp64(dtype):
+    from mpdok_gb300.lu import LUFactorization
+    X, A, b = _rbf(3000, 1600.0, 1e-2, seed=2)
+    lu = LUFactorization(A, dtype=dtype)
+    x, info = lu.gmres_ir(A, b, tol=1e-12, maxiter_outer=10, restart=30)
+    assert info["converged"]
+    xs = x.cpu().numpy()
+    rel = O.relres(A, xs, b)
+    x_lu = O.fp64_solve(A, b)
+    assert rel <= max(1e-12, 10 * O.relres(A, x_lu, b))
+    assert np.linalg.norm(xs - x_lu) / np.linalg.norm(x_lu) < 1e-9
+    assert info["inner_iters"] < 200
+
+
+def test_mixed_solver_headline_family_small():
+    from mpdok_gb300 import configs
+    from mpdok_gb300.rbf_kernel import assemble
+    from mpdok_gb300.solvers import MixedSolver
+    s = configs.headline(n=4096)
+    A = assemble(s.coords, gamma=s.gamma, reg=s.reg)
+    x, info = MixedSolver().solve(A, s.b, tol=1e-12)
+    A64 = O.rbf_matrix(s.coords, gamma=s.gamma, reg=s.reg)
+    assert info["converged"]
+    assert O.relres(A64, x.cpu().numpy(), s.b) < 1e-12
+
+
+def test_lu_not_factored_status():
+    import ctypes
+    from mpdok_gb300 import _native as N
+    lib = N.load()
+    n = 256
+    fac = torch.zeros(lib.mpdok_lu_factor_size(n, N.F16), dtype=torch.uint8, device="cuda")
+    w = torch.empty(lib.mpdok_lu_ir_work_size(n), dtype=torch.uint8, device="cuda")
+    A = torch.eye(n, dtype=torch.float64, device="cuda")
+    b = torch.ones(n, dtype=torch.float64, device="cuda")
+    x = torch.zeros_like(b)
+    info = N.SolveInfo()
+    st = lib.mpdok_lu_ir_solve(ctypes.c_void_p(A.data_ptr()), n, n, ctypes.c_void_p(fac.data_ptr()), N.F16,
+                               ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(x.data_ptr()), 1e-12, 3,
+                               ctypes.c_void_p(w.data_ptr()), w.numel(), ctypes.byref(info), None)
+    assert st == N.ERR_NOT_FACTORED
