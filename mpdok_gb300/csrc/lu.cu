@@ -100,79 +100,126 @@ __global__ void k_scaled_copy(const double* __restrict__ A, long long lda, long 
 }
 
 // ------------------------------------------------------- diagonal block LU
+// Shared memory: T (the block, then its L\U factors), XL / XU (inverses of
+// the unit-lower and upper triangles), Tmp (products of the doubling steps).
+constexpr int DP = LNB + 1;
+constexpr size_t DIAG_SMEM = (size_t)(3 * LNB * DP + 64 * 65) * sizeof(float);
+
+// Inverses by recursive doubling: the 32 x 32 diagonal blocks are inverted by
+// substitution (one warp per block, one lane per column), then
+//   [X11 0; L21 X22]^-1 off-diagonal block = -X22 L21 X11,
+//   [X11 U12; 0 X22]^-1 off-diagonal block = -X11 U12 X22,
+// for block sizes 32 and 64, each product spread over all 256 threads.
+__device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int idx = tid; idx < LNB * DP; idx += blockDim.x) { XL[idx] = 0.f; XU[idx] = 0.f; }
+  __syncthreads();
+  {
+    const int b = warp & 3;
+    const int col = b * 32 + lane;
+    if (warp < 4) {
+      XL[col * DP + col] = 1.f;
+      for (int i = col + 1; i < b * 32 + 32; ++i) {
+        float sacc = 0.f;
+        for (int k = col; k < i; ++k) sacc = fmaf(T[i * DP + k], XL[k * DP + col], sacc);
+        XL[i * DP + col] = -sacc;
+      }
+    } else {
+      XU[col * DP + col] = 1.f / T[col * DP + col];
+      for (int i = col - 1; i >= b * 32; --i) {
+        float sacc = 0.f;
+        for (int k = i + 1; k <= col; ++k) sacc = fmaf(T[i * DP + k], XU[k * DP + col], sacc);
+        XU[i * DP + col] = -sacc / T[i * DP + i];
+      }
+    }
+  }
+  __syncthreads();
+  for (int sz = 32; sz < LNB; sz *= 2) {
+    const int np = LNB / (2 * sz);
+    const int per = np * sz * sz;
+    // lower: Tmp = L21 X11 ; X21 = -X22 Tmp
+    for (int idx = tid; idx < per; idx += blockDim.x) {
+      const int pr = idx / (sz * sz), e = idx % (sz * sz), r = e / sz, c = e % sz;
+      const int R = (2 * pr + 1) * sz, C = 2 * pr * sz;
+      float a = 0.f;
+      for (int k = c; k < sz; ++k) a = fmaf(T[(R + r) * DP + C + k], XL[(C + k) * DP + C + c], a);
+      Tmp[(pr * sz + r) * 65 + c] = a;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < per; idx += blockDim.x) {
+      const int pr = idx / (sz * sz), e = idx % (sz * sz), r = e / sz, c = e % sz;
+      const int R = (2 * pr + 1) * sz, C = 2 * pr * sz;
+      float a = 0.f;
+      for (int k = 0; k <= r; ++k) a = fmaf(XL[(R + r) * DP + R + k], Tmp[(pr * sz + k) * 65 + c], a);
+      XL[(R + r) * DP + C + c] = -a;
+    }
+    __syncthreads();
+    // upper: Tmp = U12 X22 ; X12 = -X11 Tmp
+    for (int idx = tid; idx < per; idx += blockDim.x) {
+      const int pr = idx / (sz * sz), e = idx % (sz * sz), r = e / sz, c = e % sz;
+      const int R = 2 * pr * sz, C = (2 * pr + 1) * sz;
+      float a = 0.f;
+      for (int k = 0; k <= c; ++k) a = fmaf(T[(R + r) * DP + C + k], XU[(C + k) * DP + C + c], a);
+      Tmp[(pr * sz + r) * 65 + c] = a;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < per; idx += blockDim.x) {
+      const int pr = idx / (sz * sz), e = idx % (sz * sz), r = e / sz, c = e % sz;
+      const int R = 2 * pr * sz, C = (2 * pr + 1) * sz;
+      float a = 0.f;
+      for (int k = r; k < sz; ++k) a = fmaf(XU[(R + r) * DP + R + k], Tmp[(pr * sz + k) * 65 + c], a);
+      XU[(R + r) * DP + C + c] = -a;
+    }
+    __syncthreads();
+  }
+}
+
 template <typename F>
 __global__ void __launch_bounds__(256, 1)
 k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __restrict__ LU, long long ldf,
           float* __restrict__ Linv, float* __restrict__ Uinv, int* nperturb, float tau) {
   extern __shared__ float sm[];
-  float* T = sm;                      // [128][129]
-  float* X = sm + LNB * (LNB + 1);    // [128][129]
-  constexpr int P = LNB + 1;
+  float* T = sm;
+  float* XL = sm + LNB * DP;
+  float* XU = sm + 2 * LNB * DP;
+  float* Tmp = sm + 3 * LNB * DP;
   __shared__ float s_p;
   const int tid = threadIdx.x;
   for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
     const int r = idx % LNB, c = idx / LNB;
-    T[r * P + c] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
+    T[r * DP + c] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
   }
   __syncthreads();
   for (int j = 0; j < nbk; ++j) {
     if (tid == 0) {
-      float p = T[j * P + j];
+      float p = T[j * DP + j];
       if (!(fabsf(p) >= tau)) {
         p = (p < 0.f) ? -tau : tau;
         atomicAdd(nperturb, 1);
       }
-      T[j * P + j] = p;
+      T[j * DP + j] = p;
       s_p = p;
     }
     __syncthreads();
     const float p = s_p;
-    for (int i = j + 1 + tid; i < nbk; i += blockDim.x) T[i * P + j] /= p;
+    for (int i = j + 1 + tid; i < nbk; i += blockDim.x) T[i * DP + j] /= p;
     __syncthreads();
     const int w = nbk - j - 1;
     for (int idx = tid; idx < w * w; idx += blockDim.x) {
       const int i = j + 1 + idx / w, c = j + 1 + idx % w;
-      T[i * P + c] = fmaf(-T[i * P + j], T[j * P + c], T[i * P + c]);
+      T[i * DP + c] = fmaf(-T[i * DP + j], T[j * DP + c], T[i * DP + c]);
     }
     __syncthreads();
   }
-  // factor block (16-bit or FP32) into the column-major factor matrix
   for (int idx = tid; idx < nbk * nbk; idx += blockDim.x) {
     const int r = idx % nbk, c = idx / nbk;
-    LU[(j0 + r) + (j0 + c) * ldf] = from_f32<F>(T[r * P + c]);
+    LU[(j0 + r) + (j0 + c) * ldf] = from_f32<F>(T[r * DP + c]);
   }
-  // inverse of the unit-lower triangle, column c by thread c
-  if (tid < LNB) {
-    const int c = tid;
-    for (int i = 0; i < LNB; ++i) X[i * P + c] = (i == c) ? 1.f : 0.f;
-    for (int i = c + 1; i < LNB; ++i) {
-      float s = 0.f;
-      for (int k = c; k < i; ++k) s = fmaf(T[i * P + k], X[k * P + c], s);
-      X[i * P + c] = -s;
-    }
-  }
-  __syncthreads();
-  float* Li = Linv;
+  tri_inverses(T, XL, XU, Tmp);
   for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
     const int r = idx % LNB, c = idx / LNB;
-    Li[c * LNB + r] = X[r * P + c];
-  }
-  __syncthreads();
-  // inverse of the upper triangle
-  if (tid < LNB) {
-    const int c = tid;
-    for (int i = 0; i < LNB; ++i) X[i * P + c] = 0.f;
-    X[c * P + c] = 1.f / T[c * P + c];
-    for (int i = c - 1; i >= 0; --i) {
-      float s = 0.f;
-      for (int k = i + 1; k <= c; ++k) s = fmaf(T[i * P + k], X[k * P + c], s);
-      X[i * P + c] = -s / T[i * P + i];
-    }
-  }
-  __syncthreads();
-  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
-    const int r = idx % LNB, c = idx / LNB;
-    Uinv[c * LNB + r] = X[r * P + c];
+    Linv[c * LNB + r] = XL[r * DP + c];
+    Uinv[c * LNB + r] = XU[r * DP + c];
   }
 }
 
@@ -340,14 +387,85 @@ k_gemm_update_f32(float* __restrict__ C, long long ldc, const float* __restrict_
 
 // ------------------------------------------------------------ TRSV (apply)
 // Lower: y = L^-1 (d .* v), L unit lower (off-diagonal blocks from LU, diagonal
-// blocks through Linv).  Upper: z = d .* (U^-1 y).
+// blocks through Linv).  Upper: z = U^-1 y (scaled by d afterwards).
+// Block t walks the column blocks it depends on in the order they are
+// published (ascending for L, descending for U); the 128 x 8 slice of each
+// tile that a thread multiplies is loaded before waiting on that tile's flag,
+// so HBM latency overlaps the dependency chain.  The diagonal-block inverse
+// sits in shared memory from the start.
+template <typename F>
+struct TileRegs;
+template <>
+struct TileRegs<__nv_bfloat16> { uint4 r[8]; };
+template <>
+struct TileRegs<__half> { uint4 r[8]; };
+template <>
+struct TileRegs<float> { float4 r[16]; };
+
+template <typename F>
+__device__ __forceinline__ void tile_load(TileRegs<F>& T, const F* LU, long long ldf, long long c0, int cols,
+                                          long long rbase, long long n, int cg) {
+  const bool full_rows = rbase + 8 <= n;
+#pragma unroll
+  for (int cc = 0; cc < 8; ++cc) {
+    const int c = cg + 16 * cc;
+    const F* col = LU + (c0 + c) * ldf + rbase;
+    if constexpr (sizeof(F) == 2) {
+      if (c < cols && full_rows) {
+        T.r[cc] = __ldg(reinterpret_cast<const uint4*>(col));
+      } else {
+        F tmp[8];
+#pragma unroll
+        for (int v = 0; v < 8; ++v) tmp[v] = (c < cols && rbase + v < n) ? col[v] : from_f32<F>(0.f);
+        T.r[cc] = *reinterpret_cast<uint4*>(tmp);
+      }
+    } else {
+      if (c < cols && full_rows) {
+        T.r[2 * cc] = __ldg(reinterpret_cast<const float4*>(col));
+        T.r[2 * cc + 1] = __ldg(reinterpret_cast<const float4*>(col) + 1);
+      } else {
+        float tmp[8];
+#pragma unroll
+        for (int v = 0; v < 8; ++v) tmp[v] = (c < cols && rbase + v < n) ? (float)col[v] : 0.f;
+        T.r[2 * cc] = make_float4(tmp[0], tmp[1], tmp[2], tmp[3]);
+        T.r[2 * cc + 1] = make_float4(tmp[4], tmp[5], tmp[6], tmp[7]);
+      }
+    }
+  }
+}
+
+template <typename F>
+__device__ __forceinline__ void tile_fma(const TileRegs<F>& T, const float* sx, int cg, float (&acc)[8]) {
+#pragma unroll
+  for (int cc = 0; cc < 8; ++cc) {
+    const float xv = sx[cg + 16 * cc];
+    if constexpr (sizeof(F) == 2) {
+      const F* h = reinterpret_cast<const F*>(&T.r[cc]);
+#pragma unroll
+      for (int v = 0; v < 8; ++v) acc[v] = fmaf(to_f32<F>(h[v]), xv, acc[v]);
+    } else {
+      const float* f = reinterpret_cast<const float*>(&T.r[2 * cc]);
+#pragma unroll
+      for (int v = 0; v < 8; ++v) acc[v] = fmaf(f[v], xv, acc[v]);
+    }
+  }
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 template <typename F, bool LOWER>
 __global__ void __launch_bounds__(256)
 k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, long long n, int nblk,
        const float* __restrict__ rhs, const float* __restrict__ dsc, float* out, int* flags, int* ticket, int* err,
        const int* skip) {
-  __shared__ int s_t, s_abort;
-  __shared__ float s_x[LNB];
+  extern __shared__ float sDi[];      // 128 x 128 diagonal-block inverse (column-major)
+  __shared__ int s_t;
+  __shared__ int s_abort;
+  __shared__ float s_x[2][LNB];
   __shared__ float s_part[16][LNB + 1];
   __shared__ float s_a[LNB];
   if (skip != nullptr && *skip) return;
@@ -362,77 +480,64 @@ k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, 
   const int t = LOWER ? tk : (nblk - 1 - tk);
   const long long r0 = (long long)t * LNB;
   const int rows = (int)min((long long)LNB, n - r0);
+  const float* Di = Dinv + (long long)t * LNB * LNB;
+  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) sDi[idx] = __ldg(Di + idx);
   const int rg = tid % 16, cg = tid / 16;
+  const long long rbase = r0 + rg * 8;
   float acc[8];
 #pragma unroll
   for (int v = 0; v < 8; ++v) acc[v] = 0.f;
-  const int jbeg = LOWER ? 0 : t + 1;
-  const int jend = LOWER ? t : nblk;
-  for (int j = jbeg; j < jend; ++j) {
-    if (tid == 0) {
-      const volatile int* f = flags + j;
-      if (!spin_until_geq(f, 1, SPIN_LIMIT)) {
+  const int cnt = LOWER ? t : (nblk - 1 - t);
+  for (int q = 0; q < cnt; ++q) {
+    const int j = LOWER ? q : (nblk - 1 - q);
+    const long long c0 = (long long)j * LNB;
+    const int cols = (int)min((long long)LNB, n - c0);
+    TileRegs<F> T;
+    tile_load<F>(T, LU, ldf, c0, cols, rbase, n, cg);
+    if (tid < LNB) {
+      bool ok = true;
+      long long it = 0;
+      while (ld_acquire(flags + j) == 0) {
+        if (++it > SPIN_LIMIT) { ok = false; break; }
+        if (it > 256) __nanosleep(32);
+      }
+      if (!ok) {
         s_abort = 1;
         atomicExch(err, 2);
       }
-      __threadfence();
+      s_x[q & 1][tid] = (tid < cols) ? __ldcg(out + c0 + tid) : 0.f;
     }
     __syncthreads();
     if (s_abort) return;
-    const long long c0 = (long long)j * LNB;
-    const int cols = (int)min((long long)LNB, n - c0);
-    if (tid < LNB) s_x[tid] = (tid < cols) ? __ldcg(out + c0 + tid) : 0.f;
-    __syncthreads();
-    const long long rbase = r0 + rg * 8;
-#pragma unroll 2
-    for (int cc = 0; cc < 8; ++cc) {
-      const int c = cg + 16 * cc;
-      if (c >= cols) break;
-      const F* col = LU + (c0 + c) * ldf + rbase;
-      const float xv = s_x[c];
-      if (rbase + 8 <= n && sizeof(F) == 2) {
-        uint4 raw = __ldg(reinterpret_cast<const uint4*>(col));
-        const F* h = reinterpret_cast<const F*>(&raw);
-#pragma unroll
-        for (int v = 0; v < 8; ++v) acc[v] = fmaf(to_f32<F>(h[v]), xv, acc[v]);
-      } else {
-#pragma unroll
-        for (int v = 0; v < 8; ++v)
-          if (rbase + v < n) acc[v] = fmaf(to_f32<F>(col[v]), xv, acc[v]);
-      }
-    }
-    __syncthreads();
+    tile_fma<F>(T, s_x[q & 1], cg, acc);
   }
 #pragma unroll
   for (int v = 0; v < 8; ++v) s_part[cg][rg * 8 + v] = acc[v];
   __syncthreads();
   if (tid < LNB) {
-    float s = 0.f;
+    float sum = 0.f;
 #pragma unroll
-    for (int g = 0; g < 16; ++g) s += s_part[g][tid];
+    for (int g = 0; g < 16; ++g) sum += s_part[g][tid];
     float r = 0.f;
     if (tid < rows) r = LOWER ? rhs[r0 + tid] * dsc[r0 + tid] : rhs[r0 + tid];
-    s_a[tid] = r - s;
+    s_a[tid] = r - sum;
   }
   __syncthreads();
-  const float* Di = Dinv + (long long)t * LNB * LNB;  // column-major 128 x 128
   if (tid < LNB) {
     float y = 0.f;
     if (LOWER) {
-      for (int c = 0; c <= tid; ++c) y = fmaf(Di[c * LNB + tid], s_a[c], y);
+#pragma unroll 8
+      for (int c = 0; c < LNB; ++c) if (c <= tid) y = fmaf(sDi[c * LNB + tid], s_a[c], y);
     } else {
-      for (int c = tid; c < LNB; ++c) y = fmaf(Di[c * LNB + tid], s_a[c], y);
+#pragma unroll 8
+      for (int c = 0; c < LNB; ++c) if (c >= tid) y = fmaf(sDi[c * LNB + tid], s_a[c], y);
     }
-    if (tid < rows) {
-      if (LOWER) out[r0 + tid] = y;
-      else out[r0 + tid] = y;  // scaled by d after the whole solve
-    }
+    if (tid < rows) out[r0 + tid] = y;
   }
   __threadfence();
   __syncthreads();
   if (tid == 0) {
-    __threadfence();
-    atomicExch(flags + t, 1);
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(flags + t), "r"(1) : "memory");
   }
 }
 
@@ -487,9 +592,16 @@ static int lu_apply_t(const void* fbuf, long long n, int fdtype, const float* v,
   MPDOK_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 2 * L.nblk, s));
   MPDOK_CUDA_TRY(cudaMemsetAsync(tk, 0, sizeof(int) * 2, s));
   const int slot = prof_start(MPDOK_PROF_TRSV, s);
-  launch(k_trsv<F, true>, L.nblk, 256, 0, s, LU, L.ldf, Linv, n, L.nblk, v, d, y, flags, tk, err, skip);
-  launch(k_trsv<F, false>, L.nblk, 256, 0, s, LU, L.ldf, Uinv, n, L.nblk, (const float*)y, d, zz, flags + L.nblk,
-         tk + 1, err, skip);
+  const size_t smem = (size_t)LNB * LNB * sizeof(float);
+  static bool attr = false;
+  if (!attr) {
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv<F, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv<F, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  launch(k_trsv<F, true>, L.nblk, 256, smem, s, LU, L.ldf, Linv, n, L.nblk, v, d, y, flags, tk, err, skip);
+  launch(k_trsv<F, false>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, n, L.nblk, (const float*)y, d, zz,
+         flags + L.nblk, tk + 1, err, skip);
   launch(k_scale_out, grid_for(n), 256, 0, s, (const float*)zz, d, z, n, skip);
   prof_stop(slot, s, (double)n * (double)n * sizeof(F));
   MPDOK_LAUNCH_CHECK("lu apply");
@@ -529,7 +641,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   launch(k_scaled_copy, g2, 256, 0, s, A, lda, n, (const float*)d, W, w.ldw);
   MPDOK_LAUNCH_CHECK("lu scale");
 
-  const size_t smem_diag = (size_t)2 * LNB * (LNB + 1) * sizeof(float);
+  const size_t smem_diag = DIAG_SMEM;
   const size_t smem_tr = (size_t)(64 * (LNB + 4) + LNB * LNB) * sizeof(float);
   const size_t smem_tl = (size_t)(LNB * (64 + 4) + LNB * (LNB + 1)) * sizeof(float);
   static bool attrs = false;

@@ -27,17 +27,18 @@ rbf_assemble_kernel(const double* __restrict__ R, long long nr,
                     const double* __restrict__ C, long long nc,
                     double gamma, double reg, long long diag_off,
                     OutT* __restrict__ out, long long ld) {
-  __shared__ double sR[ASM_ROWS * D];
-  __shared__ double sC[ASM_COLS * D];
+  using CT = typename std::conditional<F64MATH, double, float>::type;  // coordinate type in shared memory
+  __shared__ CT sR[ASM_ROWS * D];
+  __shared__ CT sC[ASM_COLS * D];
   const long long r0 = (long long)blockIdx.x * ASM_ROWS;
   const long long c0 = (long long)blockIdx.y * ASM_COLS;
   for (int t = threadIdx.x; t < ASM_ROWS * D; t += blockDim.x) {
     long long i = r0 + t / D;
-    sR[t] = (i < nr) ? R[i * D + (t % D)] : 0.0;
+    sR[t] = (CT)((i < nr) ? R[i * D + (t % D)] : 0.0);
   }
   for (int t = threadIdx.x; t < ASM_COLS * D; t += blockDim.x) {
     long long j = c0 + t / D;
-    sC[t] = (j < nc) ? C[j * D + (t % D)] : 0.0;
+    sC[t] = (CT)((j < nc) ? C[j * D + (t % D)] : 0.0);
   }
   __syncthreads();
 
@@ -58,13 +59,13 @@ rbf_assemble_kernel(const double* __restrict__ R, long long nr,
         if (F64MATH) {
           double d2 = 0.0;
 #pragma unroll
-          for (int k = 0; k < D; ++k) { double t = sR[il * D + k] - sC[jl * D + k]; d2 = fma(t, t, d2); }
+          for (int k = 0; k < D; ++k) { double t = (double)sR[il * D + k] - (double)sC[jl * D + k]; d2 = fma(t, t, d2); }
           v = (KIND == MPDOK_KERNEL_GAUSSIAN) ? exp(-gamma * d2) : sqrt(fma(gamma, d2, 1.0));
           if (i + diag_off == j) v += reg;
         } else {
           float d2 = 0.f;
 #pragma unroll
-          for (int k = 0; k < D; ++k) { float t = (float)(sR[il * D + k] - sC[jl * D + k]); d2 = fmaf(t, t, d2); }
+          for (int k = 0; k < D; ++k) { float t = (float)sR[il * D + k] - (float)sC[jl * D + k]; d2 = fmaf(t, t, d2); }
           float vf = (KIND == MPDOK_KERNEL_GAUSSIAN) ? expf(-(float)gamma * d2) : sqrtf(fmaf((float)gamma, d2, 1.f));
           if (i + diag_off == j) vf += (float)reg;
           v = vf;
@@ -88,13 +89,13 @@ rbf_assemble_kernel(const double* __restrict__ R, long long nr,
         if (F64MATH) {
           double d2 = 0.0;
 #pragma unroll
-          for (int k = 0; k < D; ++k) { double t = sR[il * D + k] - sC[jl * D + k]; d2 = fma(t, t, d2); }
+          for (int k = 0; k < D; ++k) { double t = (double)sR[il * D + k] - (double)sC[jl * D + k]; d2 = fma(t, t, d2); }
           v = (KIND == MPDOK_KERNEL_GAUSSIAN) ? exp(-gamma * d2) : sqrt(fma(gamma, d2, 1.0));
           if (i + diag_off == j) v += reg;
         } else {
           float d2 = 0.f;
 #pragma unroll
-          for (int k = 0; k < D; ++k) { float t = (float)(sR[il * D + k] - sC[jl * D + k]); d2 = fmaf(t, t, d2); }
+          for (int k = 0; k < D; ++k) { float t = (float)sR[il * D + k] - (float)sC[jl * D + k]; d2 = fmaf(t, t, d2); }
           float vf = (KIND == MPDOK_KERNEL_GAUSSIAN) ? expf(-(float)gamma * d2) : sqrtf(fmaf((float)gamma, d2, 1.f));
           if (i + diag_off == j) vf += (float)reg;
           v = vf;

@@ -201,6 +201,20 @@ tc_gemm_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
       mma_commit(bar_mma);
     }
   }
+  // The C tile does not depend on the MMA: load its first 32-column chunk
+  // while the tensor cores run.  Loads of a chunk are issued back to back
+  // (no interleaved stores), so the chunk costs one memory round trip.
+  const int row = m0 + warp * 32 + lane;
+  const bool row_ok = row < M;
+  float* crow = C + (long long)row;
+  float cur[32];
+  auto load_chunk = [&](float (&dst)[32], int c0) {
+    const int ncol = min(32, N - (n0 + c0));
+#pragma unroll
+    for (int c = 0; c < 32; ++c)
+      dst[c] = (row_ok && c < ncol) ? __ldcg(crow + (long long)(n0 + c0 + c) * ldc) : 0.f;
+  };
+  load_chunk(cur, 0);
   __syncthreads();
   bool ok = (s_fail == 0);
   if (ok) {
@@ -210,18 +224,21 @@ tc_gemm_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   __syncthreads();
   if (s_fail == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int row = m0 + warp * 32 + lane;
-    const bool row_ok = row < M;
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 32) {
+      float nxt[32];
+      if (c0 + 32 < BN) load_chunk(nxt, c0 + 32);
       float v[32];
       tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
       if (row_ok) {
-        float* cp = C + (long long)row + (long long)(n0 + c0) * ldc;
         const int ncol = min(32, N - (n0 + c0));
 #pragma unroll
         for (int c = 0; c < 32; ++c)
-          if (c < ncol) cp[(long long)c * ldc] -= v[c];
+          if (c < ncol) __stcg(crow + (long long)(n0 + c0 + c) * ldc, cur[c] - v[c]);
+      }
+      if (c0 + 32 < BN) {
+#pragma unroll
+        for (int c = 0; c < 32; ++c) cur[c] = nxt[c];
       }
     }
   } else if (threadIdx.x == 0 && err) {
