@@ -29,6 +29,7 @@
 namespace mpdok {
 
 constexpr int LNB = 128;          // panel width / TRSV block
+constexpr int SPW = 512;          // super-panel width: K of the far trailing update
 constexpr long long SPIN_LIMIT = 1LL << 24;
 
 static int fsize(int fdtype) { return fdtype == MPDOK_F32 ? 4 : 2; }
@@ -75,8 +76,8 @@ static LUWork lu_work_layout(long long n, int fdtype) {
   size_t off = 0;
   auto take = [&](size_t b) { size_t o = off; off = align_up(off + b, 256); return o; };
   w.off_W = take((size_t)w.ldw * n * sizeof(float));
-  w.off_Lp = take((size_t)std::max(1LL, n) * LNB * fsize(fdtype));
-  w.off_Up = take((size_t)std::max(1LL, n) * LNB * fsize(fdtype));
+  w.off_Lp = take((size_t)std::max(1LL, n) * SPW * fsize(fdtype));
+  w.off_Up = take((size_t)std::max(1LL, n) * SPW * fsize(fdtype));
   w.off_err = take(64);
   w.total = off;
   return w;
@@ -183,34 +184,54 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
   float* XL = sm + LNB * DP;
   float* XU = sm + 2 * LNB * DP;
   float* Tmp = sm + 3 * LNB * DP;
-  __shared__ float s_p;
   const int tid = threadIdx.x;
   for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
     const int r = idx % LNB, c = idx / LNB;
     T[r * DP + c] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
   }
   __syncthreads();
+  // Right-looking elimination on a 16 x 16 thread grid, one barrier per
+  // column: thread (ty, tx) updates rows j+1+ty+16a and columns j+1+tx+16b.
+  // The multipliers of column j are written back after the barrier of step
+  // j, once no thread reads the original column any more.
+  const int ty = tid / 16, tx = tid % 16;
+  float lnew[8];
+  int lcol = -1;
   for (int j = 0; j < nbk; ++j) {
-    if (tid == 0) {
-      float p = T[j * DP + j];
-      if (!(fabsf(p) >= tau)) {
-        p = (p < 0.f) ? -tau : tau;
-        atomicAdd(nperturb, 1);
+    if (tx == 0 && lcol >= 0) {
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        const int i = lcol + 1 + ty + 16 * a;
+        if (i < nbk) T[i * DP + lcol] = lnew[a];
       }
+    }
+    float p = T[j * DP + j];
+    const bool pert = !(fabsf(p) >= tau);
+    if (pert) p = (p < 0.f) ? -tau : tau;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const int i = j + 1 + ty + 16 * a;
+      if (i >= nbk) break;
+      const float l = T[i * DP + j] / p;
+      lnew[a] = l;
+#pragma unroll 2
+      for (int c = j + 1 + tx; c < nbk; c += 16) T[i * DP + c] = fmaf(-l, T[j * DP + c], T[i * DP + c]);
+    }
+    lcol = j;
+    __syncthreads();
+    if (tid == 0 && pert) {
       T[j * DP + j] = p;
-      s_p = p;
+      atomicAdd(nperturb, 1);
     }
-    __syncthreads();
-    const float p = s_p;
-    for (int i = j + 1 + tid; i < nbk; i += blockDim.x) T[i * DP + j] /= p;
-    __syncthreads();
-    const int w = nbk - j - 1;
-    for (int idx = tid; idx < w * w; idx += blockDim.x) {
-      const int i = j + 1 + idx / w, c = j + 1 + idx % w;
-      T[i * DP + c] = fmaf(-T[i * DP + j], T[j * DP + c], T[i * DP + c]);
-    }
-    __syncthreads();
   }
+  if (tx == 0 && lcol >= 0) {
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const int i = lcol + 1 + ty + 16 * a;
+      if (i < nbk) T[i * DP + lcol] = lnew[a];
+    }
+  }
+  __syncthreads();
   for (int idx = tid; idx < nbk * nbk; idx += blockDim.x) {
     const int r = idx % nbk, c = idx / nbk;
     LU[(j0 + r) + (j0 + c) * ldf] = from_f32<F>(T[r * DP + c]);
@@ -228,7 +249,8 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
 template <typename F>
 __global__ void __launch_bounds__(256)
 k_trsm_right(const float* __restrict__ W, long long ldw, long long j0, long long r_begin, long long n,
-             const float* __restrict__ Uinv, F* __restrict__ Lp, F* __restrict__ LU, long long ldf) {
+             const float* __restrict__ Uinv, F* __restrict__ Lp, long long lp_pitch, long long lp_row0, int koff,
+             F* __restrict__ LU, long long ldf) {
   extern __shared__ float sm[];
   constexpr int XP = LNB + 4;
   float* Xs = sm;                 // [64][XP]   rows of W21 (then the output tile)
@@ -273,7 +295,7 @@ k_trsm_right(const float* __restrict__ W, long long ldw, long long j0, long long
   // K-major operand for the trailing GEMM: Lp[row][k]
   for (int idx = tid; idx < 64 * LNB; idx += blockDim.x) {
     const int r = idx / LNB, c = idx % LNB;
-    if (r < rows) Lp[(r0 - r_begin + r) * LNB + c] = from_f32<F>(Xs[r * XP + c]);
+    if (r < rows) Lp[(r0 - lp_row0 + r) * lp_pitch + koff + c] = from_f32<F>(Xs[r * XP + c]);
   }
   // column-major factor
   for (int idx = tid; idx < 64 * LNB; idx += blockDim.x) {
@@ -286,7 +308,8 @@ k_trsm_right(const float* __restrict__ W, long long ldw, long long j0, long long
 template <typename F>
 __global__ void __launch_bounds__(256)
 k_trsm_left(const float* __restrict__ W, long long ldw, long long j0, long long c_begin, long long n,
-            const float* __restrict__ Linv, F* __restrict__ Up, F* __restrict__ LU, long long ldf) {
+            const float* __restrict__ Linv, F* __restrict__ Up, long long up_pitch, long long up_col0, int koff,
+            F* __restrict__ LU, long long ldf) {
   extern __shared__ float sm[];
   constexpr int XP = 64 + 4;
   float* Xs = sm;                   // [128][XP]  W12 tile [k][c]
@@ -332,7 +355,7 @@ k_trsm_left(const float* __restrict__ W, long long ldw, long long j0, long long 
     const int r = idx % LNB, c = idx / LNB;
     if (c < cols) {
       const F v = from_f32<F>(Xs[r * XP + c]);
-      Up[(c0 - c_begin + c) * LNB + r] = v;
+      Up[(c0 - up_col0 + c) * up_pitch + koff + r] = v;
       LU[(j0 + r) + (c0 + c) * ldf] = v;
     }
   }
@@ -341,7 +364,7 @@ k_trsm_left(const float* __restrict__ W, long long ldw, long long j0, long long 
 // CUDA-core trailing update for FP32 factors: C -= A B^T, A (M x 128), B (N x 128) K-major FP32.
 __global__ void __launch_bounds__(256)
 k_gemm_update_f32(float* __restrict__ C, long long ldc, const float* __restrict__ A, const float* __restrict__ B,
-                  int M, int N) {
+                  long long ldk, int M, int N, int K) {
   __shared__ float As[16][128 + 4];
   __shared__ float Bs[16][128 + 4];
   const int tid = threadIdx.x;
@@ -352,11 +375,11 @@ k_gemm_update_f32(float* __restrict__ C, long long ldc, const float* __restrict_
   for (int i = 0; i < 8; ++i)
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-  for (int kb = 0; kb < LNB; kb += 16) {
+  for (int kb = 0; kb < K; kb += 16) {
     for (int idx = tid; idx < 16 * 128; idx += 256) {
       const int k = idx % 16, r = idx / 16;
-      As[k][r] = (m0 + r < M) ? A[(long long)(m0 + r) * LNB + kb + k] : 0.f;
-      Bs[k][r] = (n0 + r < N) ? B[(long long)(n0 + r) * LNB + kb + k] : 0.f;
+      As[k][r] = (m0 + r < M && kb + k < K) ? A[(long long)(m0 + r) * ldk + kb + k] : 0.f;
+      Bs[k][r] = (n0 + r < N && kb + k < K) ? B[(long long)(n0 + r) * ldk + kb + k] : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -658,32 +681,59 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     attrs = true;
   }
   const float tau = 1e-6f;
-  for (long long j0 = 0; j0 < n; j0 += LNB) {
-    const int k = (int)(j0 / LNB);
-    const int nbk = (int)std::min<long long>(LNB, n - j0);
-    const int ps = prof_start(MPDOK_PROF_LU_PANEL, s);
-    launch(k_lu_diag<F>, 1, 256, smem_diag, s, W, w.ldw, j0, nbk, LU, L.ldf, Linv + (size_t)k * LNB * LNB,
-           Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
-    const long long rest = n - j0 - nbk;
-    if (rest > 0) {
-      launch(k_trsm_right<F>, (unsigned)((rest + 63) / 64), 256, smem_tr, s, (const float*)W, w.ldw, j0,
-             j0 + LNB, n, (const float*)(Uinv + (size_t)k * LNB * LNB), Lp, LU, L.ldf);
-      launch(k_trsm_left<F>, (unsigned)((rest + 63) / 64), 256, smem_tl, s, (const float*)W, w.ldw, j0, j0 + LNB,
-             n, (const float*)(Linv + (size_t)k * LNB * LNB), Up, LU, L.ldf);
+  // C -= A B^T on one strip: A rows / B rows at the given Lp / Up offsets.
+  auto update = [&](long long crow, long long ccol, long long m, long long nn, const F* Ab, const F* Bb,
+                    int K) -> int {
+    if (m <= 0 || nn <= 0) return MPDOK_OK;
+    float* C = W + crow + ccol * w.ldw;
+    if (fdtype == MPDOK_F32) {
+      const int gs = prof_start(MPDOK_PROF_LU_GEMM, s);
+      dim3 gg((unsigned)((m + 127) / 128), (unsigned)((nn + 127) / 128));
+      launch(k_gemm_update_f32, gg, 256, 0, s, C, w.ldw, (const float*)Ab, (const float*)Bb, (long long)SPW,
+             (int)m, (int)nn, K);
+      prof_stop(gs, s, 2.0 * (double)m * (double)nn * K);
+      MPDOK_LAUNCH_CHECK("lu gemm f32");
+      return MPDOK_OK;
     }
-    prof_stop(ps, s, 2.0 * 2.0 * (double)rest * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
-    MPDOK_LAUNCH_CHECK("lu panel");
-    if (rest > 0) {
-      float* C = W + (j0 + LNB) + (j0 + LNB) * w.ldw;
-      if (fdtype == MPDOK_F32) {
-        const int gs = prof_start(MPDOK_PROF_LU_GEMM, s);
-        dim3 gg((unsigned)((rest + 127) / 128), (unsigned)((rest + 127) / 128));
-        launch(k_gemm_update_f32, gg, 256, 0, s, C, w.ldw, (const float*)Lp, (const float*)Up, (int)rest, (int)rest);
-        prof_stop(gs, s, 2.0 * (double)rest * (double)rest * LNB);
-        MPDOK_LAUNCH_CHECK("lu gemm f32");
-      } else {
-        MPDOK_TRY(gemm_update(C, w.ldw, Lp, Up, (int)rest, (int)rest, LNB, fdtype, MPDOK_ENGINE_TENSOR, errw, s));
+    return gemm_update(C, w.ldw, Ab, Bb, SPW, (int)m, (int)nn, K, fdtype, MPDOK_ENGINE_TENSOR, errw, s);
+  };
+  // Two-level right-looking LU.  Super-panel [J, Jend) of <= 512 columns is
+  // factored with 128-wide panels whose updates are confined to the
+  // super-panel's row strip (rows < Jend, all columns right of the panel) and
+  // column strip (rows >= Jend, columns < Jend); the far trailing matrix
+  // (rows, columns >= Jend) then receives all of them at once, K = 512.
+  for (long long J = 0; J < n; J += SPW) {
+    const long long Jend = std::min<long long>(n, J + SPW);
+    for (long long jp = J; jp < Jend; jp += LNB) {
+      const int k = (int)(jp / LNB);
+      const int p = (int)((jp - J) / LNB);
+      const int nbk = (int)std::min<long long>(LNB, n - jp);
+      const long long below = n - jp - nbk;
+      const int ps = prof_start(MPDOK_PROF_LU_PANEL, s);
+      launch(k_lu_diag<F>, 1, 256, smem_diag, s, W, w.ldw, jp, nbk, LU, L.ldf, Linv + (size_t)k * LNB * LNB,
+             Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
+      if (below > 0) {
+        launch(k_trsm_right<F>, (unsigned)((below + 63) / 64), 256, smem_tr, s, (const float*)W, w.ldw, jp,
+               jp + LNB, n, (const float*)(Uinv + (size_t)k * LNB * LNB), Lp, (long long)SPW, J, p * LNB, LU,
+               L.ldf);
+        launch(k_trsm_left<F>, (unsigned)((below + 63) / 64), 256, smem_tl, s, (const float*)W, w.ldw, jp, jp + LNB,
+               n, (const float*)(Linv + (size_t)k * LNB * LNB), Up, (long long)SPW, J, p * LNB, LU, L.ldf);
       }
+      prof_stop(ps, s, 2.0 * 2.0 * (double)below * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
+      MPDOK_LAUNCH_CHECK("lu panel");
+      if (below > 0) {
+        const long long r1 = jp + LNB;
+        // row strip of the super-panel: rows [r1, Jend), columns [r1, n)
+        MPDOK_TRY(update(r1, r1, Jend - r1, n - r1, Lp + (r1 - J) * SPW + p * LNB, Up + (r1 - J) * SPW + p * LNB,
+                         LNB));
+        // column strip below the super-panel: rows [Jend, n), columns [r1, Jend)
+        MPDOK_TRY(update(Jend, r1, n - Jend, Jend - r1, Lp + (Jend - J) * SPW + p * LNB,
+                         Up + (r1 - J) * SPW + p * LNB, LNB));
+      }
+    }
+    // far trailing matrix: rows and columns [Jend, n), K = Jend - J
+    if (Jend < n) {
+      MPDOK_TRY(update(Jend, Jend, n - Jend, n - Jend, Lp + (Jend - J) * SPW, Up + (Jend - J) * SPW, (int)(Jend - J)));
     }
   }
   int herr[2] = {0, 0};

@@ -129,41 +129,51 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Shared memory: [A: KB sub-tiles of 128x64][B: KB sub-tiles of 256x64][barriers][tmem addr]
-template <int KB>
+// Shared memory: STAGES x ([A 128x64][B 256x64]) ring, then barriers and the
+// tensor-memory address slot.
+template <int STAGES>
 struct Smem {
   static constexpr int A_SUB = BM * BK * 2;   // 16 KB
   static constexpr int B_SUB = BN * BK * 2;   // 32 KB
-  static constexpr int A_OFF = 0;
-  static constexpr int B_OFF = KB * A_SUB;
-  static constexpr int BAR_OFF = B_OFF + KB * B_SUB;
-  static constexpr int TOTAL = BAR_OFF + 64;
+  static constexpr int STAGE = A_SUB + B_SUB;
+  static constexpr int BAR_OFF = STAGES * STAGE;
+  static constexpr int TOTAL = BAR_OFF + 8 * (2 * STAGES + 1) + 16;
   static constexpr int ALLOC = TOTAL + 1024;  // slack for 1024-byte alignment
 };
 
-template <int KB>
+// K is consumed in 64-wide blocks through a STAGES-deep ring: lane 0 of warp 0
+// is the TMA producer (waits on empty[s], arms full[s] with the stage's bytes),
+// lane 0 of warp 1 issues the MMAs (waits on full[s], commits to empty[s]),
+// and after the last block commits to done; all four warps then drain the
+// accumulator.  The C loads of the epilogue start before the MMAs finish.
+template <int STAGES>
 __global__ void __launch_bounds__(THREADS, 1)
 tc_gemm_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, float* C,
-               long long ldc, int M, int N, int bf16, int* err) {
+               long long ldc, int M, int N, int K, int bf16, int* err) {
   extern __shared__ uint8_t smem_raw[];
-  using S = Smem<KB>;
+  using S = Smem<STAGES>;
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
   uint8_t* gbase = smem_raw + (base - raw);
-  const uint32_t bar_load = base + S::BAR_OFF;
-  const uint32_t bar_mma = base + S::BAR_OFF + 8;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + S::BAR_OFF + 16);
+  const uint32_t bar_full = base + S::BAR_OFF;
+  const uint32_t bar_empty = bar_full + 8 * STAGES;
+  const uint32_t bar_done = bar_empty + 8 * STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + S::BAR_OFF + 8 * (2 * STAGES + 1));
   __shared__ int s_fail;
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * BM;
   const int n0 = blockIdx.y * BN;
+  const int KB = K / BK;
 
   if (threadIdx.x == 0) {
     s_fail = 0;
-    mbar_init(bar_load, 1);
-    mbar_init(bar_mma, 1);
+    for (int st = 0; st < STAGES; ++st) {
+      mbar_init(bar_full + 8 * st, 1);
+      mbar_init(bar_empty + 8 * st, 1);
+    }
+    mbar_init(bar_done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -177,29 +187,41 @@ tc_gemm_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   const uint32_t tmem = *tmem_slot;
 
   if (threadIdx.x == 0) {
-    mbar_expect_tx(bar_load, (uint32_t)(KB * (S::A_SUB + S::B_SUB)));
-#pragma unroll
+    // TMA producer
     for (int kb = 0; kb < KB; ++kb) {
-      tma_load_2d(base + S::A_OFF + kb * S::A_SUB, &tmA, bar_load, kb * BK, m0);
-      tma_load_2d(base + S::B_OFF + kb * S::B_SUB, &tmB, bar_load, kb * BK, n0);
-    }
-    if (!mbar_wait_bounded(bar_load, 0)) {
-      s_fail = 1;
-    } else {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t idesc = idesc_f16(bf16 != 0, BM, BN);
-#pragma unroll
-      for (int kb = 0; kb < KB; ++kb) {
-#pragma unroll
-        for (int k = 0; k < BK / 16; ++k) {
-          // advance 16 elements (32 bytes) inside the 128-byte swizzle row
-          const uint64_t ad = smem_desc_sw128(base + S::A_OFF + kb * S::A_SUB + k * 32);
-          const uint64_t bd = smem_desc_sw128(base + S::B_OFF + kb * S::B_SUB + k * 32);
-          mma_f16(tmem, ad, bd, idesc, (kb | k) ? 1u : 0u);
-        }
+      const int st = kb % STAGES, round = kb / STAGES;
+      if (round > 0 && !mbar_wait_bounded(bar_empty + 8 * st, (round - 1) & 1)) {
+        atomicExch(&s_fail, 1);
+        break;
       }
-      mma_commit(bar_mma);
+      const uint32_t sa = base + st * S::STAGE;
+      mbar_expect_tx(bar_full + 8 * st, (uint32_t)S::STAGE);
+      tma_load_2d(sa, &tmA, bar_full + 8 * st, kb * BK, m0);
+      tma_load_2d(sa + S::A_SUB, &tmB, bar_full + 8 * st, kb * BK, n0);
     }
+  } else if (threadIdx.x == 32) {
+    // MMA issuer
+    const uint32_t idesc = idesc_f16(bf16 != 0, BM, BN);
+    bool ok = true;
+    for (int kb = 0; kb < KB && ok; ++kb) {
+      const int st = kb % STAGES, round = kb / STAGES;
+      if (!mbar_wait_bounded(bar_full + 8 * st, round & 1)) {
+        atomicExch(&s_fail, 2);
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa = base + st * S::STAGE;
+#pragma unroll
+      for (int k = 0; k < BK / 16; ++k) {
+        // advance 16 elements (32 bytes) inside the 128-byte swizzle row
+        const uint64_t ad = smem_desc_sw128(sa + k * 32);
+        const uint64_t bd = smem_desc_sw128(sa + S::A_SUB + k * 32);
+        mma_f16(tmem, ad, bd, idesc, (kb | k) ? 1u : 0u);
+      }
+      mma_commit(bar_empty + 8 * st);
+    }
+    if (ok) mma_commit(bar_done);
   }
   // The C tile does not depend on the MMA: load its first 32-column chunk
   // while the tensor cores run.  Loads of a chunk are issued back to back
@@ -216,10 +238,8 @@ tc_gemm_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   };
   load_chunk(cur, 0);
   __syncthreads();
-  bool ok = (s_fail == 0);
-  if (ok) {
-    ok = mbar_wait_bounded(bar_mma, 0);
-    if (!ok) atomicExch(&s_fail, 2);
+  if (s_fail == 0) {
+    if (!mbar_wait_bounded(bar_done, 0)) atomicExch(&s_fail, 3);
   }
   __syncthreads();
   if (s_fail == 0) {
@@ -252,8 +272,8 @@ tc_gemm_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 }
 
 // CUDA-core comparator with the same operand rounding (test use).
-__global__ void simt_gemm_update(const void* A, const void* B, int bf16, float* C, long long ldc, int M, int N,
-                                 int K) {
+__global__ void simt_gemm_update(const void* A, const void* B, long long ldk, int bf16, float* C, long long ldc,
+                                 int M, int N, int K) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= M || j >= N) return;
@@ -261,11 +281,11 @@ __global__ void simt_gemm_update(const void* A, const void* B, int bf16, float* 
   for (int k = 0; k < K; ++k) {
     float a, b;
     if (bf16) {
-      a = __bfloat162float(((const __nv_bfloat16*)A)[(long long)i * K + k]);
-      b = __bfloat162float(((const __nv_bfloat16*)B)[(long long)j * K + k]);
+      a = __bfloat162float(((const __nv_bfloat16*)A)[(long long)i * ldk + k]);
+      b = __bfloat162float(((const __nv_bfloat16*)B)[(long long)j * ldk + k]);
     } else {
-      a = __half2float(((const __half*)A)[(long long)i * K + k]);
-      b = __half2float(((const __half*)B)[(long long)j * K + k]);
+      a = __half2float(((const __half*)A)[(long long)i * ldk + k]);
+      b = __half2float(((const __half*)B)[(long long)j * ldk + k]);
     }
     acc = fmaf(a, b, acc);
   }
@@ -288,15 +308,15 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   return fn;
 }
 
-// 2-D tensor map over a K-major 16-bit operand (rows x K, row pitch K), box 64 x box_rows.
-static int make_map(CUtensorMap* map, const void* ptr, int rows, int K, int box_rows, bool bf16) {
+// 2-D tensor map over a K-major 16-bit operand (rows x K, row pitch ldk elements), box 64 x box_rows.
+static int make_map(CUtensorMap* map, const void* ptr, int rows, int K, long long ldk, int box_rows, bool bf16) {
   auto enc = get_encode();
   if (!enc) {
     set_error("cuTensorMapEncodeTiled unavailable from the driver");
     return MPDOK_ERR_UNSUPPORTED;
   }
   cuuint64_t gdim[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-  cuuint64_t gstride[1] = {(cuuint64_t)K * 2};
+  cuuint64_t gstride[1] = {(cuuint64_t)ldk * 2};
   cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = enc(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
@@ -310,46 +330,43 @@ static int make_map(CUtensorMap* map, const void* ptr, int rows, int K, int box_
   return MPDOK_OK;
 }
 
-template <int KB>
-static int launch_tc(const CUtensorMap& ma, const CUtensorMap& mb, float* C, long long ldc, int M, int N, int bf16,
-                     int* err, cudaStream_t s) {
-  using S = tc::Smem<KB>;
+constexpr int TC_STAGES = 2;
+
+static int launch_tc(const CUtensorMap& ma, const CUtensorMap& mb, float* C, long long ldc, int M, int N, int K,
+                     int bf16, int* err, cudaStream_t s) {
+  using S = tc::Smem<TC_STAGES>;
   static bool attr_set = false;
   if (!attr_set) {
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(tc::tc_gemm_update<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(tc::tc_gemm_update<TC_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         S::ALLOC));
     attr_set = true;
   }
   dim3 grid((M + tc::BM - 1) / tc::BM, (N + tc::BN - 1) / tc::BN);
-  tc::tc_gemm_update<KB><<<grid, tc::THREADS, S::ALLOC, s>>>(ma, mb, C, ldc, M, N, bf16, err);
+  tc::tc_gemm_update<TC_STAGES><<<grid, tc::THREADS, S::ALLOC, s>>>(ma, mb, C, ldc, M, N, K, bf16, err);
   count_launch();
   MPDOK_LAUNCH_CHECK("tc_gemm_update");
   return MPDOK_OK;
 }
 
-int gemm_update(float* C, long long ldc, const void* A, const void* B, int M, int N, int K, int fdtype, int engine,
-                int* err, cudaStream_t s) {
+int gemm_update(float* C, long long ldc, const void* A, const void* B, long long ldk, int M, int N, int K, int fdtype,
+                int engine, int* err, cudaStream_t s) {
   if (M <= 0 || N <= 0 || K <= 0) return MPDOK_OK;
   MPDOK_ARG_CHECK(fdtype == MPDOK_BF16 || fdtype == MPDOK_F16, "factor dtype must be BF16 or FP16");
   MPDOK_ARG_CHECK(ldc >= M, "ldc < M");
+  MPDOK_ARG_CHECK(ldk >= K, "operand pitch < K");
   const int bf16 = fdtype == MPDOK_BF16 ? 1 : 0;
   const int slot = prof_start(MPDOK_PROF_LU_GEMM, s);
   if (engine == MPDOK_ENGINE_SIMT) {
     dim3 grid((M + 127) / 128, N);
-    launch(tc::simt_gemm_update, grid, 128, 0, s, A, B, bf16, C, ldc, M, N, K);
+    launch(tc::simt_gemm_update, grid, 128, 0, s, A, B, ldk, bf16, C, ldc, M, N, K);
     MPDOK_LAUNCH_CHECK("simt_gemm_update");
   } else {
-    MPDOK_ARG_CHECK(K % tc::BK == 0 && K <= 256, "tensor-core update needs K in {64,128,192,256}");
-    MPDOK_ARG_CHECK(aligned16(A) && aligned16(B), "operands must be 16-byte aligned");
+    MPDOK_ARG_CHECK(K % tc::BK == 0, "tensor-core update needs K to be a multiple of 64");
+    MPDOK_ARG_CHECK(aligned16(A) && aligned16(B) && (ldk * 2) % 16 == 0, "operands must be 16-byte aligned");
     CUtensorMap ma, mb;
-    MPDOK_TRY(make_map(&ma, A, M, K, tc::BM, bf16));
-    MPDOK_TRY(make_map(&mb, B, N, K, tc::BN, bf16));
-    switch (K / tc::BK) {
-      case 1: MPDOK_TRY(launch_tc<1>(ma, mb, C, ldc, M, N, bf16, err, s)); break;
-      case 2: MPDOK_TRY(launch_tc<2>(ma, mb, C, ldc, M, N, bf16, err, s)); break;
-      case 3: MPDOK_TRY(launch_tc<3>(ma, mb, C, ldc, M, N, bf16, err, s)); break;
-      default: MPDOK_TRY(launch_tc<4>(ma, mb, C, ldc, M, N, bf16, err, s)); break;
-    }
+    MPDOK_TRY(make_map(&ma, A, M, K, ldk, tc::BM, bf16));
+    MPDOK_TRY(make_map(&mb, B, N, K, ldk, tc::BN, bf16));
+    MPDOK_TRY(launch_tc(ma, mb, C, ldc, M, N, K, bf16, err, s));
   }
   prof_stop(slot, s, 2.0 * (double)M * (double)N * (double)K);
   return MPDOK_OK;
@@ -364,5 +381,5 @@ extern "C" int mpdok_gemm_update(float* C, long long ldc, const void* A, const v
   MPDOK_ARG_CHECK(M >= 0 && N >= 0 && K >= 0, "negative size");
   if (M == 0 || N == 0 || K == 0) return MPDOK_OK;
   MPDOK_ARG_CHECK(C && A && B, "null pointer");
-  return gemm_update(C, ldc, A, B, M, N, K, fdtype, engine, err, stream);
+  return gemm_update(C, ldc, A, B, K, M, N, K, fdtype, engine, err, stream);
 }
