@@ -118,7 +118,9 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
   {
     const int b = warp & 3;
     const int col = b * 32 + lane;
-    if (warp < 4) {
+    if (warp >= 8) {
+      // idle during the 32 x 32 substitutions
+    } else if (warp < 4) {
       XL[col * DP + col] = 1.f;
       for (int i = col + 1; i < b * 32 + 32; ++i) {
         float sacc = 0.f;
@@ -175,8 +177,10 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
   }
 }
 
+constexpr int DIAG_THREADS = 1024;
+
 template <typename F>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(DIAG_THREADS, 1)
 k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __restrict__ LU, long long ldf,
           float* __restrict__ Linv, float* __restrict__ Uinv, int* nperturb, float tau) {
   extern __shared__ float sm[];
@@ -190,32 +194,41 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
     T[r * DP + c] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
   }
   __syncthreads();
-  // Right-looking elimination on a 16 x 16 thread grid, one barrier per
-  // column: thread (ty, tx) updates rows j+1+ty+16a and columns j+1+tx+16b.
+  // Right-looking elimination on a 32 x 32 thread grid, one barrier per
+  // column: thread (ty, tx) updates rows j+1+ty+32a and columns j+1+tx+32b.
   // The multipliers of column j are written back after the barrier of step
   // j, once no thread reads the original column any more.
-  const int ty = tid / 16, tx = tid % 16;
-  float lnew[8];
+  const int ty = tid / 32, tx = tid % 32;
+  float lnew[4];
   int lcol = -1;
   for (int j = 0; j < nbk; ++j) {
     if (tx == 0 && lcol >= 0) {
 #pragma unroll
-      for (int a = 0; a < 8; ++a) {
-        const int i = lcol + 1 + ty + 16 * a;
+      for (int a = 0; a < 4; ++a) {
+        const int i = lcol + 1 + ty + 32 * a;
         if (i < nbk) T[i * DP + lcol] = lnew[a];
       }
     }
     float p = T[j * DP + j];
     const bool pert = !(fabsf(p) >= tau);
     if (pert) p = (p < 0.f) ? -tau : tau;
+    float urow[4];
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
-      const int i = j + 1 + ty + 16 * a;
+    for (int b = 0; b < 4; ++b) {
+      const int c = j + 1 + tx + 32 * b;
+      urow[b] = (c < nbk) ? T[j * DP + c] : 0.f;
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int i = j + 1 + ty + 32 * a;
       if (i >= nbk) break;
       const float l = T[i * DP + j] / p;
       lnew[a] = l;
-#pragma unroll 2
-      for (int c = j + 1 + tx; c < nbk; c += 16) T[i * DP + c] = fmaf(-l, T[j * DP + c], T[i * DP + c]);
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int c = j + 1 + tx + 32 * b;
+        if (c < nbk) T[i * DP + c] = fmaf(-l, urow[b], T[i * DP + c]);
+      }
     }
     lcol = j;
     __syncthreads();
@@ -226,8 +239,8 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
   }
   if (tx == 0 && lcol >= 0) {
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
-      const int i = lcol + 1 + ty + 16 * a;
+    for (int a = 0; a < 4; ++a) {
+      const int i = lcol + 1 + ty + 32 * a;
       if (i < nbk) T[i * DP + lcol] = lnew[a];
     }
   }
@@ -710,7 +723,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
       const int nbk = (int)std::min<long long>(LNB, n - jp);
       const long long below = n - jp - nbk;
       const int ps = prof_start(MPDOK_PROF_LU_PANEL, s);
-      launch(k_lu_diag<F>, 1, 256, smem_diag, s, W, w.ldw, jp, nbk, LU, L.ldf, Linv + (size_t)k * LNB * LNB,
+      launch(k_lu_diag<F>, 1, DIAG_THREADS, smem_diag, s, W, w.ldw, jp, nbk, LU, L.ldf, Linv + (size_t)k * LNB * LNB,
              Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
       if (below > 0) {
         launch(k_trsm_right<F>, (unsigned)((below + 63) / 64), 256, smem_tr, s, (const float*)W, w.ldw, jp,
