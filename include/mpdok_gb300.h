@@ -94,6 +94,22 @@ MPDOK_API int mpdok_gemv(int a_dtype, int trans, const void* A, long long lda, l
                const void* X, long long ldx, int nrhs, void* Y, long long ldy, double alpha, double beta,
                void* work, size_t work_bytes, cudaStream_t stream);
 
+/* Same product as mpdok_gemv for callers that cannot allocate device memory
+ * (their GPU memory is already committed to another pool, or they must not
+ * cause the device synchronisation an allocation can bring).  No counterpart
+ * in the reference.  The scratch is a built-in device array of
+ * MPDOK_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the library until
+ * the process exits; products that need more return MPDOK_ERR_INVALID_ARG.
+ * The first call on a device looks up that array's device address (with the
+ * device current), so make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU (concurrent streams, or other host
+ * threads) race on it and must be serialised by the caller.  Nothing is
+ * allocated or freed. */
+#define MPDOK_NOALLOC_SCRATCH_BYTES (16u << 20)
+MPDOK_API int mpdok_gemv_noalloc(int a_dtype, int trans, const void* A, long long lda, long long m, long long n,
+                                 const void* X, long long ldx, int nrhs, void* Y, long long ldy, double alpha,
+                                 double beta, cudaStream_t stream);
+
 /* r = b - A x in FP64 and *rnorm2 = ||r||^2 (device scalar); workspace as
  * mpdok_gemv_workspace_size(MPDOK_F64, n, n, 1, 0).
  * Replaces DenseLinearOperator.residual_norm (dense_krylov.py:65-79). */

@@ -32,6 +32,7 @@ PROF_GEMV_F32, PROF_GEMV_F64, PROF_ASSEMBLE, PROF_LU_GEMM, PROF_TRSV, PROF_MATFR
 KERNEL_GAUSSIAN, KERNEL_MQ = 0, 1
 ENGINE_TENSOR, ENGINE_SIMT = 0, 1
 HISTORY_MAX = 256
+NOALLOC_SCRATCH_BYTES = 16 << 20
 
 c_void_p = ctypes.c_void_p
 c_int = ctypes.c_int
@@ -79,6 +80,8 @@ _SIGS = {
     "mpdok_gemv_workspace_size": (c_size_t, [c_int, c_ll, c_ll, c_int, c_int]),
     "mpdok_gemv": (c_int, [c_int, c_int, c_void_p, c_ll, c_ll, c_ll, c_void_p, c_ll, c_int, c_void_p, c_ll,
                            c_double, c_double, c_void_p, c_size_t, c_void_p]),
+    "mpdok_gemv_noalloc": (c_int, [c_int, c_int, c_void_p, c_ll, c_ll, c_ll, c_void_p, c_ll, c_int, c_void_p, c_ll,
+                                   c_double, c_double, c_void_p]),
     "mpdok_residual": (c_int, [c_void_p, c_ll, c_ll, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                                c_void_p]),
     "mpdok_krylov_workspace_size": (c_size_t, [c_ll, c_int]),

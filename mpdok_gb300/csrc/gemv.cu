@@ -15,6 +15,7 @@
 #include "gemv.cuh"
 
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 
 namespace mpdok {
@@ -345,4 +346,65 @@ extern "C" int mpdok_residual(const double* A, long long lda, long long n, const
   MPDOK_ARG_CHECK(A && b && x && r, "null pointer");
   return gemv_launch(MPDOK_F64, false, A, lda, n, n, x, n, 1, r, n, -1.0, 1.0, b, n, rnorm2, work, work_bytes,
                      stream, true, nullptr);
+}
+
+// ------------------------------------------------------------------------
+// GEMV that allocates nothing.
+//
+// Some callers cannot allocate device memory at the point where they need a
+// matrix-vector product: a host application that has already handed every
+// byte of the GPU to its own memory pool, or a caller that must not trigger
+// the device-wide synchronisation a cudaMalloc / cudaFree can cause while
+// other work is in flight.  mpdok_gemv_noalloc serves them with the same
+// kernels as mpdok_gemv, using as scratch a file-scope device array of
+// MPDOK_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+// the process exits.
+
+namespace mpdok {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MPDOK_NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device with that device current (the host-side name is only a stand-in
+// for the device array and must never be passed to a kernel).
+static int noalloc_scratch(void** out) {
+  static std::mutex mu;
+  static void* addr[64] = {};
+  int dev = 0;
+  MPDOK_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("invalid argument: device ordinal %d out of range", dev);
+    return MPDOK_ERR_INVALID_ARG;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (addr[dev] == nullptr) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return MPDOK_OK;
+}
+
+}  // namespace mpdok
+
+extern "C" int mpdok_gemv_noalloc(int a_dtype, int trans, const void* A, long long lda, long long m, long long n,
+                                  const void* X, long long ldx, int nrhs, void* Y, long long ldy, double alpha,
+                                  double beta, cudaStream_t stream) {
+  MPDOK_ARG_CHECK(A != nullptr || m == 0 || n == 0, "null A");
+  MPDOK_ARG_CHECK(m >= 0 && n >= 0 && nrhs >= 1, "bad GEMV shape");
+  const size_t need = gemv_workspace_bytes(a_dtype, m, n, nrhs, trans != 0);
+  if (need > (size_t)MPDOK_NOALLOC_SCRATCH_BYTES) {
+    set_error("invalid argument: this GEMV needs %zu bytes of scratch, more than the %u-byte built-in scratch of "
+              "mpdok_gemv_noalloc; use mpdok_gemv with a caller-owned workspace",
+              need, (unsigned)MPDOK_NOALLOC_SCRATCH_BYTES);
+    return MPDOK_ERR_INVALID_ARG;
+  }
+  void* scratch = nullptr;
+  MPDOK_TRY(noalloc_scratch(&scratch));
+  // The partial sums are written in full before they are read and no norm is
+  // requested (so the reduction ticket is unused): nothing needs clearing.
+  return gemv_launch(a_dtype, trans != 0, A, lda, m, n, X, ldx, nrhs, Y, ldy, alpha, beta, Y, ldy, nullptr, scratch,
+                     (size_t)MPDOK_NOALLOC_SCRATCH_BYTES, stream, false, nullptr);
 }
