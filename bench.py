@@ -46,6 +46,18 @@ def _peaks():
     return FALLBACK_HBM, FALLBACK_BF16, 1700.0, "fallback"
 
 
+def _traffic_model():
+    """DRAM bytes per unit of algorithmic work, from the committed ncu summary
+    (profiles/traffic.json); empty when no capture has been summarised."""
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return {}
+    return {}
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
 
@@ -117,6 +129,68 @@ def cpu_lu_sample(n_sample: int, repeats: int, config: str = "HEADLINE"):
     return d
 
 
+def gemv_standalone(n: int, warmup: int, reps: int) -> dict:
+    """Stored-matrix GEMV y = A x on (n x n) column-major FP32 / FP64 / BF16
+    operands larger than L2, timed with CUDA events on the launching stream."""
+    import ctypes
+    import torch
+    from mpdok_gb300 import _native as NV
+    lib = NV.load()
+    hbm = _peaks()[0]
+    out = {}
+    for name, code, tdt in (("f32", NV.F32, torch.float32), ("f64", NV.F64, torch.float64),
+                            ("bf16", NV.BF16, torch.bfloat16)):
+        A = torch.empty((n, n), dtype=tdt, device="cuda").normal_().t()
+        xdt = torch.float64 if name == "f64" else torch.float32
+        x = torch.randn(n, device="cuda", dtype=xdt)
+        y = torch.empty(n, device="cuda", dtype=xdt)
+        ws = torch.empty(lib.mpdok_gemv_workspace_size(code, n, n, 1, 0), dtype=torch.uint8, device="cuda")
+        args = (code, 0, ctypes.c_void_p(A.data_ptr()), n, n, n, ctypes.c_void_p(x.data_ptr()), n, 1,
+                ctypes.c_void_p(y.data_ptr()), n, 1.0, 0.0, ctypes.c_void_p(ws.data_ptr()), ws.numel(), None)
+        for _ in range(warmup):
+            NV.check(lib.mpdok_gemv(*args), "gemv")
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(reps):
+            lib.mpdok_gemv(*args)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        byts = A.element_size() * n * n + 2 * x.element_size() * n
+        out[name] = {"ms": ms, "GBs": byts / ms / 1e6, "frac_of_hbm": byts / ms / 1e6 / hbm,
+                     "bytes_per_launch": byts}
+        del A
+        torch.cuda.empty_cache()
+    # matrix-free evaluate-and-multiply on the headline centres (no stored A)
+    from mpdok_gb300 import configs
+    sysm = configs.headline(n=n)
+    coords = torch.from_numpy(sysm.coords).cuda()
+    x = torch.randn(n, device="cuda")
+    y = torch.empty(n, device="cuda")
+    ws = torch.empty(lib.mpdok_matfree_workspace_size(n, n, 1, NV.F32), dtype=torch.uint8, device="cuda")
+    args = (ctypes.c_void_p(coords.data_ptr()), n, ctypes.c_void_p(coords.data_ptr()), n, 2, NV.KERNEL_GAUSSIAN,
+            sysm.gamma, sysm.reg, 0, NV.F32, ctypes.c_void_p(x.data_ptr()), n, 1, ctypes.c_void_p(y.data_ptr()), n,
+            ctypes.c_void_p(ws.data_ptr()), ws.numel(), None)
+    for _ in range(warmup):
+        NV.check(lib.mpdok_matfree_apply(*args), "matfree")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        lib.mpdok_matfree_apply(*args)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    sfu = 16 * 152 * 2.07e9  # nominal MUFU ops/s (16 per SM per clock)
+    out["matfree_f32"] = {"ms": ms, "entries_per_s": n * n / ms * 1e3, "frac_of_nominal_sfu": n * n / ms * 1e3 / sfu,
+                          "note": "Gaussian, 2-D headline centres, entries recomputed (A never stored)"}
+    out["n"] = n
+    out["note"] = "A larger than L2 (129 MB) for n >= 8192; FP64 is bound by GB300's FP64 pipe, not HBM"
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path (SciPy FP64 LU) on rank 0."""
     rank = int(os.environ.get("RANK", "0"))
@@ -154,9 +228,16 @@ def main():
     ap.add_argument("--no-fp64-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", default="headline", choices=["headline", "gemv"],
+                    help="gemv: only the standalone stored-matrix GEMV measurement (used for kernel profiles)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only == "gemv":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps(gemv_standalone(args.n, max(3, args.warmup), max(5, args.steps))))
+        return 0
 
     import numpy as np
     import torch
@@ -227,20 +308,31 @@ def main():
     NV.profile_enable(False)
 
     hbm, bf16, bf16s, peak_kind = _peaks()
-    # dominant kernel class by device time
-    dom = max(prof.items(), key=lambda kv: kv[1][0])
-    name, (ms, cnt, work) = dom
-    if name == "lu_gemm":
-        achieved = work / (ms / 1e3) / 1e12
-        roof = {"kernel": name, "bound": "tensor", "achieved": achieved, "peak": bf16s, "unit": "TFLOP/s",
-                "frac": achieved / bf16s, "traffic": None, "launches_timed": cnt,
-                "avg_launch_ms": ms / max(1, cnt), "peak_source": f"{peak_kind} bf16 sustained"}
-    else:
-        achieved = work / (ms / 1e3) / 1e9 if ms > 0 else 0.0
-        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "launches_timed": cnt,
-                "avg_launch_ms": ms / max(1, cnt), "peak_source": f"{peak_kind} hbm copy"}
+    traffic = _traffic_model()
     share = {k: v[0] / max(1e-9, total_ms) for k, v in prof.items()}
+    rooflines = {}
+    for name, (ms, cnt, work) in prof.items():
+        if cnt == 0 or ms <= 0:
+            continue
+        if name in ("lu_gemm",):
+            ach = work / (ms / 1e3) / 1e12
+            tr = None
+            if traffic.get("lu_gemm_bytes_per_flop"):
+                tr = traffic["lu_gemm_bytes_per_flop"] * work / cnt
+            rooflines[name] = {"bound": "tensor", "achieved": ach, "peak": bf16s, "unit": "TFLOP/s",
+                               "frac": ach / bf16s, "traffic": tr, "launches": cnt, "avg_launch_ms": ms / cnt,
+                               "peak_source": f"{peak_kind} bf16 dense, sustained (kernel timed inside a long step)"}
+        elif name in ("gemv_f32", "gemv_f64", "trsv"):
+            ach = work / (ms / 1e3) / 1e9
+            tr = None
+            key = f"{name}_bytes_per_byte"
+            if traffic.get(key):
+                tr = traffic[key] * work / cnt
+            rooflines[name] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                               "traffic": tr, "launches": cnt, "avg_launch_ms": ms / cnt,
+                               "peak_source": f"{peak_kind} HBM copy"}
+    dom = max((k for k in rooflines), key=lambda k: prof[k][0]) if rooflines else None
+    roof = dict(rooflines[dom], kernel=dom) if dom else None
 
     # accuracy of the timed solves
     xs = x
@@ -282,6 +374,8 @@ def main():
         except Exception as e:  # noqa: BLE001
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {e}"}
 
+    gemv_sa = gemv_standalone(n, 3, 10) if rank == 0 else None
+
     line = {
         "metric": HEADLINE_METRIC, "value": per_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_s * 1e3, "higher_is_better": False, "scaling": "weak",
@@ -291,7 +385,9 @@ def main():
                    "l2": "inputs larger than L2 (A64 8.6 GB, A32 4.3 GB)", "parallelism": f"replicas x{world}",
                    "solver": solver.describe(), "assembly_s": t_asm},
         "relres": relres, "solve_info": infos[-1], "fp64_gpu_baseline": fp64,
-        "roofline": roof, "kernel_time_share": share, "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roof, "gemv_roofline": rooflines.get("gemv_f32"), "gemv_standalone": gemv_sa,
+        "rooflines": rooflines,
+        "kernel_time_share": share, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": ck,
     }
     if rank == 0:

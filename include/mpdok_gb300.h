@@ -153,6 +153,30 @@ MPDOK_API int mpdok_cg(const float* A32, long long lda32, const double* A64, lon
              const double* b, double* x, double tol, int maxiter, int check_every, void* work,
              size_t work_bytes, mpdok_solve_info* info, cudaStream_t stream);
 
+/* -------------------------------------------------- matrix-free RBF operator
+ * Y = K(rows, cols) X + reg X[diag_offset:] where K(i, j) = phi(||r_i - c_j||),
+ * recomputed on the fly (A never stored): FP32 (X, Y float; column tiles
+ * staged by TMA, exp2 / rsqrt on the special-function pipe) or FP64 (X, Y
+ * double; residual accuracy).  Replaces mpdok_ooc.py:205-227 (matrix-free
+ * FP64 residual) and the stored FP32 operator of the inner solves.
+ * FP32 X must be 16-byte aligned with ldx % 4 == 0.  nrhs in 1..8. */
+MPDOK_API size_t mpdok_matfree_workspace_size(long long n_rows, long long n_cols, int nrhs, int precision);
+MPDOK_API int mpdok_matfree_apply(const double* rows, long long n_rows, const double* cols, long long n_cols, int dim,
+                                  int kernel, double gamma, double reg, long long diag_offset, int precision,
+                                  const void* X, long long ldx, int nrhs, void* Y, long long ldy, void* work,
+                                  size_t work_bytes, cudaStream_t stream);
+/* GMRES-IR (inner tol, restart as mpdok_gmres_ir) and CG (as mpdok_cg) on the
+ * matrix-free operator of one RBF system (coords (n, dim) FP64): FP32
+ * evaluate-and-multiply inside, FP64 evaluate-and-multiply residuals. */
+MPDOK_API size_t mpdok_mf_krylov_workspace_size(long long n, int restart);
+MPDOK_API int mpdok_mf_gmres_ir(const double* coords, long long n, int dim, int kernel, double gamma, double reg,
+                                const double* b, double* x, double tol, int maxiter_outer, int restart,
+                                double inner_tol, void* work, size_t work_bytes, mpdok_solve_info* info,
+                                cudaStream_t stream);
+MPDOK_API int mpdok_mf_cg(const double* coords, long long n, int dim, int kernel, double gamma, double reg,
+                          const double* b, double* x, double tol, int maxiter, int check_every, void* work,
+                          size_t work_bytes, mpdok_solve_info* info, cudaStream_t stream);
+
 /* ----------------------------------------------------------- LU (tensor cores)
  * Blocked right-looking LU of W = D A D (D = diag(1/sqrt|a_ii|), panel 128)
  * with FP32 panels and a trailing update W22 -= L21 U12 whose operands are

@@ -269,6 +269,22 @@ k_norm2(const T* __restrict__ x, long long n, double* parts, unsigned* ticket, d
   ordered_grid_sum(block_sum(sq, red), parts, ticket, out);
 }
 
+// nrm2[c] = ||r[:, c]||^2, one block per column (fixed reduction order).
+__global__ void __launch_bounds__(KT) k_colnorms(const double* __restrict__ r, long long n, double* nrm2) {
+  __shared__ double red[32];
+  const double* col = r + (long long)blockIdx.x * n;
+  double s = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) s = fma(col[i], col[i], s);
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) nrm2[blockIdx.x] = s;
+}
+
+// w = b - w (the FP32 residual of a GMRES restart)
+__global__ void k_sub_from(const float* __restrict__ b, float* __restrict__ w, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    w[i] = b[i] - w[i];
+}
+
 __global__ void k_axpy_f64(const double* __restrict__ e, double* __restrict__ x, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     x[i] += e[i];
@@ -357,6 +373,12 @@ __global__ void k_set_rs(KScal* sc) {
 
 // ------------------------------------------------------------------ host side
 
+int colnorms_f64(const double* r, long long n, int nrhs, double* nrm2, cudaStream_t s) {
+  launch(k_colnorms, nrhs, KT, 0, s, r, n, nrm2);
+  MPDOK_LAUNCH_CHECK("colnorms");
+  return MPDOK_OK;
+}
+
 static unsigned vec_blocks(long long n) {
   long long b = (n + KT - 1) / KT;
   long long cap = (long long)num_sms() * 2;
@@ -408,6 +430,37 @@ static ArnState arn_state(const KWs& ws) {
   return st;
 }
 
+static int stored_apply32(const void* ctx, const float* x, float* y, int nrhs, cudaStream_t s, const int* skip) {
+  const StoredCtx* c = (const StoredCtx*)ctx;
+  return gemv_launch(MPDOK_F32, false, c->A32, c->lda32, c->n, c->n, x, c->n, nrhs, y, c->n, 1.0, 0.0, nullptr, 0,
+                     nullptr, c->gw, c->gbytes, s, false, skip);
+}
+
+static int stored_residual64(const void* ctx, const double* b, const double* x, double* r, double* nrm2, int nrhs,
+                             cudaStream_t s) {
+  const StoredCtx* c = (const StoredCtx*)ctx;
+  if (nrhs == 1)
+    return gemv_launch(MPDOK_F64, false, c->A64, c->lda64, c->n, c->n, x, c->n, 1, r, c->n, -1.0, 1.0, b, c->n,
+                       nrm2, c->gw, c->gbytes, s, true, nullptr);
+  MPDOK_TRY(gemv_launch(MPDOK_F64, false, c->A64, c->lda64, c->n, c->n, x, c->n, nrhs, r, c->n, -1.0, 1.0, b, c->n,
+                        nullptr, c->gw, c->gbytes, s, true, nullptr));
+  return colnorms_f64(r, c->n, nrhs, nrm2, s);
+}
+
+Operator32 stored_op32(const StoredCtx* c) {
+  Operator32 o;
+  o.apply = stored_apply32;
+  o.ctx = c;
+  return o;
+}
+
+Residual64 stored_res64(const StoredCtx* c) {
+  Residual64 o;
+  o.apply = stored_residual64;
+  o.ctx = c;
+  return o;
+}
+
 int read_scal(const KWs& ws, KScal* host, cudaStream_t s) {
   MPDOK_CUDA_TRY(cudaMemcpyAsync(host, ws.sc, sizeof(KScal), cudaMemcpyDeviceToHost, s));
   MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
@@ -434,8 +487,8 @@ static int cycle_start_from_f32(const KWs& ws, const float* src32, cudaStream_t 
   return MPDOK_OK;
 }
 
-int arnoldi_cycle(const KWs& ws, const float* A32, long long lda32, int m, int reorth, double tol_rel,
-                  const Precond* pc, float* x32, double* x64, cudaStream_t s) {
+int arnoldi_cycle(const KWs& ws, const Operator32& A, int m, int reorth, double tol_rel, const Precond* pc,
+                  float* x32, double* x64, cudaStream_t s) {
   const long long n = ws.n;
   const ArnState st = arn_state(ws);
   const size_t smem_dots = (size_t)ws.ch * sizeof(float);
@@ -447,8 +500,7 @@ int arnoldi_cycle(const KWs& ws, const float* A32, long long lda32, int m, int r
       MPDOK_TRY(pc->apply(pc->ctx, vk, pc->z, s, &ws.sc->done));
       opnd = pc->z;
     }
-    MPDOK_TRY(gemv_launch(MPDOK_F32, false, A32, lda32, n, n, opnd, n, 1, ws.w, n, 1.0, 0.0, nullptr, 0, nullptr,
-                          ws.gw, ws.gbytes, s, false, &ws.sc->done));
+    MPDOK_TRY(A.apply(A.ctx, opnd, ws.w, 1, s, &ws.sc->done));
     double* Hcol = ws.H + (long long)k * st.ldh;
     launch(k_dots, ws.nblk, KT, smem_dots, s, ws.V, ws.ldv, k + 1, ws.w, n, ws.ch, ws.parts, ws.tickets + 0, Hcol, ws.sc);
     if (reorth >= 2) {
@@ -495,7 +547,7 @@ static void info_reset(mpdok_solve_info* info) {
   if (info) std::memset(info, 0, sizeof(*info));
 }
 
-static int ws_prepare(const KWs& ws, size_t work_bytes, cudaStream_t s) {
+int ws_prepare(const KWs& ws, size_t work_bytes, cudaStream_t s) {
   MPDOK_ARG_CHECK(ws.V != nullptr, "null workspace");
   if (work_bytes < ws.total) {
     set_error("invalid argument: Krylov workspace too small (%zu < %zu bytes)", work_bytes, ws.total);
@@ -506,11 +558,8 @@ static int ws_prepare(const KWs& ws, size_t work_bytes, cudaStream_t s) {
   return MPDOK_OK;
 }
 
-// FP64 residual r64 = b - A64 x with ||r||^2 into sc->nrm2, then read sc.
-static int fp64_residual(const KWs& ws, const double* A64, long long lda, const double* b, const double* x,
-                         KScal* hs, cudaStream_t s) {
-  MPDOK_TRY(gemv_launch(MPDOK_F64, false, A64, lda, ws.n, ws.n, x, ws.n, 1, ws.r64, ws.n, -1.0, 1.0, b, ws.n,
-                        &ws.sc->nrm2, ws.gw, ws.gbytes, s, true, nullptr));
+int fp64_residual(const KWs& ws, const Residual64& R, const double* b, const double* x, KScal* hs, cudaStream_t s) {
+  MPDOK_TRY(R.apply(R.ctx, b, x, ws.r64, &ws.sc->nrm2, 1, s));
   return read_scal(ws, hs, s);
 }
 
@@ -523,9 +572,8 @@ static int host_bnorm(const KWs& ws, const double* b, double* bnorm, cudaStream_
 }
 
 // Restarted FP32 GMRES on rhs64 (dense_krylov.py:212-331); x64 in/out.
-static int gmres_core(const KWs& ws, const float* A32, long long lda32, const double* A64, long long lda,
-                      const double* rhs64, double* x64, double tol, int maxiter, int restart, mpdok_solve_info* info,
-                      cudaStream_t s) {
+int gmres_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* rhs64, double* x64, double tol,
+               int maxiter, int restart, mpdok_solve_info* info, cudaStream_t s) {
   const long long n = ws.n;
   if (maxiter <= 0) maxiter = (int)std::min<long long>(n, INT32_MAX);
   double bnorm = 0.0;
@@ -546,16 +594,16 @@ static int gmres_core(const KWs& ws, const float* A32, long long lda32, const do
   KScal hs;
   for (int outer = 0; outer < max_restarts; ++outer) {
     // r = b32 - A32 x32 (FP32), start vector of the cycle.
-    MPDOK_TRY(gemv_launch(MPDOK_F32, false, A32, lda32, n, n, ws.x32, n, 1, ws.w, n, -1.0, 1.0, ws.b32, n, nullptr,
-                          ws.gw, ws.gbytes, s, false, nullptr));
+    MPDOK_TRY(A.apply(A.ctx, ws.x32, ws.w, 1, s, nullptr));
+    launch(k_sub_from, vec_blocks(n), KT, 0, s, (const float*)ws.b32, ws.w, n);
     MPDOK_TRY(cycle_start_from_f32(ws, ws.w, s));
     MPDOK_TRY(read_scal(ws, &hs, s));
     if (hs.beta == 0.0) { converged = true; break; }
     const int mm = std::min(restart, maxiter - total);
     if (mm <= 0) break;
-    MPDOK_TRY(arnoldi_cycle(ws, A32, lda32, mm, 1, 0.0, nullptr, ws.x32, nullptr, s));
+    MPDOK_TRY(arnoldi_cycle(ws, A, mm, 1, 0.0, nullptr, ws.x32, nullptr, s));
     MPDOK_TRY(convert_any(ws.x32, MPDOK_F32, ws.x64t, MPDOK_F64, n, s));
-    MPDOK_TRY(fp64_residual(ws, A64, lda, rhs64, ws.x64t, &hs, s));
+    MPDOK_TRY(fp64_residual(ws, R, rhs64, ws.x64t, &hs, s));
     total += hs.m_used;
     const double rel = std::sqrt(hs.nrm2) / bnorm;
     hist_push(info, total, rel);
@@ -570,6 +618,149 @@ static int gmres_core(const KWs& ws, const float* A32, long long lda32, const do
   return MPDOK_OK;
 }
 
+int gmres_ir_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* b, double* x, double tol,
+                  int maxiter_outer, int restart, double inner_tol, const Precond* pc, mpdok_solve_info* info,
+                  cudaStream_t s) {
+  const long long n = ws.n;
+  double bnorm = 0.0;
+  MPDOK_TRY(host_bnorm(ws, b, &bnorm, s));
+  if (info) info->bnorm = bnorm;
+  if (bnorm == 0.0) {
+    MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    hist_push(info, 0, 0.0);
+    if (info) info->converged = 1;
+    return MPDOK_OK;
+  }
+  bool converged = false;
+  KScal hs;
+  int inner_total = 0;
+  for (int outer = 0; outer < maxiter_outer; ++outer) {
+    MPDOK_TRY(fp64_residual(ws, R, b, x, &hs, s));
+    if (outer > 0) inner_total += hs.m_used;
+    const double rel = std::sqrt(hs.nrm2) / bnorm;
+    hist_push(info, outer, rel);
+    if (!std::isfinite(rel)) { set_error("GMRES-IR: non-finite residual"); return MPDOK_ERR_NONFINITE; }
+    if (rel < tol) { converged = true; break; }
+    MPDOK_TRY(cycle_start_from_f64(ws, ws.r64, s));
+    MPDOK_TRY(arnoldi_cycle(ws, A, restart, 2, inner_tol, pc, nullptr, x, s));
+    if (info) info->outer_iters = outer + 1;
+  }
+  if (!converged) {
+    MPDOK_TRY(fp64_residual(ws, R, b, x, &hs, s));
+    if (maxiter_outer > 0) inner_total += hs.m_used;
+    const double rel = std::sqrt(hs.nrm2) / bnorm;
+    hist_push(info, maxiter_outer, rel);
+    converged = rel < tol;
+  }
+  if (info) { info->converged = converged ? 1 : 0; info->inner_iters = inner_total; }
+  return MPDOK_OK;
+}
+
+int dense_gmres_ir_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* b, double* x,
+                        double tol, int maxiter_outer, int restart, int maxiter_inner, mpdok_solve_info* info,
+                        cudaStream_t s) {
+  const long long n = ws.n;
+  double bnorm = 0.0;
+  MPDOK_TRY(host_bnorm(ws, b, &bnorm, s));
+  if (info) info->bnorm = bnorm;
+  if (bnorm == 0.0) {
+    MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    hist_push(info, 0, 0.0);
+    if (info) info->converged = 1;
+    return MPDOK_OK;
+  }
+  MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+  double* rhs = ws.e64 + ws.ldv;  // second FP64 vector of the e64 pair
+  bool converged = false;
+  KScal hs;
+  int inner_total = 0;
+  for (int outer = 0; outer < maxiter_outer; ++outer) {
+    MPDOK_TRY(fp64_residual(ws, R, b, x, &hs, s));
+    const double rel = std::sqrt(hs.nrm2) / bnorm;
+    hist_push(info, outer, rel);
+    if (!std::isfinite(rel)) { set_error("GMRES-IR: non-finite residual"); return MPDOK_ERR_NONFINITE; }
+    if (rel < tol) { converged = true; break; }
+    MPDOK_CUDA_TRY(cudaMemcpyAsync(rhs, ws.r64, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    MPDOK_CUDA_TRY(cudaMemsetAsync(ws.e64, 0, sizeof(double) * n, s));
+    mpdok_solve_info inner;
+    info_reset(&inner);
+    MPDOK_TRY(gmres_core(ws, A, R, rhs, ws.e64, 1e-6, maxiter_inner, restart, &inner, s));
+    inner_total += inner.inner_iters;
+    launch(k_axpy_f64, vec_blocks(n), KT, 0, s, (const double*)ws.e64, x, n);
+    MPDOK_LAUNCH_CHECK("gmres_ir update");
+    if (info) info->outer_iters = outer + 1;
+  }
+  MPDOK_TRY(fp64_residual(ws, R, b, x, &hs, s));
+  const double rel = std::sqrt(hs.nrm2) / bnorm;
+  hist_push(info, maxiter_outer, rel);
+  converged = converged || rel < tol;
+  if (info) { info->converged = converged ? 1 : 0; info->inner_iters = inner_total; }
+  return MPDOK_OK;
+}
+
+int cg_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* b, double* x, double tol,
+            int maxiter, int check_every, mpdok_solve_info* info, cudaStream_t s) {
+  const long long n = ws.n;
+  if (maxiter < 0) maxiter = (int)std::min<long long>(n, INT32_MAX);
+  double bnorm = 0.0;
+  MPDOK_TRY(host_bnorm(ws, b, &bnorm, s));
+  if (info) info->bnorm = bnorm;
+  if (bnorm == 0.0) {
+    MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    hist_push(info, 0, 0.0);
+    if (info) info->converged = 1;
+    return MPDOK_OK;
+  }
+  float* xr = ws.x32;
+  float* r = ws.w;
+  float* p = ws.p32;
+  float* q = ws.q32;
+  MPDOK_TRY(convert_any(b, MPDOK_F64, ws.b32, MPDOK_F32, n, s));
+  MPDOK_TRY(convert_any(x, MPDOK_F64, xr, MPDOK_F32, n, s));
+  MPDOK_TRY(A.apply(A.ctx, xr, r, 1, s, nullptr));
+  launch(k_sub_from, vec_blocks(n), KT, 0, s, (const float*)ws.b32, r, n);
+  launch(k_norm2<float>, vec_blocks(n), KT, 0, s, (const float*)r, n, ws.parts, ws.tickets + 4, &ws.sc->nrm2);
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(p, r, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+  launch(k_set_rs, 1, 32, 0, s, ws.sc);
+  bool converged = false;
+  double prev = std::numeric_limits<double>::infinity();
+  KScal hs;
+  int last_k = -1;
+  int it_done = 0;
+  for (int k = 0; k < maxiter; ++k) {
+    last_k = k;
+    if (k % check_every == 0) {
+      MPDOK_TRY(convert_any(xr, MPDOK_F32, ws.x64t, MPDOK_F64, n, s));
+      MPDOK_TRY(fp64_residual(ws, R, b, ws.x64t, &hs, s));
+      const double rel = std::sqrt(hs.nrm2) / bnorm;
+      hist_push(info, k, rel);
+      if (info) info->outer_iters++;
+      if (!std::isfinite(rel)) { set_error("CG: non-finite residual"); return MPDOK_ERR_NONFINITE; }
+      if (rel < tol) { converged = true; break; }
+      if (rel > prev * (1.0 - 1e-2)) { if (info) info->stagnated = 1; break; }
+      prev = rel;
+      if (hs.done) break;  // p.Ap == 0: nothing more to do
+    }
+    MPDOK_TRY(A.apply(A.ctx, p, q, 1, s, &ws.sc->done));
+    launch(k_cg_pap, vec_blocks(n), KT, 0, s, (const float*)p, (const float*)q, n, ws.parts, ws.tickets + 0, ws.sc);
+    launch(k_cg_xr, vec_blocks(n), KT, 0, s, xr, r, (const float*)p, (const float*)q, n, ws.parts, ws.tickets + 1,
+           ws.sc);
+    launch(k_cg_p, vec_blocks(n), KT, 0, s, p, (const float*)r, n, (const KScal*)ws.sc);
+    MPDOK_LAUNCH_CHECK("cg iteration");
+    it_done = k + 1;
+  }
+  if (!converged) {
+    MPDOK_TRY(convert_any(xr, MPDOK_F32, ws.x64t, MPDOK_F64, n, s));
+    MPDOK_TRY(fp64_residual(ws, R, b, ws.x64t, &hs, s));
+    const double rel = std::sqrt(hs.nrm2) / bnorm;
+    hist_push(info, last_k + 1, rel);
+    converged = rel < tol;
+  }
+  MPDOK_TRY(convert_any(xr, MPDOK_F32, x, MPDOK_F64, n, s));
+  if (info) { info->converged = converged ? 1 : 0; info->inner_iters = it_done; }
+  return MPDOK_OK;
+}
+
 }  // namespace mpdok
 
 using namespace mpdok;
@@ -577,6 +768,18 @@ using namespace mpdok;
 extern "C" size_t mpdok_krylov_workspace_size(long long n, int restart) {
   if (n < 0 || restart < 1) return 0;
   return krylov_layout(n, std::min(restart, KMAX_RESTART), nullptr).total;
+}
+
+static StoredCtx make_stored(const KWs& ws, const float* A32, long long lda32, const double* A64, long long lda) {
+  StoredCtx c;
+  c.A32 = A32;
+  c.lda32 = lda32;
+  c.A64 = A64;
+  c.lda64 = lda;
+  c.n = ws.n;
+  c.gw = ws.gw;
+  c.gbytes = ws.gbytes;
+  return c;
 }
 
 extern "C" int mpdok_gmres_ir(const double* A64, long long lda, float* A32, long long lda32, int a32_ready,
@@ -593,38 +796,9 @@ extern "C" int mpdok_gmres_ir(const double* A64, long long lda, float* A32, long
   KWs ws = krylov_layout(n, restart, work);
   MPDOK_TRY(ws_prepare(ws, work_bytes, s));
   if (!a32_ready) MPDOK_TRY(convert_matrix_f64_f32(A64, lda, A32, lda32, n, n, s));
-  double bnorm = 0.0;
-  MPDOK_TRY(host_bnorm(ws, b, &bnorm, s));
-  if (info) info->bnorm = bnorm;
-  if (bnorm == 0.0) {
-    MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
-    hist_push(info, 0, 0.0);
-    if (info) info->converged = 1;
-    return MPDOK_OK;
-  }
-  bool converged = false;
-  KScal hs;
-  int inner_total = 0;
-  for (int outer = 0; outer < maxiter_outer; ++outer) {
-    MPDOK_TRY(fp64_residual(ws, A64, lda, b, x, &hs, s));
-    if (outer > 0) inner_total += hs.m_used;
-    const double rel = std::sqrt(hs.nrm2) / bnorm;
-    hist_push(info, outer, rel);
-    if (!std::isfinite(rel)) { set_error("GMRES-IR: non-finite residual"); return MPDOK_ERR_NONFINITE; }
-    if (rel < tol) { converged = true; break; }
-    MPDOK_TRY(cycle_start_from_f64(ws, ws.r64, s));
-    MPDOK_TRY(arnoldi_cycle(ws, A32, lda32, restart, 2, inner_tol, nullptr, nullptr, x, s));
-    if (info) info->outer_iters = outer + 1;
-  }
-  if (!converged) {
-    MPDOK_TRY(fp64_residual(ws, A64, lda, b, x, &hs, s));
-    if (maxiter_outer > 0) inner_total += hs.m_used;
-    const double rel = std::sqrt(hs.nrm2) / bnorm;
-    hist_push(info, maxiter_outer, rel);
-    converged = rel < tol;
-  }
-  if (info) { info->converged = converged ? 1 : 0; info->inner_iters = inner_total; }
-  return MPDOK_OK;
+  StoredCtx c = make_stored(ws, A32, lda32, A64, lda);
+  return gmres_ir_core(ws, stored_op32(&c), stored_res64(&c), b, x, tol, maxiter_outer, restart, inner_tol, nullptr,
+                       info, s);
 }
 
 extern "C" int mpdok_gmres(const float* A32, long long lda32, const double* A64, long long lda, long long n,
@@ -637,7 +811,8 @@ extern "C" int mpdok_gmres(const float* A32, long long lda32, const double* A64,
   MPDOK_ARG_CHECK(A32 && A64 && b && x, "null pointer (GMRES needs the FP64 matrix for residual checks)");
   KWs ws = krylov_layout(n, restart, work);
   MPDOK_TRY(ws_prepare(ws, work_bytes, s));
-  return gmres_core(ws, A32, lda32, A64, lda, b, x, tol, maxiter, restart, info, s);
+  StoredCtx c = make_stored(ws, A32, lda32, A64, lda);
+  return gmres_core(ws, stored_op32(&c), stored_res64(&c), b, x, tol, maxiter, restart, info, s);
 }
 
 extern "C" int mpdok_dense_gmres_ir(const float* A32, long long lda32, const double* A64, long long lda, long long n,
@@ -651,42 +826,9 @@ extern "C" int mpdok_dense_gmres_ir(const float* A32, long long lda32, const dou
   MPDOK_ARG_CHECK(A32 && A64 && b && x, "null pointer");
   KWs ws = krylov_layout(n, restart, work);
   MPDOK_TRY(ws_prepare(ws, work_bytes, s));
-  double bnorm = 0.0;
-  MPDOK_TRY(host_bnorm(ws, b, &bnorm, s));
-  if (info) info->bnorm = bnorm;
-  if (bnorm == 0.0) {
-    MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
-    hist_push(info, 0, 0.0);
-    if (info) info->converged = 1;
-    return MPDOK_OK;
-  }
-  MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
-  double* rhs = ws.e64 + ws.ldv;  // second FP64 vector of the e64 pair
-  bool converged = false;
-  KScal hs;
-  int inner_total = 0;
-  for (int outer = 0; outer < maxiter_outer; ++outer) {
-    MPDOK_TRY(fp64_residual(ws, A64, lda, b, x, &hs, s));
-    const double rel = std::sqrt(hs.nrm2) / bnorm;
-    hist_push(info, outer, rel);
-    if (!std::isfinite(rel)) { set_error("GMRES-IR: non-finite residual"); return MPDOK_ERR_NONFINITE; }
-    if (rel < tol) { converged = true; break; }
-    MPDOK_CUDA_TRY(cudaMemcpyAsync(rhs, ws.r64, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    MPDOK_CUDA_TRY(cudaMemsetAsync(ws.e64, 0, sizeof(double) * n, s));
-    mpdok_solve_info inner;
-    info_reset(&inner);
-    MPDOK_TRY(gmres_core(ws, A32, lda32, A64, lda, rhs, ws.e64, 1e-6, maxiter_inner, restart, &inner, s));
-    inner_total += inner.inner_iters;
-    launch(k_axpy_f64, vec_blocks(n), KT, 0, s, ws.e64, x, n);
-    MPDOK_LAUNCH_CHECK("gmres_ir update");
-    if (info) info->outer_iters = outer + 1;
-  }
-  MPDOK_TRY(fp64_residual(ws, A64, lda, b, x, &hs, s));
-  const double rel = std::sqrt(hs.nrm2) / bnorm;
-  hist_push(info, maxiter_outer, rel);
-  converged = converged || rel < tol;
-  if (info) { info->converged = converged ? 1 : 0; info->inner_iters = inner_total; }
-  return MPDOK_OK;
+  StoredCtx c = make_stored(ws, A32, lda32, A64, lda);
+  return dense_gmres_ir_core(ws, stored_op32(&c), stored_res64(&c), b, x, tol, maxiter_outer, restart, maxiter_inner,
+                             info, s);
 }
 
 extern "C" int mpdok_cg(const float* A32, long long lda32, const double* A64, long long lda, long long n,
@@ -697,63 +839,8 @@ extern "C" int mpdok_cg(const float* A32, long long lda32, const double* A64, lo
   MPDOK_ARG_CHECK(check_every >= 1, "check_every must be >= 1");
   if (n == 0) { if (info) info->converged = 1; return MPDOK_OK; }
   MPDOK_ARG_CHECK(A32 && A64 && b && x, "null pointer (CG needs the FP64 matrix for residual checks)");
-  if (maxiter < 0) maxiter = (int)std::min<long long>(n, INT32_MAX);
   KWs ws = krylov_layout(n, 1, work);
   MPDOK_TRY(ws_prepare(ws, work_bytes, s));
-  double bnorm = 0.0;
-  MPDOK_TRY(host_bnorm(ws, b, &bnorm, s));
-  if (info) info->bnorm = bnorm;
-  if (bnorm == 0.0) {
-    MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
-    hist_push(info, 0, 0.0);
-    if (info) info->converged = 1;
-    return MPDOK_OK;
-  }
-  float* xr = ws.x32;
-  float* r = ws.w;
-  float* p = ws.p32;
-  float* q = ws.q32;
-  MPDOK_TRY(convert_any(b, MPDOK_F64, ws.b32, MPDOK_F32, n, s));
-  MPDOK_TRY(convert_any(x, MPDOK_F64, xr, MPDOK_F32, n, s));
-  MPDOK_TRY(gemv_launch(MPDOK_F32, false, A32, lda32, n, n, xr, n, 1, r, n, -1.0, 1.0, ws.b32, n, &ws.sc->nrm2,
-                        ws.gw, ws.gbytes, s, true, nullptr));
-  MPDOK_CUDA_TRY(cudaMemcpyAsync(p, r, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-  launch(k_set_rs, 1, 32, 0, s, ws.sc);
-  bool converged = false;
-  double prev = std::numeric_limits<double>::infinity();
-  KScal hs;
-  int last_k = -1;
-  int it_done = 0;
-  for (int k = 0; k < maxiter; ++k) {
-    last_k = k;
-    if (k % check_every == 0) {
-      MPDOK_TRY(convert_any(xr, MPDOK_F32, ws.x64t, MPDOK_F64, n, s));
-      MPDOK_TRY(fp64_residual(ws, A64, lda, b, ws.x64t, &hs, s));
-      const double rel = std::sqrt(hs.nrm2) / bnorm;
-      hist_push(info, k, rel);
-      if (info) info->outer_iters++;
-      if (!std::isfinite(rel)) { set_error("CG: non-finite residual"); return MPDOK_ERR_NONFINITE; }
-      if (rel < tol) { converged = true; break; }
-      if (rel > prev * (1.0 - 1e-2)) { if (info) info->stagnated = 1; break; }
-      prev = rel;
-      if (hs.done) break;  // p.Ap == 0: nothing more to do
-    }
-    MPDOK_TRY(gemv_launch(MPDOK_F32, false, A32, lda32, n, n, p, n, 1, q, n, 1.0, 0.0, nullptr, 0, nullptr, ws.gw,
-                          ws.gbytes, s, false, &ws.sc->done));
-    launch(k_cg_pap, vec_blocks(n), KT, 0, s, p, q, n, ws.parts, ws.tickets + 0, ws.sc);
-    launch(k_cg_xr, vec_blocks(n), KT, 0, s, xr, r, p, q, n, ws.parts, ws.tickets + 1, ws.sc);
-    launch(k_cg_p, vec_blocks(n), KT, 0, s, p, r, n, ws.sc);
-    MPDOK_LAUNCH_CHECK("cg iteration");
-    it_done = k + 1;
-  }
-  if (!converged) {
-    MPDOK_TRY(convert_any(xr, MPDOK_F32, ws.x64t, MPDOK_F64, n, s));
-    MPDOK_TRY(fp64_residual(ws, A64, lda, b, ws.x64t, &hs, s));
-    const double rel = std::sqrt(hs.nrm2) / bnorm;
-    hist_push(info, last_k + 1, rel);
-    converged = rel < tol;
-  }
-  MPDOK_TRY(convert_any(xr, MPDOK_F32, x, MPDOK_F64, n, s));
-  if (info) { info->converged = converged ? 1 : 0; info->inner_iters = it_done; }
-  return MPDOK_OK;
+  StoredCtx c = make_stored(ws, A32, lda32, A64, lda);
+  return cg_core(ws, stored_op32(&c), stored_res64(&c), b, x, tol, maxiter, check_every, info, s);
 }

@@ -37,6 +37,33 @@ struct KWs {
 
 KWs krylov_layout(long long n, int m, void* base);
 
+// FP32 operator y = A x (nrhs columns, leading dimension n) used by the
+// Krylov bodies; `skip` predicates the launches on a device flag.
+struct Operator32 {
+  int (*apply)(const void* ctx, const float* x, float* y, int nrhs, cudaStream_t s, const int* skip) = nullptr;
+  const void* ctx = nullptr;
+};
+
+// FP64 residual r = b - A x (nrhs columns) with per-column ||r||^2 into nrm2[0..nrhs).
+struct Residual64 {
+  int (*apply)(const void* ctx, const double* b, const double* x, double* r, double* nrm2, int nrhs,
+               cudaStream_t s) = nullptr;
+  const void* ctx = nullptr;
+};
+
+// Stored-matrix implementations (FP32 A32 / FP64 A64, column-major).
+struct StoredCtx {
+  const float* A32 = nullptr;
+  long long lda32 = 0;
+  const double* A64 = nullptr;
+  long long lda64 = 0;
+  long long n = 0;
+  void* gw = nullptr;
+  size_t gbytes = 0;
+};
+Operator32 stored_op32(const StoredCtx* c);
+Residual64 stored_res64(const StoredCtx* c);
+
 // Preconditioner hook for right-preconditioned cycles: z = M^{-1} v.
 struct Precond {
   int (*apply)(void* ctx, const float* v, float* z, cudaStream_t s, const int* skip) = nullptr;
@@ -49,13 +76,30 @@ struct Precond {
 // set by cycle_setup.  reorth = 1 or 2 Gram-Schmidt passes.  Early stop when
 // |g_{k+1}| / beta < tol_rel (tol_rel <= 0 disables it).  The correction
 // V y (or M^{-1} V y when preconditioned) is added to x32 or x64.
-int arnoldi_cycle(const KWs& ws, const float* A32, long long lda32, int m, int reorth, double tol_rel,
-                  const Precond* pc, float* x32, double* x64, cudaStream_t s);
+int arnoldi_cycle(const KWs& ws, const Operator32& A, int m, int reorth, double tol_rel, const Precond* pc,
+                  float* x32, double* x64, cudaStream_t s);
 
 // V[:,0] = (float) src64 and sc->nrm2, beta, flags for a new cycle.
 int cycle_start_from_f64(const KWs& ws, const double* src64, cudaStream_t s);
 
 int read_scal(const KWs& ws, KScal* host, cudaStream_t s);
 int norm2_f64(const KWs& ws, const double* x, long long n, double* out_dev, cudaStream_t s);
+int colnorms_f64(const double* r, long long n, int nrhs, double* nrm2, cudaStream_t s);
+// FP64 residual r64 = b - A x through R, ||r||^2 into sc->nrm2, then the
+// scalar block is read back to the host.
+int fp64_residual(const KWs& ws, const Residual64& R, const double* b, const double* x, KScal* hs, cudaStream_t s);
+// Restarted FP32 GMRES(m) (single Gram-Schmidt pass, FP64 check per restart).
+int gmres_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* rhs64, double* x64, double tol,
+               int maxiter, int restart, mpdok_solve_info* info, cudaStream_t s);
+// GMRES-IR outer loop (mpdok_ooc.py:315-373) over any operator pair.
+int gmres_ir_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* b, double* x, double tol,
+                  int maxiter_outer, int restart, double inner_tol, const Precond* pc, mpdok_solve_info* info,
+                  cudaStream_t s);
+int ws_prepare(const KWs& ws, size_t work_bytes, cudaStream_t s);
+int dense_gmres_ir_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* b, double* x,
+                        double tol, int maxiter_outer, int restart, int maxiter_inner, mpdok_solve_info* info,
+                        cudaStream_t s);
+int cg_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* b, double* x, double tol,
+            int maxiter, int check_every, mpdok_solve_info* info, cudaStream_t s);
 
 }  // namespace mpdok

@@ -958,48 +958,14 @@ extern "C" int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* 
   KWs ws = krylov_layout(n, restart, wb + a_bytes + align_up((size_t)n * sizeof(float), 256));
   MPDOK_CUDA_TRY(cudaMemsetAsync(ws.tickets, 0, sizeof(unsigned) * 8, s));
   MPDOK_CUDA_TRY(cudaMemsetAsync(ws.sc, 0, sizeof(KScal), s));
-  MPDOK_TRY(norm2_f64(ws, b, n, &ws.sc->aux, s));
-  KScal hs;
-  MPDOK_TRY(read_scal(ws, &hs, s));
-  const double bnorm = std::sqrt(hs.aux);
-  if (info) info->bnorm = bnorm;
-  if (bnorm == 0.0) {
-    MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
-    if (info) { info->converged = 1; info->n_history = 1; info->history[0] = 0.0; }
-    return MPDOK_OK;
-  }
-  bool conv = false;
-  int inner_total = 0;
-  for (int outer = 0; outer < maxiter_outer; ++outer) {
-    MPDOK_TRY(gemv_launch(MPDOK_F64, false, A64, lda, n, n, x, n, 1, ws.r64, n, -1.0, 1.0, b, n, &ws.sc->nrm2,
-                          ws.gw, ws.gbytes, s, true, nullptr));
-    MPDOK_TRY(read_scal(ws, &hs, s));
-    if (outer > 0) inner_total += hs.m_used;
-    const double rel = std::sqrt(hs.nrm2) / bnorm;
-    if (info && info->n_history < MPDOK_HISTORY_MAX) {
-      info->hist_iter[info->n_history] = outer;
-      info->history[info->n_history++] = rel;
-      info->relres = rel;
-    }
-    if (!std::isfinite(rel)) { set_error("GMRES-IR: non-finite residual"); return MPDOK_ERR_NONFINITE; }
-    if (rel < tol) { conv = true; break; }
-    MPDOK_TRY(cycle_start_from_f64(ws, ws.r64, s));
-    MPDOK_TRY(arnoldi_cycle(ws, A32, lda32, restart, 2, inner_tol, &pc, nullptr, x, s));
-    if (info) info->outer_iters = outer + 1;
-  }
-  if (!conv) {
-    MPDOK_TRY(gemv_launch(MPDOK_F64, false, A64, lda, n, n, x, n, 1, ws.r64, n, -1.0, 1.0, b, n, &ws.sc->nrm2,
-                          ws.gw, ws.gbytes, s, true, nullptr));
-    MPDOK_TRY(read_scal(ws, &hs, s));
-    if (maxiter_outer > 0) inner_total += hs.m_used;
-    const double rel = std::sqrt(hs.nrm2) / bnorm;
-    if (info && info->n_history < MPDOK_HISTORY_MAX) {
-      info->hist_iter[info->n_history] = maxiter_outer;
-      info->history[info->n_history++] = rel;
-    }
-    if (info) info->relres = rel;
-    conv = rel < tol;
-  }
-  if (info) { info->converged = conv ? 1 : 0; info->inner_iters = inner_total; }
-  return MPDOK_OK;
+  StoredCtx c;
+  c.A32 = A32;
+  c.lda32 = lda32;
+  c.A64 = A64;
+  c.lda64 = lda;
+  c.n = n;
+  c.gw = ws.gw;
+  c.gbytes = ws.gbytes;
+  return gmres_ir_core(ws, stored_op32(&c), stored_res64(&c), b, x, tol, maxiter_outer, restart, inner_tol, &pc, info,
+                       s);
 }

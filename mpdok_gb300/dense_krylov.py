@@ -121,6 +121,8 @@ def cg(op, b, x0=None, tol: float = 1e-6, maxiter=None, check_every: int = 10, v
     Returns ``(x_fp64, history, converged)``; history holds
     ``(iteration, fp64_relative_residual)`` at every check.
     """
+    if getattr(op, "_matrix_free", False):
+        return op.cg(b, x0=x0, tol=tol, maxiter=maxiter, check_every=check_every)
     _require_fp64(op, "cg")
     n = op.N
     maxiter = n if maxiter is None else int(maxiter)
@@ -164,6 +166,8 @@ def gmres_ir(op, b, tol: float = 1e-11, maxiter_outer: int = 5, restart: int = 5
     Outer FP64 residual, inner FP32 GMRES to 1e-6, FP64 update; the history
     holds ``(outer_iter, relres)`` with a final entry at ``maxiter_outer``.
     """
+    if getattr(op, "_matrix_free", False):
+        return op.gmres_ir(b, tol=tol, maxiter_outer=maxiter_outer, restart=restart)
     _require_fp64(op, "GMRES-IR")
     n = op.N
     b64 = as_vector(b)

@@ -1,0 +1,105 @@
+"""Matrix-free RBF operator: entries recomputed on the fly, A never stored.
+
+``MatrixFreeOperator(coords, gamma, reg, kernel)`` behaves like
+``DenseLinearOperator`` (``matvec``, ``residual_norm``) for the RBF system
+A = K(coords, coords) + reg I, and ``cg`` / ``gmres_ir`` of
+``mpdok_gb300.dense_krylov`` accept it.  The FP32 evaluate-and-multiply
+stages centre tiles into shared memory by TMA and recomputes exp / sqrt per
+entry; the FP64 variant gives residual-accurate products (the reference's
+matrix-free FP64 residual, mpdok_ooc.py:205-227).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native as N
+from ._device import Workspace, as_columns, as_vector, fortran_empty, ptr, require_cuda, stream_handle
+from .rbf_kernel import KERNELS, _coords_device
+
+
+class MatrixFreeOperator:
+    """A = phi(||c_i - c_j||) + reg I, applied without storing A."""
+
+    _matrix_free = True
+
+    def __init__(self, coords, gamma: float, reg: float = 0.0, kernel: str = "gaussian"):
+        self.coords = _coords_device(coords)
+        self.N = int(self.coords.shape[0])
+        self.dim = int(self.coords.shape[1])
+        self.gamma = float(gamma)
+        self.reg = float(reg)
+        self.kernel = kernel
+        self.kcode = KERNELS[kernel]
+        self._ws = Workspace()
+        self.A_fp64 = True  # residuals are available (computed matrix-free in FP64)
+
+    @property
+    def shape(self):
+        return (self.N, self.N)
+
+    def _apply(self, X, precision):
+        squeeze = X.dim() == 1
+        tdt = torch.float64 if precision == N.F64 else torch.float32
+        Xc = as_columns(X, tdt)
+        k = Xc.shape[1]
+        if k > 8:
+            return torch.cat([self._apply(Xc[:, i:i + 8], precision) for i in range(0, k, 8)], dim=1)
+        ld = self.N if precision == N.F64 else (self.N + 3) // 4 * 4
+        if ld != self.N:
+            Xp = fortran_empty(ld, k, tdt)
+            Xp[: self.N] = Xc
+            Xc = Xp
+        Y = fortran_empty(self.N, k, tdt)
+        lib = N.load()
+        w = self._ws.get(lib.mpdok_matfree_workspace_size(self.N, self.N, k, precision))
+        N.check(lib.mpdok_matfree_apply(ptr(self.coords), self.N, ptr(self.coords), self.N, self.dim, self.kcode,
+                                        self.gamma, self.reg, 0, precision, ptr(Xc), Xc.stride(1) if k > 1 else ld,
+                                        k, ptr(Y), self.N, ptr(w), w.numel(), stream_handle()), "matfree_apply")
+        return Y.reshape(-1) if squeeze else Y
+
+    def matvec(self, x) -> torch.Tensor:
+        """A @ x in FP32 (entries recomputed per product)."""
+        return self._apply(torch.as_tensor(x, device=require_cuda()) if not isinstance(x, torch.Tensor) else x,
+                           N.F32)
+
+    def matvec64(self, x) -> torch.Tensor:
+        """A @ x in FP64."""
+        return self._apply(torch.as_tensor(x, device=require_cuda()) if not isinstance(x, torch.Tensor) else x,
+                           N.F64)
+
+    def residual_norm(self, x, b) -> float:
+        x64 = as_vector(x)
+        b64 = as_vector(b)
+        r = b64 - self.matvec64(x64)
+        return float(torch.linalg.vector_norm(r).item())
+
+    def gmres_ir(self, b, tol=1e-11, maxiter_outer=5, restart=50, inner_tol=1e-6):
+        b64 = as_vector(b)
+        x = torch.zeros(self.N, dtype=torch.float64, device=b64.device)
+        lib = N.load()
+        w = self._ws.get(lib.mpdok_mf_krylov_workspace_size(self.N, restart))
+        info = N.SolveInfo()
+        N.check(lib.mpdok_mf_gmres_ir(ptr(self.coords), self.N, self.dim, self.kcode, self.gamma, self.reg,
+                                      ptr(b64), ptr(x), float(tol), int(maxiter_outer), int(restart),
+                                      float(inner_tol), ptr(w), w.numel(), ctypes.byref(info), stream_handle()),
+                "mf_gmres_ir")
+        return x, info.history_list(), bool(info.converged)
+
+    def cg(self, b, x0=None, tol=1e-6, maxiter=None, check_every=10):
+        b64 = as_vector(b)
+        x = torch.zeros(self.N, dtype=torch.float64, device=b64.device) if x0 is None else \
+            as_vector(x0).to(torch.float32).to(torch.float64)
+        lib = N.load()
+        w = self._ws.get(lib.mpdok_mf_krylov_workspace_size(self.N, 1))
+        info = N.SolveInfo()
+        mi = self.N if maxiter is None else int(maxiter)
+        N.check(lib.mpdok_mf_cg(ptr(self.coords), self.N, self.dim, self.kcode, self.gamma, self.reg, ptr(b64),
+                                ptr(x), float(tol), mi, int(check_every), ptr(w), w.numel(), ctypes.byref(info),
+                                stream_handle()), "mf_cg")
+        return x, info.history_list(), bool(info.converged)
+
+    def __repr__(self):
+        return f"MatrixFreeOperator(N={self.N:,}, dim={self.dim}, kernel={self.kernel}, gamma={self.gamma:g})"
