@@ -177,6 +177,35 @@ MPDOK_API int mpdok_mf_cg(const double* coords, long long n, int dim, int kernel
                           const double* b, double* x, double tol, int maxiter, int check_every, void* work,
                           size_t work_bytes, mpdok_solve_info* info, cudaStream_t stream);
 
+/* ------------------------------------------------ split operator and CG-IR
+ * Split A = A_hi + A_lo into two FP32 slices (hi = fl32(a), lo = fl32(a - hi));
+ * mpdok_split_gemv forms Y = alpha (A_hi + A_lo) X + beta B with error-free
+ * FP32 products and double-float sums (FP64-level accuracy on the FP32 pipe;
+ * X, Y, B FP64; slices 16-byte aligned with ld % 4 == 0). */
+MPDOK_API int mpdok_split_matrix(const double* A, long long lda, long long m, long long n, float* hi, float* lo,
+                                 long long ld, cudaStream_t stream);
+MPDOK_API size_t mpdok_split_gemv_workspace_size(long long m, long long n, int nrhs);
+MPDOK_API int mpdok_split_gemv(const float* hi, const float* lo, long long ld, long long m, long long n,
+                               const double* X, long long ldx, int nrhs, double* Y, long long ldy, double alpha,
+                               double beta, const double* B, long long ldb, void* work, size_t work_bytes,
+                               cudaStream_t stream);
+/* Multi-RHS CG-IR (C2 family): FP64 residual R = B - A X, inner FP32 CG on
+ * A E = R for all nrhs (<= 8) columns in lockstep, X += E in FP64.  mode 0:
+ * FP32 copy of A inside + native FP64 residual; mode 1: split A for both.
+ * opbuf holds the FP32 copy or the two slices (mpdok_cg_ir_operator_size);
+ * op_ready != 0 reuses it.  info->history holds the worst column's relres. */
+MPDOK_API size_t mpdok_cg_ir_operator_size(long long n, int mode);
+MPDOK_API size_t mpdok_cg_ir_workspace_size(long long n, int nrhs, int mode);
+MPDOK_API int mpdok_cg_ir(const double* A64, long long lda, long long n, int mode, void* opbuf, int op_ready,
+                          int nrhs, const double* B, long long ldb, double* X, long long ldx, double tol,
+                          int maxiter_outer, double inner_tol, int inner_maxiter, void* work, size_t work_bytes,
+                          mpdok_solve_info* info, cudaStream_t stream);
+MPDOK_API size_t mpdok_mf_cg_ir_workspace_size(long long n, int nrhs);
+MPDOK_API int mpdok_mf_cg_ir(const double* coords, long long n, int dim, int kernel, double gamma, double reg,
+                             int nrhs, const double* B, long long ldb, double* X, long long ldx, double tol,
+                             int maxiter_outer, double inner_tol, int inner_maxiter, void* work, size_t work_bytes,
+                             mpdok_solve_info* info, cudaStream_t stream);
+
 /* ----------------------------------------------------------- LU (tensor cores)
  * Blocked right-looking LU of W = D A D (D = diag(1/sqrt|a_ii|), panel 128)
  * with FP32 panels and a trailing update W22 -= L21 U12 whose operands are
@@ -215,6 +244,21 @@ MPDOK_API int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* A
                                 const void* factors, int fdtype, const double* b, double* x, double tol,
                                 int maxiter_outer, int restart, double inner_tol, void* work, size_t work_bytes,
                                 mpdok_solve_info* info, cudaStream_t stream);
+
+/* CG-IR preconditioned by the factors (PCG inner, z = (LU)^-1 r per column),
+ * for SPD systems too ill-conditioned for an unpreconditioned FP32 CG body.
+ * op_mode 0 / 1 as mpdok_cg_ir; mpdok_mf_lu_cg_ir applies A matrix-free.
+ * Workspace: mpdok_lu_cg_ir_workspace_size(n, nrhs, op_mode) with op_mode 2
+ * for the matrix-free entry. */
+MPDOK_API size_t mpdok_lu_cg_ir_workspace_size(long long n, int nrhs, int op_mode);
+MPDOK_API int mpdok_lu_cg_ir(const double* A64, long long lda, long long n, int op_mode, void* opbuf, int op_ready,
+                             const void* factors, int fdtype, int nrhs, const double* B, long long ldb, double* X,
+                             long long ldx, double tol, int maxiter_outer, double inner_tol, int inner_maxiter,
+                             void* work, size_t work_bytes, mpdok_solve_info* info, cudaStream_t stream);
+MPDOK_API int mpdok_mf_lu_cg_ir(const double* coords, long long n, int dim, int kernel, double gamma, double reg,
+                                const void* factors, int fdtype, int nrhs, const double* B, long long ldb, double* X,
+                                long long ldx, double tol, int maxiter_outer, double inner_tol, int inner_maxiter,
+                                void* work, size_t work_bytes, mpdok_solve_info* info, cudaStream_t stream);
 
 /* --------------------------------------------------------- instrumentation
  * mpdok_launch_count: kernels launched by this library since load.

@@ -116,6 +116,26 @@ _SIGS = {
                                   c_int, c_int, c_double, c_void_p, c_size_t, ctypes.POINTER(SolveInfo), c_void_p]),
     "mpdok_mf_cg": (c_int, [c_void_p, c_ll, c_int, c_int, c_double, c_double, c_void_p, c_void_p, c_double, c_int,
                             c_int, c_void_p, c_size_t, ctypes.POINTER(SolveInfo), c_void_p]),
+    "mpdok_split_matrix": (c_int, [c_void_p, c_ll, c_ll, c_ll, c_void_p, c_void_p, c_ll, c_void_p]),
+    "mpdok_split_gemv_workspace_size": (c_size_t, [c_ll, c_ll, c_int]),
+    "mpdok_split_gemv": (c_int, [c_void_p, c_void_p, c_ll, c_ll, c_ll, c_void_p, c_ll, c_int, c_void_p, c_ll,
+                                 c_double, c_double, c_void_p, c_ll, c_void_p, c_size_t, c_void_p]),
+    "mpdok_cg_ir_operator_size": (c_size_t, [c_ll, c_int]),
+    "mpdok_cg_ir_workspace_size": (c_size_t, [c_ll, c_int, c_int]),
+    "mpdok_cg_ir": (c_int, [c_void_p, c_ll, c_ll, c_int, c_void_p, c_int, c_int, c_void_p, c_ll, c_void_p, c_ll,
+                            c_double, c_int, c_double, c_int, c_void_p, c_size_t, ctypes.POINTER(SolveInfo),
+                            c_void_p]),
+    "mpdok_mf_cg_ir_workspace_size": (c_size_t, [c_ll, c_int]),
+    "mpdok_mf_cg_ir": (c_int, [c_void_p, c_ll, c_int, c_int, c_double, c_double, c_int, c_void_p, c_ll, c_void_p,
+                               c_ll, c_double, c_int, c_double, c_int, c_void_p, c_size_t, ctypes.POINTER(SolveInfo),
+                               c_void_p]),
+    "mpdok_lu_cg_ir_workspace_size": (c_size_t, [c_ll, c_int, c_int]),
+    "mpdok_lu_cg_ir": (c_int, [c_void_p, c_ll, c_ll, c_int, c_void_p, c_int, c_void_p, c_int, c_int, c_void_p, c_ll,
+                               c_void_p, c_ll, c_double, c_int, c_double, c_int, c_void_p, c_size_t,
+                               ctypes.POINTER(SolveInfo), c_void_p]),
+    "mpdok_mf_lu_cg_ir": (c_int, [c_void_p, c_ll, c_int, c_int, c_double, c_double, c_void_p, c_int, c_int, c_void_p,
+                                  c_ll, c_void_p, c_ll, c_double, c_int, c_double, c_int, c_void_p, c_size_t,
+                                  ctypes.POINTER(SolveInfo), c_void_p]),
     "mpdok_launch_count": (c_ll, []),
     "mpdok_profile_enable": (c_int, [c_int]),
     "mpdok_profile_query": (c_int, [c_int, ctypes.POINTER(c_double), ctypes.POINTER(c_ll), ctypes.POINTER(c_double)]),

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <vector>
 
 namespace mpdok {
 
@@ -270,9 +271,10 @@ k_norm2(const T* __restrict__ x, long long n, double* parts, unsigned* ticket, d
 }
 
 // nrm2[c] = ||r[:, c]||^2, one block per column (fixed reduction order).
-__global__ void __launch_bounds__(KT) k_colnorms(const double* __restrict__ r, long long n, double* nrm2) {
+__global__ void __launch_bounds__(KT) k_colnorms(const double* __restrict__ r, long long n, long long ld,
+                                                 double* nrm2) {
   __shared__ double red[32];
-  const double* col = r + (long long)blockIdx.x * n;
+  const double* col = r + (long long)blockIdx.x * ld;
   double s = 0.0;
   for (long long i = threadIdx.x; i < n; i += blockDim.x) s = fma(col[i], col[i], s);
   s = block_sum(s, red);
@@ -371,10 +373,197 @@ __global__ void k_set_rs(KScal* sc) {
   }
 }
 
+// --------------------------------------------------- multi-RHS CG (CG-IR inner)
+// Columns advance in lockstep so that every operator application reads A once
+// for all of them; each column has its own step lengths and stops on its own
+// relative tolerance (a stopped column keeps alpha = 0).
+struct MColState {
+  double rs, alpha, beta, r0, rz;
+  int done;
+  int pad;
+};
+
+struct MCGGlobal {
+  int done;        // every column reached the inner tolerance
+  int iters;
+};
+
+// One block per (row chunk, column); per-column ordered reduction by the last block.
+__device__ __forceinline__ bool last_block_all(unsigned* ticket) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = atomicAdd(ticket, 1u);
+    s_last = (t == gridDim.x * gridDim.y - 1);
+  }
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last;
+}
+
+__global__ void __launch_bounds__(KT)
+k_mcg_init(const double* __restrict__ R64, long long ld, long long n, float* E, float* r, float* p, double* parts,
+           unsigned* ticket, MColState* cols, MCGGlobal* g) {
+  __shared__ double red[32];
+  const int c = blockIdx.y;
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float v = (float)R64[i + c * ld];
+    E[i + c * ld] = 0.f;
+    r[i + c * ld] = v;
+    p[i + c * ld] = v;
+    acc = fma((double)v, (double)v, acc);
+  }
+  const double b = block_sum(acc, red);
+  if (threadIdx.x == 0) parts[(long long)c * gridDim.x + blockIdx.x] = b;
+  if (last_block_all(ticket)) {
+    if (threadIdx.x < gridDim.y) {
+      const int cc = threadIdx.x;
+      double t = 0.0;
+      for (unsigned k = 0; k < gridDim.x; ++k) t += __ldcg(parts + (long long)cc * gridDim.x + k);
+      cols[cc].rs = t;
+      cols[cc].rz = t;
+      cols[cc].r0 = sqrt(t);
+      cols[cc].done = (t == 0.0) ? 1 : 0;
+      cols[cc].alpha = cols[cc].beta = 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int all = 1;
+      for (unsigned cc = 0; cc < gridDim.y; ++cc) all &= cols[cc].done;
+      g->done = all;
+      g->iters = 0;
+      *ticket = 0u;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(KT)
+k_mcg_pap(const float* __restrict__ p, const float* __restrict__ q, long long ld, long long n, double* parts,
+          unsigned* ticket, MColState* cols, const MCGGlobal* g) {
+  __shared__ double red[32];
+  if (g->done) return;
+  const int c = blockIdx.y;
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc = fma((double)p[i + c * ld], (double)q[i + c * ld], acc);
+  const double b = block_sum(acc, red);
+  if (threadIdx.x == 0) parts[(long long)c * gridDim.x + blockIdx.x] = b;
+  if (last_block_all(ticket)) {
+    if (threadIdx.x < gridDim.y) {
+      const int cc = threadIdx.x;
+      double t = 0.0;
+      for (unsigned k = 0; k < gridDim.x; ++k) t += __ldcg(parts + (long long)cc * gridDim.x + k);
+      if (cols[cc].done || !(t > 0.0) || !isfinite(t)) {
+        cols[cc].alpha = 0.0;
+        if (!cols[cc].done && !(t > 0.0)) cols[cc].done = 1;
+      } else {
+        cols[cc].alpha = cols[cc].rz / t;
+      }
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+  }
+}
+
+__global__ void __launch_bounds__(KT)
+k_mcg_xr(float* E, float* r, const float* __restrict__ p, const float* __restrict__ q, long long ld, long long n,
+         double* parts, unsigned* ticket, MColState* cols, MCGGlobal* g, double inner_tol, int precond) {
+  __shared__ double red[32];
+  if (g->done) return;
+  const int c = blockIdx.y;
+  const float a = (float)cols[c].alpha;
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long k = i + c * ld;
+    E[k] = fmaf(a, p[k], E[k]);
+    const float rn = fmaf(-a, q[k], r[k]);
+    r[k] = rn;
+    acc = fma((double)rn, (double)rn, acc);
+  }
+  const double b = block_sum(acc, red);
+  if (threadIdx.x == 0) parts[(long long)c * gridDim.x + blockIdx.x] = b;
+  if (last_block_all(ticket)) {
+    if (threadIdx.x < gridDim.y) {
+      const int cc = threadIdx.x;
+      double t = 0.0;
+      for (unsigned k = 0; k < gridDim.x; ++k) t += __ldcg(parts + (long long)cc * gridDim.x + k);
+      if (!cols[cc].done) {
+        if (!precond) {
+          cols[cc].beta = (cols[cc].rz > 0.0) ? t / cols[cc].rz : 0.0;
+          cols[cc].rz = t;
+        }
+        cols[cc].rs = t;
+        if (!(sqrt(t) > inner_tol * cols[cc].r0)) cols[cc].done = 1;
+      } else {
+        cols[cc].beta = 0.0;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int all = 1;
+      for (unsigned cc = 0; cc < gridDim.y; ++cc) all &= cols[cc].done;
+      g->done = all;
+      g->iters += 1;
+      *ticket = 0u;
+    }
+  }
+}
+
+// rz_new = r . z per column; initial (init != 0): rz = rz_new; else beta = rz_new / rz, rz = rz_new.
+__global__ void __launch_bounds__(KT)
+k_mcg_rz(const float* __restrict__ r, const float* __restrict__ z, long long ld, long long n, double* parts,
+         unsigned* ticket, MColState* cols, const MCGGlobal* g, int init) {
+  __shared__ double red[32];
+  if (!init && g->done) return;
+  const int c = blockIdx.y;
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc = fma((double)r[i + c * ld], (double)z[i + c * ld], acc);
+  const double b = block_sum(acc, red);
+  if (threadIdx.x == 0) parts[(long long)c * gridDim.x + blockIdx.x] = b;
+  if (last_block_all(ticket)) {
+    if (threadIdx.x < gridDim.y) {
+      const int cc = threadIdx.x;
+      double t = 0.0;
+      for (unsigned k = 0; k < gridDim.x; ++k) t += __ldcg(parts + (long long)cc * gridDim.x + k);
+      if (init) {
+        cols[cc].rz = t;
+      } else if (!cols[cc].done) {
+        cols[cc].beta = (cols[cc].rz != 0.0) ? t / cols[cc].rz : 0.0;
+        cols[cc].rz = t;
+      }
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+  }
+}
+
+__global__ void k_mcg_p(float* p, const float* __restrict__ r, long long ld, long long n, const MColState* cols,
+                        const MCGGlobal* g) {
+  if (g->done) return;
+  const int c = blockIdx.y;
+  if (cols[c].done) return;
+  const float bt = (float)cols[c].beta;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i + c * ld] = fmaf(bt, p[i + c * ld], r[i + c * ld]);
+}
+
+__global__ void k_add_cols(const float* __restrict__ E, long long lde, double* X, long long ldx, long long n) {
+  const int c = blockIdx.y;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    X[i + c * ldx] += (double)E[i + c * lde];
+}
+
+__global__ void k_copy_cols(const double* __restrict__ src, long long lds, double* dst, long long ldd, long long n) {
+  const int c = blockIdx.y;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i + c * ldd] = src[i + c * lds];
+}
+
 // ------------------------------------------------------------------ host side
 
-int colnorms_f64(const double* r, long long n, int nrhs, double* nrm2, cudaStream_t s) {
-  launch(k_colnorms, nrhs, KT, 0, s, r, n, nrm2);
+int colnorms_f64(const double* r, long long n, int nrhs, long long ld, double* nrm2, cudaStream_t s) {
+  launch(k_colnorms, nrhs, KT, 0, s, r, n, ld, nrm2);
   MPDOK_LAUNCH_CHECK("colnorms");
   return MPDOK_OK;
 }
@@ -430,21 +619,22 @@ static ArnState arn_state(const KWs& ws) {
   return st;
 }
 
-static int stored_apply32(const void* ctx, const float* x, float* y, int nrhs, cudaStream_t s, const int* skip) {
+static int stored_apply32(const void* ctx, const float* x, float* y, int nrhs, long long ld, cudaStream_t s,
+                          const int* skip) {
   const StoredCtx* c = (const StoredCtx*)ctx;
-  return gemv_launch(MPDOK_F32, false, c->A32, c->lda32, c->n, c->n, x, c->n, nrhs, y, c->n, 1.0, 0.0, nullptr, 0,
+  return gemv_launch(MPDOK_F32, false, c->A32, c->lda32, c->n, c->n, x, ld, nrhs, y, ld, 1.0, 0.0, nullptr, 0,
                      nullptr, c->gw, c->gbytes, s, false, skip);
 }
 
 static int stored_residual64(const void* ctx, const double* b, const double* x, double* r, double* nrm2, int nrhs,
-                             cudaStream_t s) {
+                             long long ld, cudaStream_t s) {
   const StoredCtx* c = (const StoredCtx*)ctx;
   if (nrhs == 1)
-    return gemv_launch(MPDOK_F64, false, c->A64, c->lda64, c->n, c->n, x, c->n, 1, r, c->n, -1.0, 1.0, b, c->n,
-                       nrm2, c->gw, c->gbytes, s, true, nullptr);
-  MPDOK_TRY(gemv_launch(MPDOK_F64, false, c->A64, c->lda64, c->n, c->n, x, c->n, nrhs, r, c->n, -1.0, 1.0, b, c->n,
+    return gemv_launch(MPDOK_F64, false, c->A64, c->lda64, c->n, c->n, x, ld, 1, r, ld, -1.0, 1.0, b, ld, nrm2,
+                       c->gw, c->gbytes, s, true, nullptr);
+  MPDOK_TRY(gemv_launch(MPDOK_F64, false, c->A64, c->lda64, c->n, c->n, x, ld, nrhs, r, ld, -1.0, 1.0, b, ld,
                         nullptr, c->gw, c->gbytes, s, true, nullptr));
-  return colnorms_f64(r, c->n, nrhs, nrm2, s);
+  return colnorms_f64(r, c->n, nrhs, ld, nrm2, s);
 }
 
 Operator32 stored_op32(const StoredCtx* c) {
@@ -500,7 +690,7 @@ int arnoldi_cycle(const KWs& ws, const Operator32& A, int m, int reorth, double 
       MPDOK_TRY(pc->apply(pc->ctx, vk, pc->z, s, &ws.sc->done));
       opnd = pc->z;
     }
-    MPDOK_TRY(A.apply(A.ctx, opnd, ws.w, 1, s, &ws.sc->done));
+    MPDOK_TRY(A.apply(A.ctx, opnd, ws.w, 1, ws.ldv, s, &ws.sc->done));
     double* Hcol = ws.H + (long long)k * st.ldh;
     launch(k_dots, ws.nblk, KT, smem_dots, s, ws.V, ws.ldv, k + 1, ws.w, n, ws.ch, ws.parts, ws.tickets + 0, Hcol, ws.sc);
     if (reorth >= 2) {
@@ -559,7 +749,7 @@ int ws_prepare(const KWs& ws, size_t work_bytes, cudaStream_t s) {
 }
 
 int fp64_residual(const KWs& ws, const Residual64& R, const double* b, const double* x, KScal* hs, cudaStream_t s) {
-  MPDOK_TRY(R.apply(R.ctx, b, x, ws.r64, &ws.sc->nrm2, 1, s));
+  MPDOK_TRY(R.apply(R.ctx, b, x, ws.r64, &ws.sc->nrm2, 1, ws.ldv, s));
   return read_scal(ws, hs, s);
 }
 
@@ -594,7 +784,7 @@ int gmres_core(const KWs& ws, const Operator32& A, const Residual64& R, const do
   KScal hs;
   for (int outer = 0; outer < max_restarts; ++outer) {
     // r = b32 - A32 x32 (FP32), start vector of the cycle.
-    MPDOK_TRY(A.apply(A.ctx, ws.x32, ws.w, 1, s, nullptr));
+    MPDOK_TRY(A.apply(A.ctx, ws.x32, ws.w, 1, ws.ldv, s, nullptr));
     launch(k_sub_from, vec_blocks(n), KT, 0, s, (const float*)ws.b32, ws.w, n);
     MPDOK_TRY(cycle_start_from_f32(ws, ws.w, s));
     MPDOK_TRY(read_scal(ws, &hs, s));
@@ -717,7 +907,7 @@ int cg_core(const KWs& ws, const Operator32& A, const Residual64& R, const doubl
   float* q = ws.q32;
   MPDOK_TRY(convert_any(b, MPDOK_F64, ws.b32, MPDOK_F32, n, s));
   MPDOK_TRY(convert_any(x, MPDOK_F64, xr, MPDOK_F32, n, s));
-  MPDOK_TRY(A.apply(A.ctx, xr, r, 1, s, nullptr));
+  MPDOK_TRY(A.apply(A.ctx, xr, r, 1, ws.ldv, s, nullptr));
   launch(k_sub_from, vec_blocks(n), KT, 0, s, (const float*)ws.b32, r, n);
   launch(k_norm2<float>, vec_blocks(n), KT, 0, s, (const float*)r, n, ws.parts, ws.tickets + 4, &ws.sc->nrm2);
   MPDOK_CUDA_TRY(cudaMemcpyAsync(p, r, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
@@ -741,7 +931,7 @@ int cg_core(const KWs& ws, const Operator32& A, const Residual64& R, const doubl
       prev = rel;
       if (hs.done) break;  // p.Ap == 0: nothing more to do
     }
-    MPDOK_TRY(A.apply(A.ctx, p, q, 1, s, &ws.sc->done));
+    MPDOK_TRY(A.apply(A.ctx, p, q, 1, ws.ldv, s, &ws.sc->done));
     launch(k_cg_pap, vec_blocks(n), KT, 0, s, (const float*)p, (const float*)q, n, ws.parts, ws.tickets + 0, ws.sc);
     launch(k_cg_xr, vec_blocks(n), KT, 0, s, xr, r, (const float*)p, (const float*)q, n, ws.parts, ws.tickets + 1,
            ws.sc);
@@ -758,6 +948,117 @@ int cg_core(const KWs& ws, const Operator32& A, const Residual64& R, const doubl
   }
   MPDOK_TRY(convert_any(xr, MPDOK_F32, x, MPDOK_F64, n, s));
   if (info) { info->converged = converged ? 1 : 0; info->inner_iters = it_done; }
+  return MPDOK_OK;
+}
+
+CgIrWs cgir_layout(long long n, int K, void* base) {
+  CgIrWs w;
+  w.n = n;
+  w.K = K;
+  w.ld = (long long)align_up((size_t)std::max(1LL, n), 64);
+  w.nblk = vec_blocks(n);
+  size_t off = 0;
+  auto take = [&](size_t b) { size_t o = off; off = align_up(off + b, 256); return o; };
+  const size_t fcol = (size_t)w.ld * K * sizeof(float);
+  const size_t dcol = (size_t)w.ld * K * sizeof(double);
+  size_t oR = take(dcol), oB = take(dcol), oX = take(dcol), oE = take(fcol), or_ = take(fcol), op = take(fcol),
+         oq = take(fcol), oz = take(fcol);
+  size_t oparts = take(sizeof(double) * (size_t)w.nblk * K + 64);
+  size_t ocols = take(sizeof(MColState) * K);
+  size_t og = take(64);
+  size_t onrm = take(sizeof(double) * K);
+  size_t otk = take(64);
+  w.total = off;
+  if (base) {
+    char* b = (char*)base;
+    w.R64 = (double*)(b + oR); w.B64 = (double*)(b + oB); w.X64 = (double*)(b + oX);
+    w.E = (float*)(b + oE); w.r = (float*)(b + or_); w.p = (float*)(b + op); w.q = (float*)(b + oq);
+    w.z = (float*)(b + oz);
+    w.parts = (double*)(b + oparts); w.cols = (void*)(b + ocols); w.g = (void*)(b + og);
+    w.nrm2 = (double*)(b + onrm); w.ticket = (unsigned*)(b + otk);
+  }
+  return w;
+}
+
+int cg_ir_core(const CgIrWs& w, const Operator32& A, const Residual64& R, const double* B, long long ldb, double* X,
+               long long ldx, double tol, int maxiter_outer, double inner_tol, int inner_maxiter, const Precond* pc,
+               mpdok_solve_info* info, cudaStream_t s) {
+  const long long n = w.n;
+  const int K = w.K;
+  const long long ld = w.ld;
+  MColState* cols = (MColState*)w.cols;
+  MCGGlobal* g = (MCGGlobal*)w.g;
+  dim3 grid(w.nblk, K);
+  MPDOK_CUDA_TRY(cudaMemsetAsync(w.ticket, 0, 64, s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(w.X64, 0, sizeof(double) * ld * K, s));
+  launch(k_copy_cols, grid, KT, 0, s, B, ldb, w.B64, ld, n);
+  // ||B_j||
+  MPDOK_TRY(colnorms_f64(w.B64, n, K, ld, w.nrm2, s));
+  std::vector<double> bn(K), rn(K);
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(bn.data(), w.nrm2, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int j = 0; j < K; ++j) bn[j] = std::sqrt(bn[j]);  // colnorms_f64 returns squared norms
+  if (info) info->bnorm = *std::max_element(bn.begin(), bn.end());
+  bool converged = false;
+  int inner_total = 0;
+  for (int outer = 0; outer <= maxiter_outer; ++outer) {
+    MPDOK_TRY(R.apply(R.ctx, w.B64, w.X64, w.R64, w.nrm2, K, ld, s));
+    MPDOK_CUDA_TRY(cudaMemcpyAsync(rn.data(), w.nrm2, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+    MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+    double worst = 0.0;
+    for (int j = 0; j < K; ++j) {
+      const double rel = bn[j] > 0 ? std::sqrt(rn[j]) / bn[j] : 0.0;
+      worst = std::max(worst, rel);
+    }
+    hist_push(info, outer, worst);
+    if (!std::isfinite(worst)) { set_error("CG-IR: non-finite residual"); return MPDOK_ERR_NONFINITE; }
+    if (worst < tol) { converged = true; break; }
+    if (outer == maxiter_outer) break;
+    // inner FP32 CG on A E = R, all columns in lockstep
+    launch(k_mcg_init, grid, KT, 0, s, (const double*)w.R64, ld, n, w.E, w.r, w.p, w.parts, w.ticket, cols, g);
+    if (pc) {
+      // z = M^-1 r, p = z, rz = r . z
+      for (int c = 0; c < K; ++c) MPDOK_TRY(pc->apply(pc->ctx, w.r + (long long)c * ld, w.z + (long long)c * ld, s, nullptr));
+      launch(k_mcg_rz, grid, KT, 0, s, (const float*)w.r, (const float*)w.z, ld, n, w.parts, w.ticket + 3, cols,
+             (const MCGGlobal*)g, 1);
+      MPDOK_CUDA_TRY(cudaMemcpyAsync(w.p, w.z, sizeof(float) * ld * K, cudaMemcpyDeviceToDevice, s));
+    }
+    MCGGlobal hg{0, 0};
+    int it = 0;
+    while (it < inner_maxiter) {
+      const int batch = std::min(20, inner_maxiter - it);
+      for (int b = 0; b < batch; ++b) {
+        MPDOK_TRY(A.apply(A.ctx, w.p, w.q, K, ld, s, &g->done));
+        launch(k_mcg_pap, grid, KT, 0, s, (const float*)w.p, (const float*)w.q, ld, n, w.parts, w.ticket + 1, cols,
+               (const MCGGlobal*)g);
+        launch(k_mcg_xr, grid, KT, 0, s, w.E, w.r, (const float*)w.p, (const float*)w.q, ld, n, w.parts,
+               w.ticket + 2, cols, g, inner_tol, pc ? 1 : 0);
+        if (pc) {
+          for (int c = 0; c < K; ++c)
+            MPDOK_TRY(pc->apply(pc->ctx, w.r + (long long)c * ld, w.z + (long long)c * ld, s, &g->done));
+          launch(k_mcg_rz, grid, KT, 0, s, (const float*)w.r, (const float*)w.z, ld, n, w.parts, w.ticket + 3, cols,
+                 (const MCGGlobal*)g, 0);
+        }
+        launch(k_mcg_p, grid, KT, 0, s, w.p, (const float*)(pc ? w.z : w.r), ld, n, (const MColState*)cols,
+               (const MCGGlobal*)g);
+      }
+      MPDOK_LAUNCH_CHECK("cg-ir inner");
+      it += batch;
+      MPDOK_CUDA_TRY(cudaMemcpyAsync(&hg, g, sizeof(hg), cudaMemcpyDeviceToHost, s));
+      MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+      if (hg.done) break;
+    }
+    inner_total += hg.iters;
+    launch(k_add_cols, grid, KT, 0, s, (const float*)w.E, ld, w.X64, ld, n);
+    MPDOK_LAUNCH_CHECK("cg-ir update");
+    if (info) info->outer_iters = outer + 1;
+  }
+  launch(k_copy_cols, grid, KT, 0, s, (const double*)w.X64, ld, X, ldx, n);
+  MPDOK_LAUNCH_CHECK("cg-ir out");
+  if (info) {
+    info->converged = converged ? 1 : 0;
+    info->inner_iters = inner_total;
+  }
   return MPDOK_OK;
 }
 

@@ -37,16 +37,32 @@ struct KWs {
 
 KWs krylov_layout(long long n, int m, void* base);
 
-// FP32 operator y = A x (nrhs columns, leading dimension n) used by the
-// Krylov bodies; `skip` predicates the launches on a device flag.
+// Workspace of a multi-RHS CG-IR solve (n x K blocks, leading dimension ld).
+struct CgIrWs {
+  long long n = 0, ld = 0;
+  int K = 1;
+  unsigned nblk = 1;
+  double *R64 = nullptr, *B64 = nullptr, *X64 = nullptr, *parts = nullptr, *nrm2 = nullptr;
+  float *E = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr;
+  void *cols = nullptr, *g = nullptr;
+  unsigned* ticket = nullptr;
+  size_t total = 0;
+};
+CgIrWs cgir_layout(long long n, int K, void* base);
+
+// FP32 operator y = A x (nrhs columns, leading dimension ld for x and y, ld a
+// multiple of 4) used by the Krylov bodies; `skip` predicates the launches on
+// a device flag.
 struct Operator32 {
-  int (*apply)(const void* ctx, const float* x, float* y, int nrhs, cudaStream_t s, const int* skip) = nullptr;
+  int (*apply)(const void* ctx, const float* x, float* y, int nrhs, long long ld, cudaStream_t s,
+               const int* skip) = nullptr;
   const void* ctx = nullptr;
 };
 
-// FP64 residual r = b - A x (nrhs columns) with per-column ||r||^2 into nrm2[0..nrhs).
+// FP64 residual r = b - A x (nrhs columns, leading dimension ld) with
+// per-column ||r||^2 into nrm2[0..nrhs).
 struct Residual64 {
-  int (*apply)(const void* ctx, const double* b, const double* x, double* r, double* nrm2, int nrhs,
+  int (*apply)(const void* ctx, const double* b, const double* x, double* r, double* nrm2, int nrhs, long long ld,
                cudaStream_t s) = nullptr;
   const void* ctx = nullptr;
 };
@@ -84,7 +100,7 @@ int cycle_start_from_f64(const KWs& ws, const double* src64, cudaStream_t s);
 
 int read_scal(const KWs& ws, KScal* host, cudaStream_t s);
 int norm2_f64(const KWs& ws, const double* x, long long n, double* out_dev, cudaStream_t s);
-int colnorms_f64(const double* r, long long n, int nrhs, double* nrm2, cudaStream_t s);
+int colnorms_f64(const double* r, long long n, int nrhs, long long ld, double* nrm2, cudaStream_t s);
 // FP64 residual r64 = b - A x through R, ||r||^2 into sc->nrm2, then the
 // scalar block is read back to the host.
 int fp64_residual(const KWs& ws, const Residual64& R, const double* b, const double* x, KScal* hs, cudaStream_t s);
@@ -96,6 +112,12 @@ int gmres_ir_core(const KWs& ws, const Operator32& A, const Residual64& R, const
                   int maxiter_outer, int restart, double inner_tol, const Precond* pc, mpdok_solve_info* info,
                   cudaStream_t s);
 int ws_prepare(const KWs& ws, size_t work_bytes, cudaStream_t s);
+// CG-IR: FP64 residual R = B - A X through R, inner FP32 CG on A E = R for all
+// columns in lockstep (relative inner tolerance, inner_maxiter), X += E in FP64.
+// pc (optional): inner PCG with z = M^-1 r applied per column.
+int cg_ir_core(const CgIrWs& w, const Operator32& A, const Residual64& R, const double* B, long long ldb, double* X,
+               long long ldx, double tol, int maxiter_outer, double inner_tol, int inner_maxiter, const Precond* pc,
+               mpdok_solve_info* info, cudaStream_t s);
 int dense_gmres_ir_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* b, double* x,
                         double tol, int maxiter_outer, int restart, int maxiter_inner, mpdok_solve_info* info,
                         cudaStream_t s);

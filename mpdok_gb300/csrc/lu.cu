@@ -21,6 +21,8 @@
 // are handed out in order, so a block only ever waits on blocks that are
 // already running; every wait is bounded and reports a timeout.
 #include "krylov.cuh"
+#include "matfree.cuh"
+#include "split.cuh"
 #include "tc_gemm.cuh"
 
 #include <cmath>
@@ -968,4 +970,117 @@ extern "C" int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* 
   c.gbytes = ws.gbytes;
   return gmres_ir_core(ws, stored_op32(&c), stored_res64(&c), b, x, tol, maxiter_outer, restart, inner_tol, &pc, info,
                        s);
+}
+
+// --------------------------------------------------- LU-preconditioned CG-IR
+// CG-IR whose inner CG is preconditioned by the BF16/FP16 factors (PCG, z =
+// (LU)^-1 r per column): the FP32 CG body then works on a well-conditioned
+// operator, which it needs once kappa(A) * 6e-8 >= 1 (the C2 family).
+// op_mode 0: FP32 copy of A + native FP64 residual; 1: split A for both;
+// 2: matrix-free (coords) FP32 inside, FP64 matrix-free residual.
+extern "C" size_t mpdok_lu_cg_ir_workspace_size(long long n, int nrhs, int op_mode) {
+  if (n < 0 || nrhs < 1 || nrhs > 8 || op_mode < 0 || op_mode > 2) return 0;
+  size_t g;
+  if (op_mode == 0)
+    g = std::max(gemv_workspace_bytes(MPDOK_F32, n, n, nrhs, false), gemv_workspace_bytes(MPDOK_F64, n, n, nrhs, false));
+  else if (op_mode == 1)
+    g = split_gemv_work_bytes(n, n, nrhs);
+  else
+    g = align_up(matfree_work_bytes(n, n, nrhs, MPDOK_F32), 256) + matfree_work_bytes(n, n, nrhs, MPDOK_F64);
+  return align_up(apply_layout(n).total, 256) + align_up(cgir_layout(n, nrhs, nullptr).total, 256) + align_up(g, 256) +
+         256;
+}
+
+static int lu_cg_ir_run(const Operator32& A, const Residual64& R, long long n, const void* factors, int fdtype, int nrhs,
+                        const double* B, long long ldb, double* X, long long ldx, double tol, int maxiter_outer,
+                        double inner_tol, int inner_maxiter, char* awork, const CgIrWs& w, mpdok_solve_info* info,
+                        cudaStream_t s) {
+  LUMeta hm;
+  MPDOK_TRY(read_meta(factors, n, fdtype, &hm, s));
+  if (!hm.valid || hm.fdtype != fdtype || hm.n_lo != (int)(n & 0x7fffffff)) {
+    set_error("no factorization of this size / type in the factor buffer");
+    return MPDOK_ERR_NOT_FACTORED;
+  }
+  PcCtx ctx{factors, n, fdtype, awork};
+  Precond pc;
+  pc.apply = pc_apply;
+  pc.ctx = &ctx;
+  return cg_ir_core(w, A, R, B, ldb, X, ldx, tol, maxiter_outer, inner_tol, inner_maxiter, &pc, info, s);
+}
+
+extern "C" int mpdok_lu_cg_ir(const double* A64, long long lda, long long n, int op_mode, void* opbuf, int op_ready,
+                              const void* factors, int fdtype, int nrhs, const double* B, long long ldb, double* X,
+                              long long ldx, double tol, int maxiter_outer, double inner_tol, int inner_maxiter,
+                              void* work, size_t work_bytes, mpdok_solve_info* info, cudaStream_t s) {
+  if (info) std::memset(info, 0, sizeof(*info));
+  MPDOK_ARG_CHECK(n >= 0, "negative n");
+  MPDOK_ARG_CHECK(op_mode == 0 || op_mode == 1, "op_mode must be 0 (FP32 copy) or 1 (split)");
+  MPDOK_ARG_CHECK(nrhs >= 1 && nrhs <= 8, "nrhs must be in 1..8");
+  if (n == 0) { if (info) info->converged = 1; return MPDOK_OK; }
+  MPDOK_ARG_CHECK(A64 && opbuf && factors && B && X && work, "null pointer");
+  MPDOK_ARG_CHECK(work_bytes >= mpdok_lu_cg_ir_workspace_size(n, nrhs, op_mode), "workspace too small");
+  char* wb = (char*)work;
+  char* awork = wb;
+  const size_t a_bytes = align_up(apply_layout(n).total, 256);
+  CgIrWs w = cgir_layout(n, nrhs, wb + a_bytes);
+  char* gw = wb + a_bytes + align_up(w.total, 256);
+  const size_t gbytes = work_bytes - a_bytes - align_up(w.total, 256);
+  const long long ld = (long long)align_up((size_t)n, 4);
+  if (op_mode == 0) {
+    float* A32 = (float*)opbuf;
+    if (!op_ready) MPDOK_TRY(convert_matrix_f64_f32(A64, lda, A32, ld, n, n, s));
+    StoredCtx c;
+    c.A32 = A32;
+    c.lda32 = ld;
+    c.A64 = A64;
+    c.lda64 = lda;
+    c.n = n;
+    c.gw = gw;
+    c.gbytes = gbytes;
+    return lu_cg_ir_run(stored_op32(&c), stored_res64(&c), n, factors, fdtype, nrhs, B, ldb, X, ldx, tol,
+                        maxiter_outer, inner_tol, inner_maxiter, awork, w, info, s);
+  }
+  float* hi = (float*)opbuf;
+  float* lo = (float*)((char*)opbuf + align_up((size_t)ld * n * sizeof(float), 256));
+  if (!op_ready) MPDOK_TRY(split_matrix(A64, lda, n, n, hi, lo, ld, s));
+  SplitCtx c;
+  c.hi = hi;
+  c.lo = lo;
+  c.ld = ld;
+  c.n = n;
+  c.work = gw;
+  c.work_bytes = gbytes;
+  return lu_cg_ir_run(split_op32(&c), split_res64(&c), n, factors, fdtype, nrhs, B, ldb, X, ldx, tol, maxiter_outer,
+                      inner_tol, inner_maxiter, awork, w, info, s);
+}
+
+extern "C" int mpdok_mf_lu_cg_ir(const double* coords, long long n, int dim, int kernel, double gamma, double reg,
+                                 const void* factors, int fdtype, int nrhs, const double* B, long long ldb, double* X,
+                                 long long ldx, double tol, int maxiter_outer, double inner_tol, int inner_maxiter,
+                                 void* work, size_t work_bytes, mpdok_solve_info* info, cudaStream_t s) {
+  if (info) std::memset(info, 0, sizeof(*info));
+  MPDOK_ARG_CHECK(n >= 0, "negative n");
+  MPDOK_ARG_CHECK(nrhs >= 1 && nrhs <= 8, "nrhs must be in 1..8");
+  if (n == 0) { if (info) info->converged = 1; return MPDOK_OK; }
+  MPDOK_ARG_CHECK(coords && factors && B && X && work, "null pointer");
+  MPDOK_ARG_CHECK(work_bytes >= mpdok_lu_cg_ir_workspace_size(n, nrhs, 2), "workspace too small");
+  char* wb = (char*)work;
+  const size_t a_bytes = align_up(apply_layout(n).total, 256);
+  CgIrWs w = cgir_layout(n, nrhs, wb + a_bytes);
+  char* base = wb + a_bytes + align_up(w.total, 256);
+  MfCtx c;
+  c.op.rows = coords;
+  c.op.cols = coords;
+  c.op.nrows = n;
+  c.op.ncols = n;
+  c.op.dim = dim;
+  c.op.kernel = kernel;
+  c.op.gamma = gamma;
+  c.op.reg = reg;
+  c.w32 = base;
+  c.w32_bytes = matfree_work_bytes(n, n, nrhs, MPDOK_F32);
+  c.w64 = base + align_up(c.w32_bytes, 256);
+  c.w64_bytes = matfree_work_bytes(n, n, nrhs, MPDOK_F64);
+  return lu_cg_ir_run(mf_op32(&c), mf_res64(&c), n, factors, fdtype, nrhs, B, ldb, X, ldx, tol, maxiter_outer,
+                      inner_tol, inner_maxiter, wb, w, info, s);
 }

@@ -381,18 +381,17 @@ int matfree_apply(const MfOperand& op, int precision, const void* X, long long l
 
 // Krylov operator adapters -------------------------------------------------
 
-static int mf_apply32(const void* ctx, const float* x, float* y, int nrhs, cudaStream_t s, const int* skip) {
+static int mf_apply32(const void* ctx, const float* x, float* y, int nrhs, long long ld, cudaStream_t s,
+                      const int* skip) {
   const MfCtx* c = (const MfCtx*)ctx;
-  return matfree_apply(c->op, MPDOK_F32, x, c->op.ncols, nrhs, y, c->op.nrows, 1.0, 0.0, nullptr, 0, c->w32,
-                       c->w32_bytes, s, skip);
+  return matfree_apply(c->op, MPDOK_F32, x, ld, nrhs, y, ld, 1.0, 0.0, nullptr, 0, c->w32, c->w32_bytes, s, skip);
 }
 
 static int mf_residual64(const void* ctx, const double* b, const double* x, double* r, double* nrm2, int nrhs,
-                         cudaStream_t s) {
+                         long long ld, cudaStream_t s) {
   const MfCtx* c = (const MfCtx*)ctx;
-  MPDOK_TRY(matfree_apply(c->op, MPDOK_F64, x, c->op.ncols, nrhs, r, c->op.nrows, -1.0, 1.0, b, c->op.nrows, c->w64,
-                          c->w64_bytes, s, nullptr));
-  return colnorms_f64(r, c->op.nrows, nrhs, nrm2, s);
+  MPDOK_TRY(matfree_apply(c->op, MPDOK_F64, x, ld, nrhs, r, ld, -1.0, 1.0, b, ld, c->w64, c->w64_bytes, s, nullptr));
+  return colnorms_f64(r, c->op.nrows, nrhs, ld, nrm2, s);
 }
 
 Operator32 mf_op32(const MfCtx* c) {
@@ -443,8 +442,8 @@ extern "C" int mpdok_matfree_apply(const double* rows, long long n_rows, const d
 
 extern "C" size_t mpdok_mf_krylov_workspace_size(long long n, int restart) {
   if (n < 0 || restart < 1) return 0;
-  return krylov_layout(n, restart, nullptr).total + matfree_work_bytes(n, n, 1, MPDOK_F32) +
-         matfree_work_bytes(n, n, 1, MPDOK_F64) + 512;
+  return krylov_layout(n, restart, nullptr).total + matfree_work_bytes(n, n, 8, MPDOK_F32) +
+         matfree_work_bytes(n, n, 8, MPDOK_F64) + 512;
 }
 
 static int mf_setup(const double* coords, long long n, int dim, int kernel, double gamma, double reg, int restart,
@@ -463,11 +462,11 @@ static int mf_setup(const double* coords, long long n, int dim, int kernel, doub
   c->op.reg = reg;
   c->op.diag_offset = 0;
   c->w32 = w;
-  c->w32_bytes = matfree_work_bytes(n, n, 1, MPDOK_F32);
+  c->w32_bytes = matfree_work_bytes(n, n, 8, MPDOK_F32);
   c->w64 = w + align_up(c->w32_bytes, 256);
-  c->w64_bytes = matfree_work_bytes(n, n, 1, MPDOK_F64);
+  c->w64_bytes = matfree_work_bytes(n, n, 8, MPDOK_F64);
   // pack the centres once for every FP32 apply of the solve
-  const MfPlan p = mf_plan(n, n, 1, false);
+  const MfPlan p = mf_plan(n, n, 8, false);
   float4* rp = (float4*)(w + p.part_bytes + 256);
   launch(k_pack_coords, (unsigned)std::min<long long>((n + 255) / 256, 1024), 256, 0, s, coords, n, dim, rp);
   MPDOK_LAUNCH_CHECK("pack");

@@ -183,3 +183,56 @@ def gmres_ir(op, b, tol: float = 1e-11, maxiter_outer: int = 5, restart: int = 5
         for it, r in hist:
             print(f"  GMRES-IR outer {it:2d}  rel_res(FP64) = {r:.3e}")
     return x, hist, bool(info.converged)
+
+
+def cg_ir(op, B, tol: float = 1e-12, maxiter_outer: int = 10, inner_tol: float = 1e-6, inner_maxiter: int = 500,
+          split: bool = False, precond=None):
+    """Multi-RHS CG with FP64 refinement (the FP32 CG body of dense_krylov.py:119-205
+    inside the refinement loop of :338-421).
+
+    B: (N,) or (N, k<=8).  ``split=True`` stores A as two FP32 slices and forms
+    every product with error-free FP32 arithmetic (FP64-level accuracy on the
+    FP32 pipe) for both the inner operator and the residual.  ``precond`` (an
+    ``mpdok_gb300.lu.LUFactorization``) preconditions the inner CG, which an
+    FP32 CG body needs once kappa(A) * 6e-8 >= 1.
+    Returns ``(X_fp64, history, converged)``; history holds the worst column.
+    """
+    if getattr(op, "_matrix_free", False):
+        return op.cg_ir(B, tol=tol, maxiter_outer=maxiter_outer, inner_tol=inner_tol, inner_maxiter=inner_maxiter,
+                        precond=precond)
+    _require_fp64(op, "cg_ir")
+    from ._device import as_columns
+    n = op.N
+    Bc = as_columns(B, torch.float64)
+    k = Bc.shape[1]
+    if k > 8:
+        raise ValueError("cg_ir handles up to 8 right-hand sides per call")
+    X = fortran_empty(n, k, torch.float64)
+    lib = N.load()
+    mode = 1 if split else 0
+    ld4 = (n + 3) // 4 * 4
+    if mode == 0 and ld4 == n:
+        opbuf, ready = op.A_fp32, 1
+    else:
+        cache = getattr(op, "_cgir_opbuf", None)
+        if cache is None or cache[0] != mode:
+            buf = torch.empty(lib.mpdok_cg_ir_operator_size(n, mode), dtype=torch.uint8, device=Bc.device)
+            op._cgir_opbuf = (mode, buf)
+            ready = 0
+        else:
+            buf, ready = cache[1], 1
+        opbuf = buf
+    info = N.SolveInfo()
+    if precond is None:
+        w = op._ws.get(lib.mpdok_cg_ir_workspace_size(n, k, mode))
+        N.check(lib.mpdok_cg_ir(ptr(op.A_fp64), n, n, mode, ptr(opbuf), ready, k, ptr(Bc), n, ptr(X), n,
+                                float(tol), int(maxiter_outer), float(inner_tol), int(inner_maxiter), ptr(w),
+                                w.numel(), ctypes.byref(info), stream_handle()), "cg_ir")
+    else:
+        w = op._ws.get(lib.mpdok_lu_cg_ir_workspace_size(n, k, mode))
+        N.check(lib.mpdok_lu_cg_ir(ptr(op.A_fp64), n, n, mode, ptr(opbuf), ready, ptr(precond.factors),
+                                   precond.fdtype, k, ptr(Bc), n, ptr(X), n, float(tol), int(maxiter_outer),
+                                   float(inner_tol), int(inner_maxiter), ptr(w), w.numel(), ctypes.byref(info),
+                                   stream_handle()), "lu_cg_ir")
+    hist = info.history_list()
+    return (X.reshape(-1) if torch.as_tensor(B).dim() == 1 else X), hist, bool(info.converged)

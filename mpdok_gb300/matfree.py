@@ -101,5 +101,29 @@ class MatrixFreeOperator:
                                 stream_handle()), "mf_cg")
         return x, info.history_list(), bool(info.converged)
 
+    def cg_ir(self, B, tol=1e-12, maxiter_outer=10, inner_tol=1e-6, inner_maxiter=500, precond=None):
+        """Multi-RHS CG-IR on the matrix-free operator (optionally LU-preconditioned)."""
+        Bc = as_columns(B, torch.float64)
+        k = Bc.shape[1]
+        if k > 8:
+            raise ValueError("cg_ir handles up to 8 right-hand sides per call")
+        X = fortran_empty(self.N, k, torch.float64)
+        lib = N.load()
+        info = N.SolveInfo()
+        if precond is None:
+            w = self._ws.get(lib.mpdok_mf_cg_ir_workspace_size(self.N, k))
+            N.check(lib.mpdok_mf_cg_ir(ptr(self.coords), self.N, self.dim, self.kcode, self.gamma, self.reg, k,
+                                       ptr(Bc), self.N, ptr(X), self.N, float(tol), int(maxiter_outer),
+                                       float(inner_tol), int(inner_maxiter), ptr(w), w.numel(), ctypes.byref(info),
+                                       stream_handle()), "mf_cg_ir")
+        else:
+            w = self._ws.get(lib.mpdok_lu_cg_ir_workspace_size(self.N, k, 2))
+            N.check(lib.mpdok_mf_lu_cg_ir(ptr(self.coords), self.N, self.dim, self.kcode, self.gamma, self.reg,
+                                          ptr(precond.factors), precond.fdtype, k, ptr(Bc), self.N, ptr(X), self.N,
+                                          float(tol), int(maxiter_outer), float(inner_tol), int(inner_maxiter),
+                                          ptr(w), w.numel(), ctypes.byref(info), stream_handle()), "mf_lu_cg_ir")
+        squeeze = torch.as_tensor(B).dim() == 1 if not isinstance(B, torch.Tensor) else B.dim() == 1
+        return (X.reshape(-1) if squeeze else X), info.history_list(), bool(info.converged)
+
     def __repr__(self):
         return f"MatrixFreeOperator(N={self.N:,}, dim={self.dim}, kernel={self.kernel}, gamma={self.gamma:g})"
