@@ -260,6 +260,29 @@ MPDOK_API int mpdok_mf_lu_cg_ir(const double* coords, long long n, int dim, int 
                                 long long ldx, double tol, int maxiter_outer, double inner_tol, int inner_maxiter,
                                 void* work, size_t work_bytes, mpdok_solve_info* info, cudaStream_t stream);
 
+/* -------------------------------------------------------- out-of-core (OOC)
+ * FP32 A of an RBF system kept outside HBM and streamed per product
+ * (mpdok_ooc.py:51-383).  store 0: pinned host RAM (N*N*4 bytes, allocated
+ * here); store 1: raw row-major FP32 file without a header at `path` (the
+ * reference's SSD format), read through pinned staging.  Tiles of tile_rows
+ * rows are copied on a side stream into a ring of device buffers while the
+ * previous tile is multiplied.  The handle owns its device buffers. */
+MPDOK_API int mpdok_ooc_create(long long n, int tile_rows, int store, const char* path, void** handle);
+MPDOK_API int mpdok_ooc_destroy(void* handle);
+MPDOK_API int mpdok_ooc_build(void* handle, const double* coords, int dim, int kernel, double gamma, double reg,
+                              cudaStream_t stream);
+MPDOK_API int mpdok_ooc_matvec(void* handle, const float* x, float* y, cudaStream_t stream);
+MPDOK_API double mpdok_ooc_bytes_moved(void* handle);
+/* Host copy of rows [row0, row0 + rows) of the stored matrix (row-major FP32). */
+MPDOK_API int mpdok_ooc_read_rows(void* handle, long long row0, long long rows, float* dst);
+/* GMRES-IR of MPDOKOOCSolver.solve: outer FP64 residual recomputed matrix-free
+ * from coords, inner FP32 GMRES on the streamed operator. */
+MPDOK_API size_t mpdok_ooc_workspace_size(long long n, int restart);
+MPDOK_API int mpdok_ooc_gmres_ir(void* handle, const double* coords, int dim, int kernel, double gamma, double reg,
+                                 const double* b, double* x, double tol, int maxiter_outer, int restart,
+                                 double inner_tol, void* work, size_t work_bytes, mpdok_solve_info* info,
+                                 cudaStream_t stream);
+
 /* --------------------------------------------------------- instrumentation
  * mpdok_launch_count: kernels launched by this library since load.
  * mpdok_profile_enable(1) clears and starts per-launch CUDA-event timing of

@@ -136,6 +136,16 @@ _SIGS = {
     "mpdok_mf_lu_cg_ir": (c_int, [c_void_p, c_ll, c_int, c_int, c_double, c_double, c_void_p, c_int, c_int, c_void_p,
                                   c_ll, c_void_p, c_ll, c_double, c_int, c_double, c_int, c_void_p, c_size_t,
                                   ctypes.POINTER(SolveInfo), c_void_p]),
+    "mpdok_ooc_create": (c_int, [c_ll, c_int, c_int, ctypes.c_char_p, ctypes.POINTER(c_void_p)]),
+    "mpdok_ooc_destroy": (c_int, [c_void_p]),
+    "mpdok_ooc_build": (c_int, [c_void_p, c_void_p, c_int, c_int, c_double, c_double, c_void_p]),
+    "mpdok_ooc_matvec": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "mpdok_ooc_bytes_moved": (c_double, [c_void_p]),
+    "mpdok_ooc_read_rows": (c_int, [c_void_p, c_ll, c_ll, c_void_p]),
+    "mpdok_ooc_workspace_size": (c_size_t, [c_ll, c_int]),
+    "mpdok_ooc_gmres_ir": (c_int, [c_void_p, c_void_p, c_int, c_int, c_double, c_double, c_void_p, c_void_p,
+                                   c_double, c_int, c_int, c_double, c_void_p, c_size_t, ctypes.POINTER(SolveInfo),
+                                   c_void_p]),
     "mpdok_launch_count": (c_ll, []),
     "mpdok_profile_enable": (c_int, [c_int]),
     "mpdok_profile_query": (c_int, [c_int, ctypes.POINTER(c_double), ctypes.POINTER(c_ll), ctypes.POINTER(c_double)]),

@@ -159,4 +159,10 @@ inline void launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaS
 int prof_start(int cls, cudaStream_t s);
 void prof_stop(int slot, cudaStream_t s, double work);
 
+// Row-major FP32 RBF tile computed in FP64 and rounded once, nugget added in
+// FP32 after the rounding (the reference's out-of-core tile).
+int rbf_tile_f32_from_f64(const double* rows, long long n_rows, const double* cols, long long n_cols, int dim,
+                          int kernel, double gamma, double reg, long long diag_offset, float* out, long long ld,
+                          cudaStream_t s);
+
 }  // namespace mpdok

@@ -21,6 +21,15 @@ namespace mpdok {
 constexpr int ASM_ROWS = 128;  // rows per block (4 per thread x 32 lanes)
 constexpr int ASM_COLS = 64;   // columns per block (8 warps x 8 columns)
 
+// Diagonal nugget of the FP64-math path: FP64 output adds it in FP64; FP32
+// output rounds phi first and adds the nugget in FP32, the order of
+// mpdok_ooc.py:45,122 (astype(float32), then tile[k, i+k] += reg).
+template <typename OutT>
+__device__ __forceinline__ double nugget(double v, double reg) {
+  if (std::is_same<OutT, float>::value) return (double)((float)v + (float)reg);
+  return v + reg;
+}
+
 template <int D, int KIND, typename OutT, bool COLMAJOR, bool F64MATH>
 __global__ void __launch_bounds__(256)
 rbf_assemble_kernel(const double* __restrict__ R, long long nr,
@@ -61,7 +70,7 @@ rbf_assemble_kernel(const double* __restrict__ R, long long nr,
 #pragma unroll
           for (int k = 0; k < D; ++k) { double t = (double)sR[il * D + k] - (double)sC[jl * D + k]; d2 = fma(t, t, d2); }
           v = (KIND == MPDOK_KERNEL_GAUSSIAN) ? exp(-gamma * d2) : sqrt(fma(gamma, d2, 1.0));
-          if (i + diag_off == j) v += reg;
+          if (i + diag_off == j) v = nugget<OutT>(v, reg);
         } else {
           float d2 = 0.f;
 #pragma unroll
@@ -91,7 +100,7 @@ rbf_assemble_kernel(const double* __restrict__ R, long long nr,
 #pragma unroll
           for (int k = 0; k < D; ++k) { double t = (double)sR[il * D + k] - (double)sC[jl * D + k]; d2 = fma(t, t, d2); }
           v = (KIND == MPDOK_KERNEL_GAUSSIAN) ? exp(-gamma * d2) : sqrt(fma(gamma, d2, 1.0));
-          if (i + diag_off == j) v += reg;
+          if (i + diag_off == j) v = nugget<OutT>(v, reg);
         } else {
           float d2 = 0.f;
 #pragma unroll
@@ -118,6 +127,15 @@ static void launch_asm(const double* R, long long nr, const double* C, long long
     launch(rbf_assemble_kernel<D, KIND, OutT, false, F64>, grid, 256, 0, s, R, nr, C, nc, gamma, reg, diag_off, (OutT*)out, ld);
 }
 
+// FP32 row-major tile computed in FP64 and rounded once (the reference's
+// out-of-core tile, mpdok_ooc.py:39-46).
+template <int D, int KIND>
+static void launch_f32_exact(const double* R, long long nr, const double* C, long long nc, double gamma, double reg,
+                             long long diag_off, float* out, long long ld, cudaStream_t s) {
+  dim3 grid((unsigned)((nr + ASM_ROWS - 1) / ASM_ROWS), (unsigned)((nc + ASM_COLS - 1) / ASM_COLS));
+  launch(rbf_assemble_kernel<D, KIND, float, false, true>, grid, 256, 0, s, R, nr, C, nc, gamma, reg, diag_off, out, ld);
+}
+
 template <int D, int KIND>
 static int dispatch_dtype(int dt, const double* R, long long nr, const double* C, long long nc, double gamma,
                           double reg, long long doff, void* out, long long ld, bool cm, cudaStream_t s) {
@@ -128,6 +146,26 @@ static int dispatch_dtype(int dt, const double* R, long long nr, const double* C
     case MPDOK_F16: launch_asm<D, KIND, __half>(R, nr, C, nc, gamma, reg, doff, out, ld, cm, s); break;
     default: set_error("rbf_assemble: unknown out dtype %d", dt); return MPDOK_ERR_INVALID_ARG;
   }
+  return MPDOK_OK;
+}
+
+int rbf_tile_f32_from_f64(const double* rows, long long n_rows, const double* cols, long long n_cols, int dim,
+                          int kernel, double gamma, double reg, long long diag_offset, float* out, long long ld,
+                          cudaStream_t s) {
+  MPDOK_ARG_CHECK(dim >= 1 && dim <= 3, "dim must be 1, 2 or 3");
+  MPDOK_ARG_CHECK(kernel == MPDOK_KERNEL_GAUSSIAN || kernel == MPDOK_KERNEL_MQ, "unknown kernel");
+  MPDOK_ARG_CHECK(ld >= n_cols && (n_cols + ASM_COLS - 1) / ASM_COLS < 65536, "bad tile shape");
+  if (n_rows == 0 || n_cols == 0) return MPDOK_OK;
+  const int pslot = prof_start(MPDOK_PROF_ASSEMBLE, s);
+  const bool g = kernel == MPDOK_KERNEL_GAUSSIAN;
+  if (dim == 1) (g ? launch_f32_exact<1, MPDOK_KERNEL_GAUSSIAN> : launch_f32_exact<1, MPDOK_KERNEL_MQ>)(
+      rows, n_rows, cols, n_cols, gamma, reg, diag_offset, out, ld, s);
+  else if (dim == 2) (g ? launch_f32_exact<2, MPDOK_KERNEL_GAUSSIAN> : launch_f32_exact<2, MPDOK_KERNEL_MQ>)(
+      rows, n_rows, cols, n_cols, gamma, reg, diag_offset, out, ld, s);
+  else (g ? launch_f32_exact<3, MPDOK_KERNEL_GAUSSIAN> : launch_f32_exact<3, MPDOK_KERNEL_MQ>)(
+      rows, n_rows, cols, n_cols, gamma, reg, diag_offset, out, ld, s);
+  prof_stop(pslot, s, (double)n_rows * (double)n_cols * 4.0);
+  MPDOK_LAUNCH_CHECK("rbf_tile_f32_from_f64");
   return MPDOK_OK;
 }
 
