@@ -300,11 +300,12 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     per_s = total_ms / 1e3 / args.steps
-    prof = {}
+    prof, skipped = {}, {}
     for name, cls in (("gemv_f32", NV.PROF_GEMV_F32), ("gemv_f64", NV.PROF_GEMV_F64), ("lu_gemm", NV.PROF_LU_GEMM),
                       ("trsv", NV.PROF_TRSV), ("lu_panel", NV.PROF_LU_PANEL)):
         ms, cnt, work = NV.profile_query(cls)
         prof[name] = (ms, cnt, work)
+        skipped[name] = NV.profile_skipped(cls)
     NV.profile_enable(False)
 
     hbm, bf16, bf16s, peak_kind = _peaks()
@@ -321,6 +322,7 @@ def main():
                 tr = traffic["lu_gemm_bytes_per_flop"] * work / cnt
             rooflines[name] = {"bound": "tensor", "achieved": ach, "peak": bf16s, "unit": "TFLOP/s",
                                "frac": ach / bf16s, "traffic": tr, "launches": cnt, "avg_launch_ms": ms / cnt,
+                               "work_per_launch": work / cnt,
                                "peak_source": f"{peak_kind} bf16 dense, sustained (kernel timed inside a long step)"}
         elif name in ("gemv_f32", "gemv_f64", "trsv"):
             ach = work / (ms / 1e3) / 1e9
@@ -330,6 +332,7 @@ def main():
                 tr = traffic[key] * work / cnt
             rooflines[name] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                                "traffic": tr, "launches": cnt, "avg_launch_ms": ms / cnt,
+                               "work_per_launch": work / cnt, "skipped_launches": skipped[name],
                                "peak_source": f"{peak_kind} HBM copy"}
     dom = max((k for k in rooflines), key=lambda k: prof[k][0]) if rooflines else None
     roof = dict(rooflines[dom], kernel=dom) if dom else None

@@ -302,6 +302,9 @@ enum {
 MPDOK_API long long mpdok_launch_count(void);
 MPDOK_API int mpdok_profile_enable(int on);
 MPDOK_API int mpdok_profile_query(int kernel_class, double* total_ms, long long* launches, double* work);
+/* Launches of the class that a device skip flag turned off (a finished
+ * Arnoldi cycle): excluded from mpdok_profile_query's totals. */
+MPDOK_API long long mpdok_profile_skipped(int kernel_class);
 
 /* ------------------------------------------- reference ctypes ABI (mpdok.so)
  * mpdok_ops.py:362-373: A (N x N FP64, Fortran order), b, x (FP64, x is the

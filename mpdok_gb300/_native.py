@@ -146,6 +146,7 @@ _SIGS = {
     "mpdok_ooc_gmres_ir": (c_int, [c_void_p, c_void_p, c_int, c_int, c_double, c_double, c_void_p, c_void_p,
                                    c_double, c_int, c_int, c_double, c_void_p, c_size_t, ctypes.POINTER(SolveInfo),
                                    c_void_p]),
+    "mpdok_profile_skipped": (c_ll, [c_int]),
     "mpdok_launch_count": (c_ll, []),
     "mpdok_profile_enable": (c_int, [c_int]),
     "mpdok_profile_query": (c_int, [c_int, ctypes.POINTER(c_double), ctypes.POINTER(c_ll), ctypes.POINTER(c_double)]),
@@ -228,6 +229,11 @@ def profile_query(cls: int):
     w = c_double(0.0)
     check(load().mpdok_profile_query(cls, ctypes.byref(t), ctypes.byref(n), ctypes.byref(w)), "profile_query")
     return t.value, n.value, w.value
+
+
+def profile_skipped(cls: int) -> int:
+    """Launches of one class that a device skip flag turned off."""
+    return int(load().mpdok_profile_skipped(cls))
 
 
 def launch_count() -> int:

@@ -155,9 +155,10 @@ inline void launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaS
 
 // Opt-in per-kernel-class timing with CUDA events on the launching stream.
 // prof_start returns a slot (or -1 when profiling is off); prof_stop records
-// the closing event and the algorithmic bytes / flops of the launch.
+// the closing event and the algorithmic bytes / flops of the launch, and for a
+// launch predicated on a device skip flag, that flag's value.
 int prof_start(int cls, cudaStream_t s);
-void prof_stop(int slot, cudaStream_t s, double work);
+void prof_stop(int slot, cudaStream_t s, double work, const int* skip = nullptr);
 
 // Row-major FP32 RBF tile computed in FP64 and rounded once, nugget added in
 // FP32 after the rounding (the reference's out-of-core tile).

@@ -294,7 +294,7 @@ int gemv_launch(int a_dtype, bool trans, const void* A, long long lda, long long
         case MPDOK_BF16: launch_stage1_k<__nv_bfloat16>(K, trans, p, A, lda, m, n, Xk, ldx, P, vec_ok, skip, s); break;
         case MPDOK_F16: launch_stage1_k<__half>(K, trans, p, A, lda, m, n, Xk, ldx, P, vec_ok, skip, s); break;
       }
-      prof_stop(pslot, s, (double)m * (double)n * eb + (double)K * (double)(m + n) * acc_bytes);
+      prof_stop(pslot, s, (double)m * (double)n * eb + (double)K * (double)(m + n) * acc_bytes, skip);
       MPDOK_LAUNCH_CHECK("gemv stage1");
     }
     if (nrm2 && zero_ticket) MPDOK_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s));

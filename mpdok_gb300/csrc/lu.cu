@@ -641,7 +641,7 @@ static int lu_apply_t(const void* fbuf, long long n, int fdtype, const float* v,
   launch(k_trsv<F, false>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, n, L.nblk, (const float*)y, d, zz,
          flags + L.nblk, tk + 1, err, skip);
   launch(k_scale_out, grid_for(n), 256, 0, s, (const float*)zz, d, z, n, skip);
-  prof_stop(slot, s, (double)n * (double)n * sizeof(F));
+  prof_stop(slot, s, (double)n * (double)n * sizeof(F), skip);
   MPDOK_LAUNCH_CHECK("lu apply");
   return MPDOK_OK;
 }

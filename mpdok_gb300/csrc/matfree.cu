@@ -365,7 +365,7 @@ int matfree_apply(const MfOperand& op, int precision, const void* X, long long l
 #undef MF_CASE
   }
   MPDOK_LAUNCH_CHECK("matfree");
-  prof_stop(slot, s, (double)nr * (double)nc * K);
+  prof_stop(slot, s, (double)nr * (double)nc * K, skip);
   const unsigned fb = (unsigned)std::max(1LL, std::min<long long>((nr * K + 255) / 256, (long long)num_sms() * 4));
   if (f64)
     launch(k_mf_finalize<double>, fb, MF_THREADS, 0, s, (const double*)P, p.S, K, nr, alpha, beta,

@@ -21,12 +21,18 @@ struct ProfRec {
   int cls = 0;
   double work = 0.0;
   bool closed = false;
+  bool predicated = false;  // the launch read a device skip flag
 };
 
 static std::mutex g_pmu;
 static bool g_prof_on = false;
 static std::vector<ProfRec> g_recs;
 static std::vector<cudaEvent_t> g_pool;
+// Pinned copy of each predicated launch's skip flag, written on the stream
+// right after the launch: a predicated-off launch returns at once, so counting
+// its algorithmic work would overstate the achieved rate.
+constexpr size_t PROF_MAX = 1u << 20;
+static int* g_skiplog = nullptr;
 
 static cudaEvent_t get_event() {
   if (!g_pool.empty()) {
@@ -42,7 +48,7 @@ static cudaEvent_t get_event() {
 int prof_start(int cls, cudaStream_t s) {
   if (!g_prof_on) return -1;
   std::lock_guard<std::mutex> lk(g_pmu);
-  if (g_recs.size() >= (1u << 20)) return -1;
+  if (g_recs.size() >= PROF_MAX) return -1;
   ProfRec r;
   r.cls = cls;
   r.a = get_event();
@@ -53,13 +59,22 @@ int prof_start(int cls, cudaStream_t s) {
   return (int)g_recs.size() - 1;
 }
 
-void prof_stop(int slot, cudaStream_t s, double work) {
+void prof_stop(int slot, cudaStream_t s, double work, const int* skip) {
   if (slot < 0) return;
   std::lock_guard<std::mutex> lk(g_pmu);
   if ((size_t)slot >= g_recs.size()) return;
   cudaEventRecord(g_recs[slot].b, s);
   g_recs[slot].work = work;
   g_recs[slot].closed = true;
+  if (skip != nullptr) {
+    if (!g_skiplog && cudaHostAlloc((void**)&g_skiplog, PROF_MAX * sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+      g_skiplog = nullptr;
+      return;
+    }
+    g_skiplog[slot] = 0;
+    if (cudaMemcpyAsync(&g_skiplog[slot], skip, sizeof(int), cudaMemcpyDeviceToHost, s) == cudaSuccess)
+      g_recs[slot].predicated = true;
+  }
 }
 
 }  // namespace mpdok
@@ -79,15 +94,19 @@ extern "C" int mpdok_profile_enable(int on) {
   return MPDOK_OK;
 }
 
+// Totals over the launches of one class that did their work; launches that a
+// device skip flag turned off are counted by mpdok_profile_skipped.
 extern "C" int mpdok_profile_query(int cls, double* total_ms, long long* launches, double* work) {
   std::lock_guard<std::mutex> lk(g_pmu);
   double t = 0.0, w = 0.0;
   long long n = 0;
-  for (auto& r : g_recs) {
+  for (size_t i = 0; i < g_recs.size(); ++i) {
+    const ProfRec& r = g_recs[i];
     if (r.cls != cls || !r.closed) continue;
     float ms = 0.f;
-    cudaError_t e = cudaEventElapsedTime(&ms, r.a, r.b);
+    cudaError_t e = cudaEventElapsedTime(&ms, r.a, r.b);  // also orders the skip-flag copy before the read
     if (e != cudaSuccess) return cuda_status(e, "mpdok_profile_query");
+    if (r.predicated && g_skiplog[i] != 0) continue;
     t += ms;
     w += r.work;
     ++n;
@@ -96,4 +115,16 @@ extern "C" int mpdok_profile_query(int cls, double* total_ms, long long* launche
   if (launches) *launches = n;
   if (work) *work = w;
   return MPDOK_OK;
+}
+
+extern "C" long long mpdok_profile_skipped(int cls) {
+  std::lock_guard<std::mutex> lk(g_pmu);
+  long long n = 0;
+  for (size_t i = 0; i < g_recs.size(); ++i) {
+    const ProfRec& r = g_recs[i];
+    if (r.cls != cls || !r.closed || !r.predicated) continue;
+    if (cudaEventSynchronize(r.b) != cudaSuccess) return -1;
+    if (g_skiplog[i] != 0) ++n;
+  }
+  return n;
 }

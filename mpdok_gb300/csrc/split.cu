@@ -205,7 +205,7 @@ int split_gemv(const float* hi, const float* lo, long long lda, long long m, lon
       case 2: launch_split<2, TX>(p, hi, lo, lda, m, n, Xk, ldx, P, skip, s); break;
       default: launch_split<1, TX>(p, hi, lo, lda, m, n, Xk, ldx, P, skip, s); break;
     }
-    prof_stop(slot, s, 8.0 * (double)m * (double)n + (double)K * (double)(m + n) * sizeof(TX));
+    prof_stop(slot, s, 8.0 * (double)m * (double)n + (double)K * (double)(m + n) * sizeof(TX), skip);
     const unsigned fb = (unsigned)std::max(1LL, std::min<long long>((m * K + 255) / 256, (long long)num_sms() * 4));
     launch(k_split_finalize<TY>, fb, SP_THREADS, 0, s, (const double*)P, p.S, K, m, alpha, beta,
            bsrc ? bsrc + (long long)done * ldb : (const TY*)nullptr, ldb, Y + (long long)done * ldy, ldy, skip);
