@@ -283,6 +283,43 @@ MPDOK_API int mpdok_ooc_gmres_ir(void* handle, const double* coords, int dim, in
                                  double inner_tol, void* work, size_t work_bytes, mpdok_solve_info* info,
                                  cudaStream_t stream);
 
+/* ------------------------------------------------------------------ batched
+ * Many SPD RBF systems of uneven size, each with nrhs <= 8 right-hand sides:
+ * A_s = phi(eps_s * ||c_i - c_j||) + reg_s I (gamma = eps^2).  A plan holds
+ * the FP64 matrices (lower triangle overwritten by the Cholesky factor, upper
+ * triangle kept for the FP64 residual), the diagonal-block inverses and the
+ * level schedule (systems sorted by N; one launch per level covers every
+ * active system).  arith 1 runs the O(N^3) trailing update in double-float
+ * on the FP32 pipe, arith 0 in FP64; everything else is FP64.  grid_mult
+ * scales the persistent trailing-update grid (resident CTAs x SMs x mult).
+ * Packing (caller order): coords = concatenated (n_s x dim) row-major;
+ * B / X = concatenated (n_s x nrhs) column-major blocks.  All device
+ * pointers.  Not in the reference; the batched workload of the Python layer. */
+MPDOK_API int mpdok_batch_create(int nsys, const long long* n, int dim, int nrhs, int kernel, int arith,
+                                 int grid_mult, void** plan);
+MPDOK_API int mpdok_batch_destroy(void* plan);
+MPDOK_API size_t mpdok_batch_bytes(void* plan);
+/* coords on the device; eps, reg on the host (nsys each). */
+MPDOK_API int mpdok_batch_load(void* plan, const double* coords, const double* eps, const double* reg,
+                               cudaStream_t stream);
+/* Assemble and factor every system (no host synchronisation). */
+MPDOK_API int mpdok_batch_factor(void* plan, cudaStream_t stream);
+/* X = A^{-1} B with `refine` FP64 refinement steps (no host synchronisation). */
+MPDOK_API int mpdok_batch_solve(void* plan, const double* B, double* X, int refine, cudaStream_t stream);
+/* relres[s] = max over RHS of ||B - A X|| / ||B|| (device array, caller order). */
+MPDOK_API int mpdok_batch_relres(void* plan, const double* B, const double* X, double* relres, cudaStream_t stream);
+/* Gradients of a loss L(X) from Lam = A^{-1} dL/dX: grad_coords packed like
+ * coords, grad_eps and grad_reg (nsys, device).  phi recomputed in FP64. */
+MPDOK_API int mpdok_batch_adjoint(void* plan, const double* X, const double* Lam, double* grad_coords,
+                                  double* grad_eps, double* grad_reg, cudaStream_t stream);
+/* Pivots perturbed by the last factorization (synchronises the stream). */
+MPDOK_API int mpdok_batch_perturbed(void* plan, cudaStream_t stream);
+/* Capture factor + solve (+ refine) on fixed B / X into one CUDA graph, then
+ * replay it with one launch. */
+MPDOK_API int mpdok_batch_graph_build(void* plan, const double* B, double* X, int refine);
+MPDOK_API int mpdok_batch_graph_launch(void* plan, cudaStream_t stream);
+MPDOK_API long long mpdok_batch_graph_nodes(void* plan);
+
 /* --------------------------------------------------------- instrumentation
  * mpdok_launch_count: kernels launched by this library since load.
  * mpdok_profile_enable(1) clears and starts per-launch CUDA-event timing of

@@ -147,6 +147,18 @@ _SIGS = {
                                    c_double, c_int, c_int, c_double, c_void_p, c_size_t, ctypes.POINTER(SolveInfo),
                                    c_void_p]),
     "mpdok_profile_skipped": (c_ll, [c_int]),
+    "mpdok_batch_create": (c_int, [c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, ctypes.POINTER(c_void_p)]),
+    "mpdok_batch_destroy": (c_int, [c_void_p]),
+    "mpdok_batch_bytes": (c_size_t, [c_void_p]),
+    "mpdok_batch_load": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "mpdok_batch_factor": (c_int, [c_void_p, c_void_p]),
+    "mpdok_batch_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "mpdok_batch_relres": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "mpdok_batch_adjoint": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "mpdok_batch_perturbed": (c_int, [c_void_p, c_void_p]),
+    "mpdok_batch_graph_build": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
+    "mpdok_batch_graph_launch": (c_int, [c_void_p, c_void_p]),
+    "mpdok_batch_graph_nodes": (c_ll, [c_void_p]),
     "mpdok_launch_count": (c_ll, []),
     "mpdok_profile_enable": (c_int, [c_int]),
     "mpdok_profile_query": (c_int, [c_int, ctypes.POINTER(c_double), ctypes.POINTER(c_ll), ctypes.POINTER(c_double)]),

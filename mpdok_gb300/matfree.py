@@ -125,5 +125,57 @@ class MatrixFreeOperator:
         squeeze = torch.as_tensor(B).dim() == 1 if not isinstance(B, torch.Tensor) else B.dim() == 1
         return (X.reshape(-1) if squeeze else X), info.history_list(), bool(info.converged)
 
+    def evaluate(self, query, alpha, precision: str = "f64") -> torch.Tensor:
+        """f(q) = sum_i alpha_i phi(||q - c_i||) at query points (no nugget)."""
+        return rbf_evaluate(alpha, self.coords, query, self.gamma, kernel=self.kernel, precision=precision)
+
     def __repr__(self):
         return f"MatrixFreeOperator(N={self.N:,}, dim={self.dim}, kernel={self.kernel}, gamma={self.gamma:g})"
+
+
+def rbf_evaluate(alpha, centres, query, gamma: float, kernel: str = "gaussian", precision: str = "f64",
+                 chunk: int | None = None) -> torch.Tensor:
+    """Interpolant at query points: f(q) = sum_i alpha_i phi(||q - c_i||).
+
+    The evaluation step that consumes every solve (enkf_solver.py:162-200,
+    ``reconstruct``): the reference assembles (chunk x N) FP64 blocks of K and
+    multiplies; here the same evaluate-and-multiply kernel as the solvers
+    recomputes phi from TMA-staged centre tiles, so nothing of size M x N is
+    ever stored.  ``alpha`` is (N,) or (N, k); the result is (M,) or (M, k),
+    FP64 (``precision='f64'``, the reference's output type) or FP32.
+    ``chunk`` is accepted for signature compatibility; no chunking is needed.
+    """
+    del chunk
+    if precision not in ("f64", "f32"):
+        raise ValueError("precision must be 'f64' or 'f32'")
+    c = _coords_device(centres)
+    q = _coords_device(query)
+    if q.shape[1] != c.shape[1]:
+        raise ValueError(f"query dimension {q.shape[1]} != centre dimension {c.shape[1]}")
+    n, m, dim = int(c.shape[0]), int(q.shape[0]), int(c.shape[1])
+    pcode = N.F64 if precision == "f64" else N.F32
+    tdt = torch.float64 if precision == "f64" else torch.float32
+    if not isinstance(alpha, torch.Tensor):
+        alpha = torch.as_tensor(np.asarray(alpha), device=require_cuda())
+    squeeze = alpha.dim() == 1
+    A = as_columns(alpha, tdt)
+    if A.shape[0] != n:
+        raise ValueError(f"alpha has {A.shape[0]} rows, expected {n}")
+    k = A.shape[1]
+    out = fortran_empty(m, k, torch.float64)
+    if m == 0 or k == 0:
+        return out.reshape(-1) if squeeze else out
+    lib = N.load()
+    ld = n if pcode == N.F64 else (n + 3) // 4 * 4
+    ws = Workspace()
+    for j0 in range(0, k, 8):
+        kk = min(8, k - j0)
+        Xc = fortran_empty(ld, kk, tdt)
+        Xc[:n] = A[:, j0:j0 + kk]
+        Y = fortran_empty(m, kk, tdt)
+        w = ws.get(lib.mpdok_matfree_workspace_size(m, n, kk, pcode))
+        N.check(lib.mpdok_matfree_apply(ptr(q), m, ptr(c), n, dim, KERNELS[kernel], float(gamma), 0.0, 0, pcode,
+                                        ptr(Xc), ld, kk, ptr(Y), m, ptr(w), w.numel(), stream_handle()),
+                "matfree_apply (evaluate)")
+        out[:, j0:j0 + kk] = Y
+    return out.reshape(-1) if squeeze else out

@@ -89,3 +89,34 @@ def test_matfree_gmres_ir_and_cg_solve():
     x2, h2, c2 = cg(mf, b, tol=1e-5, check_every=5)
     x3, h3, c3 = O.cg(A, b, tol=1e-5, check_every=5)
     assert c2 and c3 and abs(len(h2) - len(h3)) <= 1
+
+
+@pytest.mark.parametrize("m,n,k", [(1, 1, 1), (3001, 1234, 1), (257, 4096, 3), (64, 513, 11)])
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_rbf_evaluate_at_query_points(m, n, k, precision):
+    """f(q) = sum_i alpha_i phi(||q - c_i||) (enkf_solver.py:162-200) against the dense oracle."""
+    from mpdok_gb300.matfree import rbf_evaluate
+    rng = np.random.default_rng(m + n + k)
+    C = rng.uniform(0, 1, (n, 2))
+    Q = rng.uniform(-0.1, 1.1, (m, 2))
+    alpha = rng.standard_normal((n, k)) if k > 1 else rng.standard_normal(n)
+    K = O.rbf_matrix(Q, C, gamma=30.0, reg=0.0)
+    ref = K @ alpha
+    got = rbf_evaluate(alpha, C, Q, 30.0, precision=precision).cpu().numpy()
+    assert got.shape == ref.shape and got.dtype == np.float64
+    bound = np.abs(K) @ np.abs(alpha)
+    tol = 1e-13 if precision == "f64" else 2e-5
+    assert np.all(np.abs(got - ref) <= tol * bound + (0 if precision == "f64" else 1e-6))
+
+
+def test_rbf_evaluate_reconstructs_solved_field():
+    """Solve on the centres, evaluate back at the centres: reproduces b up to the nugget term."""
+    from mpdok_gb300.matfree import MatrixFreeOperator
+    rng = np.random.default_rng(5)
+    C = rng.uniform(0, 1, (800, 2))
+    b = np.sin(2 * np.pi * C[:, 0]) * np.cos(2 * np.pi * C[:, 1])
+    A = O.rbf_matrix(C, gamma=400.0, reg=1e-3)
+    alpha = O.fp64_solve(A, b)
+    op = MatrixFreeOperator(C, gamma=400.0, reg=1e-3)
+    f = op.evaluate(C, alpha).cpu().numpy()
+    np.testing.assert_allclose(f + 1e-3 * alpha, b, atol=1e-10)
