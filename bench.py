@@ -191,6 +191,235 @@ def gemv_standalone(n: int, warmup: int, reps: int) -> dict:
     return out
 
 
+DF_FMA_OPS = 13  # FP32 instructions per double-float multiply-add in the trailing update
+
+
+def bench_batch(args) -> int:
+    """C4: 256 Gaussian RBF systems, N ~ U{500..8000}, eps ~ U(2, 8), nugget 1e-8,
+    8 RHS each.  One step = factor + solve + 2 FP64 refinement steps (one CUDA
+    graph launch) + the adjoint of L = ||X - X*||^2 (one more solve on the
+    stored factors + the fused gradient contraction), inputs resident in HBM."""
+    import numpy as np
+    import torch
+    from mpdok_gb300 import configs
+    from mpdok_gb300.batch import BatchedRBFSolver, pack_coords, pack_rhs
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    rank = int(os.environ.get("RANK", "0"))
+    systems = configs.c4(n_systems=args.systems)
+    sizes = [q.n for q in systems]
+    eps = np.array([np.sqrt(q.gamma) for q in systems])
+    C = pack_coords([q.coords for q in systems])
+    B = pack_rhs([q.b for q in systems], 8)
+    rng = np.random.default_rng(30)
+    T = torch.from_numpy(rng.standard_normal(B.numel())).cuda()
+    solver = BatchedRBFSolver(sizes, dim=2, nrhs=8, arith="df32")
+    solver.load(C, eps, 1e-8)
+    tune = solver.autotune()
+    Bbuf, Xbuf = solver.build_graph(B, refine=2)
+    flops = sum(n ** 3 / 3.0 for n in sizes)
+
+    def step():
+        solver.run_graph()
+        G = 2.0 * (Xbuf - T)
+        lam = solver.solve(G, refine=1)
+        return solver.adjoint(Xbuf, lam)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        grads = step()
+    e1.record()
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    per = e0.elapsed_time(e1) / 1e3 / args.steps
+    # factor alone, for the roofline of the trailing update
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    solver.factor()
+    f1.record()
+    torch.cuda.synchronize()
+    t_factor = f0.elapsed_time(f1) / 1e3
+    relres = solver.relres(B, Xbuf).cpu().numpy()
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    fp32_peak = 128 * 2 * sms * 2.07e9 / 1e12        # nominal FP32 FMA rate at the maximum SM clock
+    df_peak = fp32_peak / DF_FMA_OPS                  # FP64-equivalent flops of double-float multiply-adds
+    ach = flops / t_factor / 1e12                     # Cholesky: sum n^3 / 3 flops
+    # plain FP64 GPU solve: the vendor Cholesky per system (torch.linalg) + triangular solves
+    base = None
+    if not args.no_fp64_baseline:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        worst = 0.0
+        for q in systems:
+            c = torch.from_numpy(q.coords).cuda()
+            b = torch.from_numpy(np.asarray(q.b)).cuda()
+            d2 = ((c[:, None, :] - c[None, :, :]) ** 2).sum(-1)
+            A = torch.exp(-q.gamma * d2)
+            A.diagonal().add_(q.reg)
+            L = torch.linalg.cholesky(A)
+            x = torch.cholesky_solve(b, L)
+            worst = max(worst, float((torch.linalg.norm(b - A @ x, dim=0) / torch.linalg.norm(b, dim=0)).max()))
+            del A, L
+        torch.cuda.synchronize()
+        base = {"seconds_factor_solve": time.perf_counter() - t0, "relres_max": worst,
+                "method": "torch.linalg.cholesky + cholesky_solve (FP64, vendor library) per system, assembly inside"}
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        pick = list(range(0, len(systems), max(1, len(systems) // 12)))
+        try:
+            threads = len(os.sched_getaffinity(0))
+        except AttributeError:
+            threads = os.cpu_count() or 1
+        env = dict(os.environ, OPENBLAS_NUM_THREADS=str(threads), OMP_NUM_THREADS=str(threads))
+        out = subprocess.run([sys.executable, "-m", "oracle.cpu_baseline", "--config", "C4", "--systems",
+                              ",".join(map(str, pick))], cwd=str(ROOT), env=env, capture_output=True, text=True,
+                             timeout=1800)
+        if out.returncode == 0:
+            d = json.loads(out.stdout.strip().splitlines()[-1])
+            scale = flops / d["flops"]
+            cpu = {"value": d["seconds"] * scale, "unit": "s", "cores": threads, "kind": "port",
+                   "sample": f"scipy cho_factor/cho_solve FP64 (8 RHS) on {len(pick)} of the {len(systems)} systems: "
+                             f"{d['seconds']:.2f} s, x{scale:.1f} by sum n^3 (factor + solve only, no adjoint); "
+                             f"relres max {d['relres_max']:.2e}"}
+    h2d = C.numel() * 8 + B.numel() * 8
+    line = {
+        "metric": "C4 batched solve + adjoint time per step (256 Gaussian RBF systems, 8 RHS)", "value": per,
+        "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": per * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (double-float update)",
+        "data": "synthetic (seeded NumPy, C4)",
+        "config": {"workload": f"C4: {len(sizes)} systems, N in [{min(sizes)}, {max(sizes)}], sum N = {sum(sizes)}, "
+                               "2-D uniform centres, eps~U(2,8), nugget 1e-8, 8 RHS; step = graph(factor + solve + "
+                               "2 FP64 IR) + adjoint (solve + contraction)",
+                   "l2": "inputs larger than L2 (A: %.1f GB FP64)" % (sum(n * n for n in sizes) * 8 / 1e9),
+                   "grid_mult": solver.grid_mult, "autotune": tune},
+        "relres_max": float(relres.max()), "relres_median": float(np.median(relres)),
+        "factor_seconds": t_factor,
+        "roofline": {"bound": "fp32 pipe (double-float trailing update)", "achieved": ach,
+                     "peak": df_peak, "unit": "TFLOP/s (FP64-equivalent)", "frac": ach / df_peak, "traffic": None,
+                     "kernel": "batched Cholesky factor (k_bsyrk dominant)",
+                     "peak_source": f"nominal FP32 FMA rate {fp32_peak:.1f} TFLOP/s / {DF_FMA_OPS} instructions "
+                                    "per double-float multiply-add"},
+        "fp64_gpu_baseline": base, "cpu_baseline": cpu,
+        "e2e": None, "gpu_launches": solver.graph_nodes * args.steps, "clocks": ck,
+        "gradient_norms": {"coords": float(grads[0].norm()), "eps": float(grads[1].norm()),
+                           "reg": float(grads[2].norm())},
+    }
+    # end to end: host inputs -> device, graph, adjoint, gradients back to the host
+    Ch = C.cpu().pin_memory()
+    Bh = B.cpu().pin_memory()
+    times = []
+    for i in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Cd = Ch.cuda(non_blocking=True)
+        Bbuf.copy_(Bh, non_blocking=True)
+        solver.load(Cd, eps, 1e-8)
+        gr = step()
+        out = [g.cpu() for g in gr] + [Xbuf.cpu()]
+        torch.cuda.synchronize()
+        if i > 0:
+            times.append(time.perf_counter() - t0)
+    line["e2e"] = {"value": sum(times) / len(times), "unit": "s", "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": sum(o.numel() * 8 for o in out),
+                   "api": "BatchedRBFSolver.load + run_graph + solve + adjoint from pinned host coords/B"}
+    print(json.dumps(line))
+    return 0
+
+
+def bench_ooc(args) -> int:
+    """C5 layout: FP32 A in pinned host RAM in 16384-row tiles (or a raw file),
+    streamed per product; reported against the pinned host->device copy rate
+    measured in the same run, next to the matrix-free in-HBM product."""
+    import numpy as np
+    import torch
+    from mpdok_gb300.matfree import MatrixFreeOperator
+    from mpdok_gb300.mpdok_ooc import MPDOKOOCSolver
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    n = args.n
+    rng = np.random.default_rng(4)
+    X = rng.uniform(0.0, 1.0, size=(n, 3))
+    # host link: one pinned 1 GiB buffer -> device
+    hb = torch.empty(1 << 28, dtype=torch.float32).pin_memory()
+    db = torch.empty_like(hb, device="cuda")
+    for _ in range(3):
+        db.copy_(hb, non_blocking=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        db.copy_(hb, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    link = hb.numel() * 4 * 5 / (e0.elapsed_time(e1) / 1e3) / 1e9
+    del hb, db
+    s = MPDOKOOCSolver(tile_rows=min(16384, n))
+    s.build(X, gamma=100.0, reg=1e-6, store="ram", verbose=False)
+    v = torch.randn(n, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        s._tiled_sgemv(v)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    e0.record()
+    for _ in range(args.steps):
+        y = s._tiled_sgemv(v)
+    e1.record()
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    gbs = 4.0 * n * n / (ms / 1e3) / 1e9
+    s.free()
+    op = MatrixFreeOperator(X, gamma=100.0, reg=1e-6)
+    for _ in range(3):
+        op.matvec(v)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        op.matvec(v)
+    e1.record()
+    torch.cuda.synchronize()
+    mf_ms = e0.elapsed_time(e1) / args.steps
+    ssd = None
+    path = ROOT / "gpurun_out" / "ooc_store.bin" if (ROOT / "gpurun_out").exists() else Path("/tmp/ooc_store.bin")
+    try:
+        n2 = min(n, 16384)
+        s2 = MPDOKOOCSolver(tile_rows=2048)
+        s2.build(X[:n2], gamma=100.0, reg=1e-6, store="ssd", path=str(path), verbose=False)
+        v2 = torch.randn(n2, device="cuda")
+        s2._tiled_sgemv(v2)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(3):
+            s2._tiled_sgemv(v2)
+        e1.record()
+        torch.cuda.synchronize()
+        ssd = {"n": n2, "ms": e0.elapsed_time(e1) / 3, "GBs": 4.0 * n2 * n2 / (e0.elapsed_time(e1) / 3e3) / 1e9,
+               "note": "raw row-major FP32 file read by 8 pread threads into pinned staging (page cache warm)"}
+        s2.free()
+    finally:
+        if path.exists():
+            path.unlink()
+    line = {"metric": "OOC streamed FP32 matvec rate (C5 layout, pinned host RAM store)", "value": gbs, "unit": "GB/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded NumPy, C5 centres)",
+            "config": {"workload": f"C5 layout at N={n}: Gaussian eps=10 (gamma=100), 3-D uniform seed 4, nugget 1e-6, "
+                                   f"FP32 store {4.0 * n * n / 1e9:.1f} GB, 16384-row tiles; step = one streamed "
+                                   "product y = A v", "l2": "store far larger than L2"},
+            "roofline": {"bound": "host link (pinned H2D)", "achieved": gbs, "peak": link, "unit": "GB/s",
+                         "frac": gbs / link, "traffic": 4.0 * n * n,
+                         "peak_source": "pinned 1 GiB host->device copy measured in this run"},
+            "matrix_free_in_hbm_ms": mf_ms, "streamed_over_matrix_free": ms / mf_ms, "ssd_store": ssd,
+            "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": ck}
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path (SciPy FP64 LU) on rank 0."""
     rank = int(os.environ.get("RANK", "0"))
@@ -228,8 +457,10 @@ def main():
     ap.add_argument("--no-fp64-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--only", default="headline", choices=["headline", "gemv"],
-                    help="gemv: only the standalone stored-matrix GEMV measurement (used for kernel profiles)")
+    ap.add_argument("--only", default="headline", choices=["headline", "gemv", "batch", "ooc"],
+                    help="gemv: only the standalone stored-matrix GEMV measurement (used for kernel profiles); "
+                         "batch: the batched C4 solve + adjoint line; ooc: the out-of-core C5 streaming line")
+    ap.add_argument("--systems", type=int, default=256, help="--only batch: number of C4 systems")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -238,6 +469,10 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         print(json.dumps(gemv_standalone(args.n, max(3, args.warmup), max(5, args.steps))))
         return 0
+    if args.only == "batch":
+        return bench_batch(args)
+    if args.only == "ooc":
+        return bench_ooc(args)
 
     import numpy as np
     import torch

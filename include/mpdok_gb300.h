@@ -58,7 +58,8 @@ typedef struct mpdok_solve_info {
   int converged;          /* 1 when the FP64 relative residual fell below tol */
   int outer_iters;        /* outer refinement steps (or restarts / CG checks) */
   int inner_iters;        /* total inner matvecs */
-  int stagnated;          /* 1 when the 1 % stagnation rule stopped the solve */
+  int stagnated;          /* 1: the 1 % stagnation rule stopped the solve; 2: the residual diverged and the
+                             best iterate was restored (mpdok_lu_gmres_ir) */
   double relres;          /* final FP64 ||b - A x|| / ||b|| */
   double bnorm;           /* ||b|| */
   int n_history;          /* entries used in history[] */

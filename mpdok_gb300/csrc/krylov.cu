@@ -810,7 +810,7 @@ int gmres_core(const KWs& ws, const Operator32& A, const Residual64& R, const do
 
 int gmres_ir_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* b, double* x, double tol,
                   int maxiter_outer, int restart, double inner_tol, const Precond* pc, mpdok_solve_info* info,
-                  cudaStream_t s) {
+                  cudaStream_t s, double* xbest) {
   const long long n = ws.n;
   double bnorm = 0.0;
   MPDOK_TRY(host_bnorm(ws, b, &bnorm, s));
@@ -821,28 +821,59 @@ int gmres_ir_core(const KWs& ws, const Operator32& A, const Residual64& R, const
     if (info) info->converged = 1;
     return MPDOK_OK;
   }
-  bool converged = false;
+  bool converged = false, diverged = false;
+  double best = INFINITY;
   KScal hs;
   int inner_total = 0;
+  // guarded mode (xbest != nullptr): keep the best iterate; a non-finite
+  // residual or one 1e3 x above the best ends the solve with the best restored
+  auto guard = [&](double rel, int it) -> int {
+    if (!std::isfinite(rel) || rel > 1e3 * best) {
+      MPDOK_CUDA_TRY(cudaMemcpyAsync(x, xbest, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      hist_push(info, it, best);
+      diverged = true;
+    } else if (rel < best) {
+      best = rel;
+      MPDOK_CUDA_TRY(cudaMemcpyAsync(xbest, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    }
+    return MPDOK_OK;
+  };
   for (int outer = 0; outer < maxiter_outer; ++outer) {
     MPDOK_TRY(fp64_residual(ws, R, b, x, &hs, s));
     if (outer > 0) inner_total += hs.m_used;
     const double rel = std::sqrt(hs.nrm2) / bnorm;
     hist_push(info, outer, rel);
-    if (!std::isfinite(rel)) { set_error("GMRES-IR: non-finite residual"); return MPDOK_ERR_NONFINITE; }
+    if (xbest) {
+      MPDOK_TRY(guard(rel, outer));
+      if (diverged) break;
+    } else if (!std::isfinite(rel)) {
+      set_error("GMRES-IR: non-finite residual");
+      return MPDOK_ERR_NONFINITE;
+    }
     if (rel < tol) { converged = true; break; }
     MPDOK_TRY(cycle_start_from_f64(ws, ws.r64, s));
     MPDOK_TRY(arnoldi_cycle(ws, A, restart, 2, inner_tol, pc, nullptr, x, s));
     if (info) info->outer_iters = outer + 1;
   }
-  if (!converged) {
+  if (!converged && !diverged) {
     MPDOK_TRY(fp64_residual(ws, R, b, x, &hs, s));
     if (maxiter_outer > 0) inner_total += hs.m_used;
     const double rel = std::sqrt(hs.nrm2) / bnorm;
     hist_push(info, maxiter_outer, rel);
-    converged = rel < tol;
+    if (xbest) {
+      MPDOK_TRY(guard(rel, maxiter_outer));
+      if (!diverged && rel > best) {  // an earlier iterate was better
+        MPDOK_CUDA_TRY(cudaMemcpyAsync(x, xbest, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        hist_push(info, maxiter_outer, best);
+      }
+    }
+    converged = info ? info->relres < tol : rel < tol;
   }
-  if (info) { info->converged = converged ? 1 : 0; info->inner_iters = inner_total; }
+  if (info) {
+    info->converged = converged ? 1 : 0;
+    info->inner_iters = inner_total;
+    if (diverged) info->stagnated = 2;
+  }
   return MPDOK_OK;
 }
 

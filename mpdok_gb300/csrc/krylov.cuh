@@ -107,10 +107,13 @@ int fp64_residual(const KWs& ws, const Residual64& R, const double* b, const dou
 // Restarted FP32 GMRES(m) (single Gram-Schmidt pass, FP64 check per restart).
 int gmres_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* rhs64, double* x64, double tol,
                int maxiter, int restart, mpdok_solve_info* info, cudaStream_t s);
-// GMRES-IR outer loop (mpdok_ooc.py:315-373) over any operator pair.
+// GMRES-IR outer loop (mpdok_ooc.py:315-373) over any operator pair.  With
+// xbest (n doubles of scratch) the loop is guarded: the best iterate is kept,
+// and a non-finite residual or one 1e3 x above the best restores it and stops
+// (info->stagnated = 2); without it a non-finite residual is an error.
 int gmres_ir_core(const KWs& ws, const Operator32& A, const Residual64& R, const double* b, double* x, double tol,
                   int maxiter_outer, int restart, double inner_tol, const Precond* pc, mpdok_solve_info* info,
-                  cudaStream_t s);
+                  cudaStream_t s, double* xbest = nullptr);
 int ws_prepare(const KWs& ws, size_t work_bytes, cudaStream_t s);
 // CG-IR: FP64 residual R = B - A X through R, inner FP32 CG on A E = R for all
 // columns in lockstep (relative inner tolerance, inner_maxiter), X += E in FP64.

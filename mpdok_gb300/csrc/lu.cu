@@ -931,7 +931,7 @@ extern "C" int mpdok_lu_ir_solve(const double* A, long long lda, long long n, co
 extern "C" size_t mpdok_lu_gmres_ir_work_size(long long n, int restart) {
   if (n < 0 || restart < 1) return 0;
   return align_up(apply_layout(n).total, 256) + align_up((size_t)std::max(1LL, n) * sizeof(float), 256) +
-         krylov_layout(n, restart, nullptr).total + 256;
+         align_up(krylov_layout(n, restart, nullptr).total, 256) + align_up((size_t)std::max(1LL, n) * 8, 256) + 256;
 }
 
 extern "C" int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* A32, long long lda32, long long n,
@@ -968,8 +968,11 @@ extern "C" int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* 
   c.n = n;
   c.gw = ws.gw;
   c.gbytes = ws.gbytes;
+  // the mixed solve is guarded: on a singular or badly scaled system it returns
+  // the best iterate with info->stagnated = 2 instead of diverging
+  double* xbest = (double*)(wb + a_bytes + align_up((size_t)n * sizeof(float), 256) + align_up(ws.total, 256));
   return gmres_ir_core(ws, stored_op32(&c), stored_res64(&c), b, x, tol, maxiter_outer, restart, inner_tol, &pc, info,
-                       s);
+                       s, xbest);
 }
 
 // --------------------------------------------------- LU-preconditioned CG-IR

@@ -25,7 +25,8 @@ DTYPES = {"bf16": N.BF16, "bfloat16": N.BF16, "fp16": N.F16, "float16": N.F16, "
 
 def _info(info: N.SolveInfo) -> dict:
     return {"converged": bool(info.converged), "outer_iters": int(info.outer_iters),
-            "inner_iters": int(info.inner_iters), "relres": float(info.relres), "history": info.history_list()}
+            "inner_iters": int(info.inner_iters), "relres": float(info.relres), "history": info.history_list(),
+            "diverged": int(info.stagnated) == 2}
 
 
 class LUFactorization:

@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes
 import time
+import warnings
 
 import torch
 
@@ -21,7 +22,7 @@ from ._device import Workspace, as_fortran, as_vector, fortran_empty, ptr, strea
 def _info_dict(info: N.SolveInfo) -> dict:
     return {"converged": bool(info.converged), "outer_iters": int(info.outer_iters),
             "inner_iters": int(info.inner_iters), "relres": float(info.relres),
-            "history": info.history_list()}
+            "history": info.history_list(), "diverged": int(info.stagnated) == 2}
 
 
 class MixedSolver:
@@ -83,6 +84,11 @@ class MixedSolver:
         d["refine_ms"] = ev[1].elapsed_time(ev[2])
         d["perturbed_pivots"] = lu.n_perturbed
         self.last_timing = {"factor_ms": d["factor_ms"], "refine_ms": d["refine_ms"]}
+        if not d["converged"]:
+            why = ("the FP64 residual diverged; the best iterate is returned" if d["diverged"]
+                   else f"not converged in {self.maxiter_outer} outer steps")
+            warnings.warn(f"MixedSolver ({self.factor_dtype} LU-GMRES-IR): {why} (relres {d['relres']:.2e}, "
+                          f"{lu.n_perturbed} perturbed pivots)", RuntimeWarning, stacklevel=2)
         return x, d
 
 

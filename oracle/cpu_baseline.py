@@ -8,6 +8,10 @@ residual meets the tolerance, on the same seeded RBF family as the GPU run.
 
     python -m oracle.cpu_baseline --n 8192 --repeats 1 --config HEADLINE
 prints one JSON line: {"seconds": [...], "n": ..., "threads": ..., "relres": ...}
+
+    python -m oracle.cpu_baseline --config C4 --systems 0,37,101
+times SciPy FP64 cho_factor + cho_solve (8 RHS) on the listed C4 systems and
+prints {"seconds": ..., "flops": sum n^3/3, "relres_max": ..., "threads": ...}.
 """
 from __future__ import annotations
 
@@ -24,6 +28,7 @@ def main(argv=None):
     ap.add_argument("--repeats", type=int, default=1)
     ap.add_argument("--config", default="HEADLINE")
     ap.add_argument("--tol", type=float, default=1e-12)
+    ap.add_argument("--systems", default="")
     args = ap.parse_args(argv)
 
     import numpy as np
@@ -32,6 +37,23 @@ def main(argv=None):
     sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
     from mpdok_gb300 import configs
     from oracle.krylov_ref import rbf_matrix
+
+    if args.config.upper() == "C4":
+        systems = configs.c4()
+        pick = [int(t) for t in args.systems.split(",") if t.strip()] or [0]
+        total, flops, worst = 0.0, 0.0, 0.0
+        for i in pick:
+            sysm = systems[i]
+            A = rbf_matrix(sysm.coords, gamma=sysm.gamma, reg=sysm.reg)
+            B = np.asarray(sysm.b, dtype=np.float64)
+            t0 = time.perf_counter()
+            x = sla.cho_solve(sla.cho_factor(A, lower=True, check_finite=False), B, check_finite=False)
+            total += time.perf_counter() - t0
+            flops += sysm.n ** 3 / 3.0
+            worst = max(worst, float(np.max(np.linalg.norm(B - A @ x, axis=0) / np.linalg.norm(B, axis=0))))
+        print(json.dumps({"seconds": total, "flops": flops, "systems": pick, "relres_max": worst,
+                          "threads": int(os.environ.get("OPENBLAS_NUM_THREADS", "0")), "config": "C4"}))
+        return
 
     gen = {"HEADLINE": configs.headline, "C3": configs.c3}[args.config.upper()]
     sysm = gen(n=args.n)

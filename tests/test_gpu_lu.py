@@ -128,3 +128,47 @@ def test_lu_not_factored_status():
                                ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(x.data_ptr()), 1e-12, 3,
                                ctypes.c_void_p(w.data_ptr()), w.numel(), ctypes.byref(info), None)
     assert st == N.ERR_NOT_FACTORED
+
+
+def test_mixed_solver_guard_on_singular_c3():
+    """C3 as specified (MQ, eps=2, no nugget) is singular to working precision:
+    the pivoted FP64 LU reaches relres ~1e2.  The guarded mixed solve returns
+    its best iterate (relres <= 1, finite) with a RuntimeWarning."""
+    import warnings
+    from mpdok_gb300 import configs
+    from mpdok_gb300.rbf_kernel import assemble
+    from mpdok_gb300.solvers import MixedSolver
+    c3 = configs.c3(n=4096)
+    A = assemble(c3.coords, gamma=c3.gamma, reg=c3.reg, kernel=c3.kernel, dtype=torch.float64)
+    b = torch.from_numpy(c3.b).cuda()
+    for fd in ("fp16", "bf16"):
+        with warnings.catch_warnings(record=True) as w:
+            warnings.simplefilter("always")
+            x, info = MixedSolver(factor_dtype=fd).solve(A, b, tol=1e-12)
+        assert not info["converged"]
+        assert any(issubclass(m.category, RuntimeWarning) for m in w)
+        assert torch.isfinite(x).all()
+        rel = float(torch.linalg.norm(b - A @ x) / torch.linalg.norm(b))
+        assert rel <= 1.0 + 1e-12 and abs(rel - info["relres"]) <= 1e-6 * max(rel, 1e-30)
+
+
+def test_mixed_solver_fp32_factors_on_moderate_mq():
+    """MQ with a sharp shape parameter (gamma = 1e4, N = 2048, kappa ~ 1.7e8,
+    one positive eigenvalue): the unpivoted FP32-factor LU-GMRES-IR reaches the
+    FP64 LU oracle's own residual floor."""
+    import warnings
+    from mpdok_gb300 import configs
+    from mpdok_gb300.rbf_kernel import assemble
+    from mpdok_gb300.solvers import MixedSolver
+    X = configs.stratified_jitter(2048, 2)
+    b = np.random.default_rng(7).standard_normal(2048)
+    A64 = O.rbf_matrix(X, gamma=1e4, reg=0.0, kernel="mq")
+    x_ref = O.fp64_solve(A64, b)
+    floor = O.relres(A64, x_ref, b)
+    A = assemble(X, gamma=1e4, reg=0.0, kernel="mq", dtype=torch.float64)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        x, info = MixedSolver(factor_dtype="fp32").solve(A, torch.from_numpy(b).cuda(), tol=1e-12)
+    xh = x.cpu().numpy()
+    assert O.relres(A64, xh, b) <= 10 * floor
+    assert np.linalg.norm(xh - x_ref) / np.linalg.norm(x_ref) < 1e-8
