@@ -78,8 +78,10 @@ static LUWork lu_work_layout(long long n, int fdtype) {
   size_t off = 0;
   auto take = [&](size_t b) { size_t o = off; off = align_up(off + b, 256); return o; };
   w.off_W = take((size_t)w.ldw * n * sizeof(float));
-  w.off_Lp = take((size_t)std::max(1LL, n) * SPW * fsize(fdtype));
-  w.off_Up = take((size_t)std::max(1LL, n) * SPW * fsize(fdtype));
+  // two operand buffers each: super-panel J + 1 is factored while the far
+  // update of super-panel J still reads its own operands (look-ahead)
+  w.off_Lp = take(2 * (size_t)std::max(1LL, n) * SPW * fsize(fdtype));
+  w.off_Up = take(2 * (size_t)std::max(1LL, n) * SPW * fsize(fdtype));
   w.off_err = take(64);
   w.total = off;
   return w;
@@ -107,6 +109,52 @@ __global__ void k_scaled_copy(const double* __restrict__ A, long long lda, long 
 // the unit-lower and upper triangles), Tmp (products of the doubling steps).
 constexpr int DP = LNB + 1;
 constexpr size_t DIAG_SMEM = (size_t)(3 * LNB * DP + 64 * 65) * sizeof(float);
+
+// One doubling step of the triangular inverses for diagonal blocks of size
+// SZ (a compile-time power of two, so the index arithmetic is shifts):
+//   lower  X21 = -X22 (L21 X11),   upper  X12 = -X11 (U12 X22).
+template <int SZ>
+__device__ __forceinline__ void inverse_doubling(const float* T, float* XL, float* XU, float* Tmp) {
+  constexpr int NP = LNB / (2 * SZ);
+  constexpr int PER = NP * SZ * SZ;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < PER; idx += blockDim.x) {
+    const int pr = idx / (SZ * SZ), e = idx % (SZ * SZ), r = e / SZ, c = e % SZ;
+    const int R = (2 * pr + 1) * SZ, C = 2 * pr * SZ;
+    float a = 0.f;
+#pragma unroll 8
+    for (int k = c; k < SZ; ++k) a = fmaf(T[(R + r) * DP + C + k], XL[(C + k) * DP + C + c], a);
+    Tmp[(pr * SZ + r) * 65 + c] = a;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < PER; idx += blockDim.x) {
+    const int pr = idx / (SZ * SZ), e = idx % (SZ * SZ), r = e / SZ, c = e % SZ;
+    const int R = (2 * pr + 1) * SZ, C = 2 * pr * SZ;
+    float a = 0.f;
+#pragma unroll 8
+    for (int k = 0; k <= r; ++k) a = fmaf(XL[(R + r) * DP + R + k], Tmp[(pr * SZ + k) * 65 + c], a);
+    XL[(R + r) * DP + C + c] = -a;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < PER; idx += blockDim.x) {
+    const int pr = idx / (SZ * SZ), e = idx % (SZ * SZ), r = e / SZ, c = e % SZ;
+    const int R = 2 * pr * SZ, C = (2 * pr + 1) * SZ;
+    float a = 0.f;
+#pragma unroll 8
+    for (int k = 0; k <= c; ++k) a = fmaf(T[(R + r) * DP + C + k], XU[(C + k) * DP + C + c], a);
+    Tmp[(pr * SZ + r) * 65 + c] = a;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < PER; idx += blockDim.x) {
+    const int pr = idx / (SZ * SZ), e = idx % (SZ * SZ), r = e / SZ, c = e % SZ;
+    const int R = 2 * pr * SZ, C = (2 * pr + 1) * SZ;
+    float a = 0.f;
+#pragma unroll 8
+    for (int k = r; k < SZ; ++k) a = fmaf(XU[(R + r) * DP + R + k], Tmp[(pr * SZ + k) * 65 + c], a);
+    XU[(R + r) * DP + C + c] = -a;
+  }
+  __syncthreads();
+}
 
 // Inverses by recursive doubling: the 32 x 32 diagonal blocks are inverted by
 // substitution (one warp per block, one lane per column), then
@@ -139,48 +187,21 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
     }
   }
   __syncthreads();
-  for (int sz = 32; sz < LNB; sz *= 2) {
-    const int np = LNB / (2 * sz);
-    const int per = np * sz * sz;
-    // lower: Tmp = L21 X11 ; X21 = -X22 Tmp
-    for (int idx = tid; idx < per; idx += blockDim.x) {
-      const int pr = idx / (sz * sz), e = idx % (sz * sz), r = e / sz, c = e % sz;
-      const int R = (2 * pr + 1) * sz, C = 2 * pr * sz;
-      float a = 0.f;
-      for (int k = c; k < sz; ++k) a = fmaf(T[(R + r) * DP + C + k], XL[(C + k) * DP + C + c], a);
-      Tmp[(pr * sz + r) * 65 + c] = a;
-    }
-    __syncthreads();
-    for (int idx = tid; idx < per; idx += blockDim.x) {
-      const int pr = idx / (sz * sz), e = idx % (sz * sz), r = e / sz, c = e % sz;
-      const int R = (2 * pr + 1) * sz, C = 2 * pr * sz;
-      float a = 0.f;
-      for (int k = 0; k <= r; ++k) a = fmaf(XL[(R + r) * DP + R + k], Tmp[(pr * sz + k) * 65 + c], a);
-      XL[(R + r) * DP + C + c] = -a;
-    }
-    __syncthreads();
-    // upper: Tmp = U12 X22 ; X12 = -X11 Tmp
-    for (int idx = tid; idx < per; idx += blockDim.x) {
-      const int pr = idx / (sz * sz), e = idx % (sz * sz), r = e / sz, c = e % sz;
-      const int R = 2 * pr * sz, C = (2 * pr + 1) * sz;
-      float a = 0.f;
-      for (int k = 0; k <= c; ++k) a = fmaf(T[(R + r) * DP + C + k], XU[(C + k) * DP + C + c], a);
-      Tmp[(pr * sz + r) * 65 + c] = a;
-    }
-    __syncthreads();
-    for (int idx = tid; idx < per; idx += blockDim.x) {
-      const int pr = idx / (sz * sz), e = idx % (sz * sz), r = e / sz, c = e % sz;
-      const int R = 2 * pr * sz, C = (2 * pr + 1) * sz;
-      float a = 0.f;
-      for (int k = r; k < sz; ++k) a = fmaf(XU[(R + r) * DP + R + k], Tmp[(pr * sz + k) * 65 + c], a);
-      XU[(R + r) * DP + C + c] = -a;
-    }
-    __syncthreads();
-  }
+  inverse_doubling<32>(T, XL, XU, Tmp);
+  inverse_doubling<64>(T, XL, XU, Tmp);
 }
 
 constexpr int DIAG_THREADS = 1024;
 
+// Blocked LU of the 128 x 128 diagonal block in four 32-column sub-panels.
+// The kernel is issue-bound on its single SM, so the work is arranged for
+// few instructions per flop:
+//   A  the sub-panel (rows >= c0, 32 columns) is factored by 4 warps; thread
+//      r keeps row r of it in registers, the pivot row goes through shared
+//      memory (double-buffered) with one 128-thread barrier per column;
+//   B  U12 = L11^-1 A12 by column-parallel forward substitution (one thread
+//      per trailing column, the column in registers);
+//   C  A22 -= L21 U12 (K = 32) by all 1024 threads.
 template <typename F>
 __global__ void __launch_bounds__(DIAG_THREADS, 1)
 k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __restrict__ LU, long long ldf,
@@ -190,61 +211,78 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
   float* XL = sm + LNB * DP;
   float* XU = sm + 2 * LNB * DP;
   float* Tmp = sm + 3 * LNB * DP;
+  __shared__ float prow[2][32];
   const int tid = threadIdx.x;
   for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
     const int r = idx % LNB, c = idx / LNB;
     T[r * DP + c] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
   }
   __syncthreads();
-  // Right-looking elimination on a 32 x 32 thread grid, one barrier per
-  // column: thread (ty, tx) updates rows j+1+ty+32a and columns j+1+tx+32b.
-  // The multipliers of column j are written back after the barrier of step
-  // j, once no thread reads the original column any more.
-  const int ty = tid / 32, tx = tid % 32;
-  float lnew[4];
-  int lcol = -1;
-  for (int j = 0; j < nbk; ++j) {
-    if (tx == 0 && lcol >= 0) {
+  for (int c0 = 0; c0 < nbk; c0 += 32) {
+    // ---- A: sub-panel columns [c0, c0 + 32), rows [c0, 128)
+    if (tid < LNB) {
+      const int r = tid;
+      float row[32];
 #pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        const int i = lcol + 1 + ty + 32 * a;
-        if (i < nbk) T[i * DP + lcol] = lnew[a];
+      for (int c = 0; c < 32; ++c) row[c] = (r >= c0) ? T[r * DP + c0 + c] : 0.f;
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj) {
+        const int j = c0 + jj;
+        if (j >= nbk) break;  // uniform across the 128 threads
+        float* pr = prow[jj & 1];
+        if (r == j) {
+          float p = row[jj];
+          if (!(fabsf(p) >= tau)) {
+            p = (p < 0.f) ? -tau : tau;
+            row[jj] = p;
+            atomicAdd(nperturb, 1);
+          }
+#pragma unroll
+          for (int c = 0; c < 32; ++c) pr[c] = row[c];
+        }
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (r > j) {
+          const float l = row[jj] * __frcp_rn(pr[jj]);  // within 1.5 ulp of row[jj] / pivot
+          row[jj] = l;
+#pragma unroll
+          for (int c = jj + 1; c < 32; ++c) row[c] = fmaf(-l, pr[c], row[c]);
+        }
+      }
+      if (r >= c0) {
+#pragma unroll
+        for (int c = 0; c < 32; ++c) T[r * DP + c0 + c] = row[c];
       }
     }
-    float p = T[j * DP + j];
-    const bool pert = !(fabsf(p) >= tau);
-    if (pert) p = (p < 0.f) ? -tau : tau;
-    float urow[4];
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const int c = j + 1 + tx + 32 * b;
-      urow[b] = (c < nbk) ? T[j * DP + c] : 0.f;
-    }
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      const int i = j + 1 + ty + 32 * a;
-      if (i >= nbk) break;
-      const float l = T[i * DP + j] / p;
-      lnew[a] = l;
-#pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        const int c = j + 1 + tx + 32 * b;
-        if (c < nbk) T[i * DP + c] = fmaf(-l, urow[b], T[i * DP + c]);
-      }
-    }
-    lcol = j;
     __syncthreads();
-    if (tid == 0 && pert) {
-      T[j * DP + j] = p;
-      atomicAdd(nperturb, 1);
-    }
-  }
-  if (tx == 0 && lcol >= 0) {
+    const int c1 = c0 + 32;
+    if (c1 >= LNB) break;
+    // ---- B: U12 = L11^-1 A12, rows [c0, c1), columns [c1, 128): one column per thread
+    if (tid < LNB - c1) {
+      const int c = c1 + tid;
+      float u[32];
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      const int i = lcol + 1 + ty + 32 * a;
-      if (i < nbk) T[i * DP + lcol] = lnew[a];
+      for (int i = 0; i < 32; ++i) u[i] = T[(c0 + i) * DP + c];
+#pragma unroll
+      for (int i = 1; i < 32; ++i) {
+        float acc = u[i];
+#pragma unroll
+        for (int k = 0; k < i; ++k) acc = fmaf(-T[(c0 + i) * DP + c0 + k], u[k], acc);
+        u[i] = acc;
+      }
+#pragma unroll
+      for (int i = 1; i < 32; ++i) T[(c0 + i) * DP + c] = u[i];
     }
+    __syncthreads();
+    // ---- C: A22 -= L21 U12 over rows and columns [c1, 128), K = 32
+    const int m = LNB - c1;
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      const int i = c1 + e / m, c = c1 + e % m;
+      float acc = T[i * DP + c];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) acc = fmaf(-T[i * DP + c0 + k], T[(c0 + k) * DP + c], acc);
+      T[i * DP + c] = acc;
+    }
+    __syncthreads();
   }
   __syncthreads();
   for (int idx = tid; idx < nbk * nbk; idx += blockDim.x) {
@@ -262,16 +300,17 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
 // --------------------------------------------------------------- TRSMs
 // L21 = W21 * Uinv.  Block: 64 rows x 128 columns; thread 4 rows x 8 columns.
 template <typename F>
-__global__ void __launch_bounds__(256)
-k_trsm_right(const float* __restrict__ W, long long ldw, long long j0, long long r_begin, long long n,
-             const float* __restrict__ Uinv, F* __restrict__ Lp, long long lp_pitch, long long lp_row0, int koff,
-             F* __restrict__ LU, long long ldf) {
+__device__ __forceinline__ void trsm_right_body(const float* __restrict__ W, long long ldw, long long j0,
+                                                long long r_begin, long long n, const float* __restrict__ Uinv,
+                                                F* __restrict__ Lp, long long lp_pitch, long long lp_row0, int koff,
+                                                F* __restrict__ LU, long long ldf, int bid) {
   extern __shared__ float sm[];
-  constexpr int XP = LNB + 4;
+  constexpr int XP = LNB + 1;     // odd pitch: the row-fastest staging writes hit distinct banks
+  constexpr int TSP = LNB + 4;    // keeps the float4 reads of Ts aligned; staging writes 4-way at most
   float* Xs = sm;                 // [64][XP]   rows of W21 (then the output tile)
-  float* Ts = sm + 64 * XP;       // [128][128] Uinv row-major [k][c]
+  float* Ts = sm + 64 * XP;       // [128][TSP] Uinv row-major [k][c]
   const int tid = threadIdx.x;
-  const long long r0 = r_begin + (long long)blockIdx.x * 64;
+  const long long r0 = r_begin + (long long)bid * 64;
   const int rows = (int)min(64LL, n - r0);
   for (int idx = tid; idx < 64 * LNB; idx += blockDim.x) {
     const int r = idx % 64, c = idx / 64;
@@ -279,7 +318,7 @@ k_trsm_right(const float* __restrict__ W, long long ldw, long long j0, long long
   }
   for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
     const int k = idx % LNB, c = idx / LNB;  // Uinv column-major: [c*128 + k]
-    Ts[k * LNB + c] = Uinv[c * LNB + k];
+    Ts[k * TSP + c] = Uinv[c * LNB + k];
   }
   __syncthreads();
   const int ty = tid / 16, tx = tid % 16;
@@ -293,8 +332,8 @@ k_trsm_right(const float* __restrict__ W, long long ldw, long long j0, long long
     float a[4], b[8];
 #pragma unroll
     for (int i = 0; i < 4; ++i) a[i] = Xs[(ty * 4 + i) * XP + k];
-    const float4 b0 = *reinterpret_cast<const float4*>(&Ts[k * LNB + tx * 8]);
-    const float4 b1 = *reinterpret_cast<const float4*>(&Ts[k * LNB + tx * 8 + 4]);
+    const float4 b0 = *reinterpret_cast<const float4*>(&Ts[k * TSP + tx * 8]);
+    const float4 b1 = *reinterpret_cast<const float4*>(&Ts[k * TSP + tx * 8 + 4]);
     b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w; b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -321,17 +360,17 @@ k_trsm_right(const float* __restrict__ W, long long ldw, long long j0, long long
 
 // U12 = Linv * W12.  Block: 128 rows x 64 columns; thread 8 rows x 4 columns.
 template <typename F>
-__global__ void __launch_bounds__(256)
-k_trsm_left(const float* __restrict__ W, long long ldw, long long j0, long long c_begin, long long n,
-            const float* __restrict__ Linv, F* __restrict__ Up, long long up_pitch, long long up_col0, int koff,
-            F* __restrict__ LU, long long ldf) {
+__device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long long ldw, long long j0,
+                                               long long c_begin, long long n, const float* __restrict__ Linv,
+                                               F* __restrict__ Up, long long up_pitch, long long up_col0, int koff,
+                                               F* __restrict__ LU, long long ldf, int bid) {
   extern __shared__ float sm[];
   constexpr int XP = 64 + 4;
   float* Xs = sm;                   // [128][XP]  W12 tile [k][c]
   float* Ts = sm + LNB * XP;        // [128][LNB+1] Linv row-major [r][k]
   constexpr int TP = LNB + 1;
   const int tid = threadIdx.x;
-  const long long c0 = c_begin + (long long)blockIdx.x * 64;
+  const long long c0 = c_begin + (long long)bid * 64;
   const int cols = (int)min(64LL, n - c0);
   for (int idx = tid; idx < LNB * 64; idx += blockDim.x) {
     const int k = idx % LNB, c = idx / LNB;
@@ -374,6 +413,20 @@ k_trsm_left(const float* __restrict__ W, long long ldw, long long j0, long long 
       LU[(j0 + r) + (c0 + c) * ldf] = v;
     }
   }
+}
+
+// Both panel solves of one inner panel in one launch: blocks [0, nb) form
+// L21 = W21 Uinv (64 rows each), the rest U12 = Linv W12 (64 columns each);
+// they write disjoint outputs, so they run side by side.
+template <typename F>
+__global__ void __launch_bounds__(256)
+k_trsm_pair(const float* __restrict__ W, long long ldw, long long j0, long long begin, long long n,
+            const float* __restrict__ Uinv, const float* __restrict__ Linv, F* __restrict__ Lp, F* __restrict__ Up,
+            long long pitch, long long base0, int koff, F* __restrict__ LU, long long ldf, int nb) {
+  if ((int)blockIdx.x < nb)
+    trsm_right_body<F>(W, ldw, j0, begin, n, Uinv, Lp, pitch, base0, koff, LU, ldf, (int)blockIdx.x);
+  else
+    trsm_left_body<F>(W, ldw, j0, begin, n, Linv, Up, pitch, base0, koff, LU, ldf, (int)blockIdx.x - nb);
 }
 
 // CUDA-core trailing update for FP32 factors: C -= A B^T, A (M x 128), B (N x 128) K-major FP32.
@@ -669,8 +722,9 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   float* d = (float*)(fb + L.off_d);
   LUMeta* meta = (LUMeta*)(fb + L.off_meta);
   float* W = (float*)(wb + w.off_W);
-  F* Lp = (F*)(wb + w.off_Lp);
-  F* Up = (F*)(wb + w.off_Up);
+  F* Lp2 = (F*)(wb + w.off_Lp);
+  F* Up2 = (F*)(wb + w.off_Up);
+  const size_t opsz = (size_t)std::max(1LL, n) * SPW;  // elements of one operand buffer
   int* errw = (int*)(wb + w.off_err);
   MPDOK_CUDA_TRY(cudaMemsetAsync(errw, 0, 64, s));
   MPDOK_CUDA_TRY(cudaMemsetAsync(meta, 0, sizeof(LUMeta), s));
@@ -680,77 +734,152 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   MPDOK_LAUNCH_CHECK("lu scale");
 
   const size_t smem_diag = DIAG_SMEM;
-  const size_t smem_tr = (size_t)(64 * (LNB + 4) + LNB * LNB) * sizeof(float);
+  const size_t smem_tr = (size_t)(64 * (LNB + 1) + LNB * (LNB + 4)) * sizeof(float);
   const size_t smem_tl = (size_t)(LNB * (64 + 4) + LNB * (LNB + 1)) * sizeof(float);
+  const size_t smem_tp = std::max(smem_tr, smem_tl);
   static bool attrs = false;
   if (!attrs) {
     MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
     MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
     MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_right<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tr));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_right<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tr));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_right<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tr));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_left<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tl));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_left<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tl));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_left<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tl));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
     attrs = true;
   }
   const float tau = 1e-6f;
   // C -= A B^T on one strip: A rows / B rows at the given Lp / Up offsets.
-  auto update = [&](long long crow, long long ccol, long long m, long long nn, const F* Ab, const F* Bb,
-                    int K) -> int {
+  auto update = [&](long long crow, long long ccol, long long m, long long nn, const F* Ab, const F* Bb, int K,
+                    cudaStream_t st) -> int {
     if (m <= 0 || nn <= 0) return MPDOK_OK;
     float* C = W + crow + ccol * w.ldw;
     if (fdtype == MPDOK_F32) {
-      const int gs = prof_start(MPDOK_PROF_LU_GEMM, s);
+      const int gs = prof_start(MPDOK_PROF_LU_GEMM, st);
       dim3 gg((unsigned)((m + 127) / 128), (unsigned)((nn + 127) / 128));
-      launch(k_gemm_update_f32, gg, 256, 0, s, C, w.ldw, (const float*)Ab, (const float*)Bb, (long long)SPW,
+      launch(k_gemm_update_f32, gg, 256, 0, st, C, w.ldw, (const float*)Ab, (const float*)Bb, (long long)SPW,
              (int)m, (int)nn, K);
-      prof_stop(gs, s, 2.0 * (double)m * (double)nn * K);
+      prof_stop(gs, st, 2.0 * (double)m * (double)nn * K);
       MPDOK_LAUNCH_CHECK("lu gemm f32");
       return MPDOK_OK;
     }
-    return gemm_update(C, w.ldw, Ab, Bb, SPW, (int)m, (int)nn, K, fdtype, MPDOK_ENGINE_TENSOR, errw, s);
+    return gemm_update(C, w.ldw, Ab, Bb, SPW, (int)m, (int)nn, K, fdtype, MPDOK_ENGINE_TENSOR, errw, st);
   };
   // Two-level right-looking LU.  Super-panel [J, Jend) of <= 512 columns is
   // factored with 128-wide panels whose updates are confined to the
   // super-panel's row strip (rows < Jend, all columns right of the panel) and
   // column strip (rows >= Jend, columns < Jend); the far trailing matrix
   // (rows, columns >= Jend) then receives all of them at once, K = 512.
-  for (long long J = 0; J < n; J += SPW) {
-    const long long Jend = std::min<long long>(n, J + SPW);
-    for (long long jp = J; jp < Jend; jp += LNB) {
-      const int k = (int)(jp / LNB);
-      const int p = (int)((jp - J) / LNB);
-      const int nbk = (int)std::min<long long>(LNB, n - jp);
-      const long long below = n - jp - nbk;
-      const int ps = prof_start(MPDOK_PROF_LU_PANEL, s);
-      launch(k_lu_diag<F>, 1, DIAG_THREADS, smem_diag, s, W, w.ldw, jp, nbk, LU, L.ldf, Linv + (size_t)k * LNB * LNB,
-             Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
-      if (below > 0) {
-        launch(k_trsm_right<F>, (unsigned)((below + 63) / 64), 256, smem_tr, s, (const float*)W, w.ldw, jp,
-               jp + LNB, n, (const float*)(Uinv + (size_t)k * LNB * LNB), Lp, (long long)SPW, J, p * LNB, LU,
-               L.ldf);
-        launch(k_trsm_left<F>, (unsigned)((below + 63) / 64), 256, smem_tl, s, (const float*)W, w.ldw, jp, jp + LNB,
-               n, (const float*)(Linv + (size_t)k * LNB * LNB), Up, (long long)SPW, J, p * LNB, LU, L.ldf);
-      }
-      prof_stop(ps, s, 2.0 * 2.0 * (double)below * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
-      MPDOK_LAUNCH_CHECK("lu panel");
-      if (below > 0) {
-        const long long r1 = jp + LNB;
-        // row strip of the super-panel: rows [r1, Jend), columns [r1, n)
-        MPDOK_TRY(update(r1, r1, Jend - r1, n - r1, Lp + (r1 - J) * SPW + p * LNB, Up + (r1 - J) * SPW + p * LNB,
-                         LNB));
-        // column strip below the super-panel: rows [Jend, n), columns [r1, Jend)
-        MPDOK_TRY(update(Jend, r1, n - Jend, Jend - r1, Lp + (Jend - J) * SPW + p * LNB,
-                         Up + (r1 - J) * SPW + p * LNB, LNB));
-      }
+  //
+  // Look-ahead: super-panels are factored on a high-priority side stream.
+  // The far update of super-panel J runs on the caller's stream in two parts:
+  // (a) the rows and columns of super-panel J + 1 (rows [Jend, Jn) x columns
+  // >= Jend, and rows >= Jn x columns [Jend, Jn)), after which the side
+  // stream may factor super-panel J + 1; (b) the rest, rows and columns >= Jn,
+  // concurrently with it.  The two touch disjoint parts of W: the inner loop
+  // of J + 1 writes rows < Jn or columns < Jn only.  Operands alternate between
+  // two buffers, so (b) of J still reads its own while J + 1 writes the other.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_ready = nullptr, ev_panel = nullptr;
+  auto cleanup = [&]() {
+    if (ev_ready) cudaEventDestroy(ev_ready);
+    if (ev_panel) cudaEventDestroy(ev_panel);
+    if (side) cudaStreamDestroy(side);
+  };
+  const bool lookahead = n > SPW;
+  if (lookahead) {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    cudaError_t e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_panel, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      cleanup();
+      return cuda_status(e, "lu look-ahead stream / events");
     }
-    // far trailing matrix: rows and columns [Jend, n), K = Jend - J
-    if (Jend < n) {
-      MPDOK_TRY(update(Jend, Jend, n - Jend, n - Jend, Lp + (Jend - J) * SPW, Up + (Jend - J) * SPW, (int)(Jend - J)));
+    e = cudaEventRecord(ev_ready, s);  // scaling and the working copy are done
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev_ready, 0);
+    if (e != cudaSuccess) {
+      cleanup();
+      return cuda_status(e, "lu look-ahead start");
     }
   }
+  auto body = [&]() -> int {
+    for (long long J = 0; J < n; J += SPW) {
+      const long long Jend = std::min<long long>(n, J + SPW);
+      const int buf = (int)((J / SPW) & 1);
+      F* Lp = Lp2 + (size_t)buf * opsz;
+      F* Up = Up2 + (size_t)buf * opsz;
+      cudaStream_t ps_stream = lookahead ? side : s;
+      for (long long jp = J; jp < Jend; jp += LNB) {
+        const int k = (int)(jp / LNB);
+        const int p = (int)((jp - J) / LNB);
+        const int nbk = (int)std::min<long long>(LNB, n - jp);
+        const long long below = n - jp - nbk;
+        const int ps = prof_start(MPDOK_PROF_LU_PANEL, ps_stream);
+        launch(k_lu_diag<F>, 1, DIAG_THREADS, smem_diag, ps_stream, W, w.ldw, jp, nbk, LU, L.ldf,
+               Linv + (size_t)k * LNB * LNB, Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
+        if (below > 0) {
+          const int nb = (int)((below + 63) / 64);
+          launch(k_trsm_pair<F>, (unsigned)(2 * nb), 256, smem_tp, ps_stream, (const float*)W, w.ldw, jp, jp + LNB, n,
+                 (const float*)(Uinv + (size_t)k * LNB * LNB), (const float*)(Linv + (size_t)k * LNB * LNB), Lp, Up,
+                 (long long)SPW, J, p * LNB, LU, L.ldf, nb);
+        }
+        prof_stop(ps, ps_stream, 2.0 * 2.0 * (double)below * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
+        MPDOK_LAUNCH_CHECK("lu panel");
+        if (below > 0) {
+          const long long r1 = jp + LNB;
+          // row strip of the super-panel: rows [r1, Jend), columns [r1, n)
+          MPDOK_TRY(update(r1, r1, Jend - r1, n - r1, Lp + (r1 - J) * SPW + p * LNB,
+                           Up + (r1 - J) * SPW + p * LNB, LNB, ps_stream));
+          // column strip below the super-panel: rows [Jend, n), columns [r1, Jend)
+          MPDOK_TRY(update(Jend, r1, n - Jend, Jend - r1, Lp + (Jend - J) * SPW + p * LNB,
+                           Up + (r1 - J) * SPW + p * LNB, LNB, ps_stream));
+        }
+      }
+      if (lookahead) {
+        MPDOK_CUDA_TRY(cudaEventRecord(ev_panel, side));
+        MPDOK_CUDA_TRY(cudaStreamWaitEvent(s, ev_panel, 0));
+      }
+      if (Jend < n) {
+        const int K = (int)(Jend - J);
+        const F* La = Lp + (Jend - J) * SPW;
+        const F* Ua = Up + (Jend - J) * SPW;
+        if (!lookahead) {
+          MPDOK_TRY(update(Jend, Jend, n - Jend, n - Jend, La, Ua, K, s));
+        } else {
+          const long long Jn = std::min<long long>(n, Jend + SPW);
+          // (a) what super-panel J + 1 reads and writes first
+          MPDOK_TRY(update(Jend, Jend, Jn - Jend, n - Jend, La, Ua, K, s));
+          MPDOK_TRY(update(Jn, Jend, n - Jn, Jn - Jend, Lp + (Jn - J) * SPW, Ua, K, s));
+          MPDOK_CUDA_TRY(cudaEventRecord(ev_ready, s));
+          MPDOK_CUDA_TRY(cudaStreamWaitEvent(side, ev_ready, 0));
+          // (b) the rest of the trailing matrix, concurrent with J + 1, in up to
+          // four column chunks: a kernel boundary on this stream drains the
+          // SMs, which lets the side stream's panel kernels (one of them needs
+          // a whole SM) in without waiting for the whole update
+          const long long rest = n - Jn;
+          const long long chunk = std::max<long long>(2048, (rest / 4 + 255) / 256 * 256);
+          for (long long c = Jn; c < n; c += chunk) {
+            const long long w = std::min<long long>(chunk, n - c);
+            MPDOK_TRY(update(Jn, c, n - Jn, w, Lp + (Jn - J) * SPW, Up + (c - J) * SPW, K, s));
+          }
+        }
+      }
+    }
+    return MPDOK_OK;
+  };
+  const int bst = body();
+  if (lookahead) {
+    // the caller's stream owns the result: join the side stream
+    if (bst == MPDOK_OK) {
+      cudaEventRecord(ev_panel, side);
+      cudaStreamWaitEvent(s, ev_panel, 0);
+    } else {
+      cudaStreamSynchronize(side);
+    }
+    cleanup();
+  }
+  if (bst < 0) return bst;
   int herr[2] = {0, 0};
   MPDOK_CUDA_TRY(cudaMemcpyAsync(herr, errw, sizeof(herr), cudaMemcpyDeviceToHost, s));
   MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
