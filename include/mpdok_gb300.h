@@ -343,6 +343,9 @@ MPDOK_API int mpdok_profile_query(int kernel_class, double* total_ms, long long*
 /* Launches of the class that a device skip flag turned off (a finished
  * Arnoldi cycle): excluded from mpdok_profile_query's totals. */
 MPDOK_API long long mpdok_profile_skipped(int kernel_class);
+/* Algorithmic bytes of a class whose work counts flops (MPDOK_PROF_LU_GEMM:
+ * the FP32 C tile read and written plus the operands), for its HBM roofline. */
+MPDOK_API double mpdok_profile_bytes(int kernel_class);
 
 /* ------------------------------------------- reference ctypes ABI (mpdok.so)
  * mpdok_ops.py:362-373: A (N x N FP64, Fortran order), b, x (FP64, x is the

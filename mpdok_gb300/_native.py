@@ -147,6 +147,7 @@ _SIGS = {
                                    c_double, c_int, c_int, c_double, c_void_p, c_size_t, ctypes.POINTER(SolveInfo),
                                    c_void_p]),
     "mpdok_profile_skipped": (c_ll, [c_int]),
+    "mpdok_profile_bytes": (c_double, [c_int]),
     "mpdok_batch_create": (c_int, [c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, ctypes.POINTER(c_void_p)]),
     "mpdok_batch_destroy": (c_int, [c_void_p]),
     "mpdok_batch_bytes": (c_size_t, [c_void_p]),
@@ -241,6 +242,11 @@ def profile_query(cls: int):
     w = c_double(0.0)
     check(load().mpdok_profile_query(cls, ctypes.byref(t), ctypes.byref(n), ctypes.byref(w)), "profile_query")
     return t.value, n.value, w.value
+
+
+def profile_bytes(cls: int) -> float:
+    """Algorithmic bytes of a class whose work counts flops."""
+    return float(load().mpdok_profile_bytes(cls))
 
 
 def profile_skipped(cls: int) -> int:

@@ -159,6 +159,8 @@ inline void launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaS
 // launch predicated on a device skip flag, that flag's value.
 int prof_start(int cls, cudaStream_t s);
 void prof_stop(int slot, cudaStream_t s, double work, const int* skip = nullptr);
+// Algorithmic bytes of the same launch, for classes whose `work` counts flops.
+void prof_stop_bytes(int slot, double bytes);
 
 // Row-major FP32 RBF tile computed in FP64 and rounded once, nugget added in
 // FP32 after the rounding (the reference's out-of-core tile).

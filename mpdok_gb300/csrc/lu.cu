@@ -759,6 +759,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
       launch(k_gemm_update_f32, gg, 256, 0, st, C, w.ldw, (const float*)Ab, (const float*)Bb, (long long)SPW,
              (int)m, (int)nn, K);
       prof_stop(gs, st, 2.0 * (double)m * (double)nn * K);
+      prof_stop_bytes(gs, 8.0 * (double)m * (double)nn + 4.0 * (double)K * ((double)m + (double)nn));
       MPDOK_LAUNCH_CHECK("lu gemm f32");
       return MPDOK_OK;
     }

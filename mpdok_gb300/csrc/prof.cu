@@ -20,6 +20,7 @@ struct ProfRec {
   cudaEvent_t a = nullptr, b = nullptr;
   int cls = 0;
   double work = 0.0;
+  double bytes = 0.0;       // algorithmic bytes, where the class records flops in `work`
   bool closed = false;
   bool predicated = false;  // the launch read a device skip flag
 };
@@ -57,6 +58,12 @@ int prof_start(int cls, cudaStream_t s) {
   cudaEventRecord(r.a, s);
   g_recs.push_back(r);
   return (int)g_recs.size() - 1;
+}
+
+void prof_stop_bytes(int slot, double bytes) {
+  if (slot < 0) return;
+  std::lock_guard<std::mutex> lk(g_pmu);
+  if ((size_t)slot < g_recs.size()) g_recs[slot].bytes = bytes;
 }
 
 void prof_stop(int slot, cudaStream_t s, double work, const int* skip) {
@@ -115,6 +122,19 @@ extern "C" int mpdok_profile_query(int cls, double* total_ms, long long* launche
   if (launches) *launches = n;
   if (work) *work = w;
   return MPDOK_OK;
+}
+
+// Algorithmic bytes of one class (recorded where `work` counts flops).
+extern "C" double mpdok_profile_bytes(int cls) {
+  std::lock_guard<std::mutex> lk(g_pmu);
+  double b = 0.0;
+  for (size_t i = 0; i < g_recs.size(); ++i) {
+    const ProfRec& r = g_recs[i];
+    if (r.cls != cls || !r.closed) continue;
+    if (r.predicated && g_skiplog[i] != 0) continue;
+    b += r.bytes;
+  }
+  return b;
 }
 
 extern "C" long long mpdok_profile_skipped(int cls) {
