@@ -25,9 +25,12 @@
 //  * Nothing in factor / solve / refine synchronises with the host, so the
 //    whole sequence is captured once into a CUDA graph and replayed with a
 //    single graph launch.
-//  * A keeps its upper triangle (the factor overwrites the lower one), so the
-//    FP64 refinement residual is a symmetric product from the stored upper
-//    triangle and the known diagonal phi(0) + reg.
+//  * Storage of A_s: the lower triangle with the diagonal, which becomes the
+//    factor, holds double-float pairs (hi, lo FP32 in the 8-byte slot), so the
+//    trailing update reads and writes it on the FP32 pipe without a single
+//    FP64 conversion; the strict upper triangle keeps A in FP64, and the FP64
+//    refinement residual is a symmetric product from it and the known
+//    diagonal phi(0) + reg.
 //  * The adjoint contraction recomputes phi and its derivatives from the
 //    coordinates (nothing of size N^2 is stored for the gradient).
 #include "common.cuh"
@@ -99,6 +102,30 @@ __device__ __forceinline__ DF to_df(double v) {
   return r;
 }
 
+// Lower-triangle slots hold double-float pairs.
+__device__ __forceinline__ DF ld_df(const double* p) {
+  const float2 f = *reinterpret_cast<const float2*>(p);
+  DF r;
+  r.h = f.x;
+  r.l = f.y;
+  return r;
+}
+__device__ __forceinline__ void st_df(double* p, DF v) {
+  *reinterpret_cast<float2*>(p) = make_float2(v.h, v.l);
+}
+__device__ __forceinline__ double df_to_f64(DF v) { return (double)v.h + (double)v.l; }
+// (a - b) in double-float with renormalisation (two-sum based).
+__device__ __forceinline__ DF df_sub(DF a, float bh, float bl) {
+  const float s = a.h - bh;
+  const float bb = s - a.h;
+  float e = (a.h - (s - bb)) + (-bh - bb);
+  e += a.l - bl;
+  DF r;
+  r.h = s + e;
+  r.l = e - (r.h - s);
+  return r;
+}
+
 // phi(r2) and its partial derivatives: g = dphi/d(r2), h = dphi/dgamma.
 template <int KIND>
 __device__ __forceinline__ void phi_derivs(double r2, double gamma, double& phi, double& g, double& h) {
@@ -152,7 +179,9 @@ __global__ void __launch_bounds__(BT) k_bassemble(const BSys* __restrict__ sys, 
     }
     double v = phi_only<KIND>(r2, q.gamma);
     if (i == j) v += q.reg;
-    Ab[(long long)i + (long long)j * q.n] = v;
+    double* slot = Ab + (long long)i + (long long)j * q.n;
+    if (i >= j) st_df(slot, to_df(v));
+    else *slot = v;
   }
 }
 
@@ -173,7 +202,7 @@ __global__ void __launch_bounds__(BT) k_bpotrf(const BSys* __restrict__ sys, int
   for (int e = threadIdx.x; e < BNB * BNB; e += BT) {
     const int i = e & 63, j = e >> 6;
     double v = 0.0;
-    if (i < nb && j < nb && i >= j) v = Ab[(long long)(kb + i) + (long long)(kb + j) * lda];
+    if (i < nb && j < nb && i >= j) v = df_to_f64(ld_df(Ab + (long long)(kb + i) + (long long)(kb + j) * lda));
     sL[i * BPAD + j] = v;
     sI[i * BPAD + j] = 0.0;
   }
@@ -213,7 +242,7 @@ __global__ void __launch_bounds__(BT) k_bpotrf(const BSys* __restrict__ sys, int
   }
   for (int e = threadIdx.x; e < BNB * BNB; e += BT) {
     const int i = e & 63, j = e >> 6;
-    if (i < nb && j < nb && i >= j) Ab[(long long)(kb + i) + (long long)(kb + j) * lda] = sL[i * BPAD + j];
+    if (i < nb && j < nb && i >= j) st_df(Ab + (long long)(kb + i) + (long long)(kb + j) * lda, to_df(sL[i * BPAD + j]));
     Linv[q.offL + (long long)k * BNB * BNB + i + (long long)j * BNB] = sI[i * BPAD + j];
   }
 }
@@ -263,15 +292,19 @@ __device__ __forceinline__ void tile_fma_df(const DF* sA, const DF* sB, float (&
   }
 }
 
-// Stage a (rows x 64) block of a column-major matrix into sT[kk][row]
-// (rows beyond `nr` and columns beyond `nc` are zero).
+// Stage a (rows x 64) block of the lower triangle (double-float slots) into
+// sT[kk][row], as FP64 or as double-float (rows beyond `nr` and columns
+// beyond `nc` are zero).
 template <typename T>
 __device__ __forceinline__ void stage_block(T* sT, const double* __restrict__ src, long long ld, int nr, int nc) {
   for (int e = threadIdx.x; e < BNB * BNB; e += BT) {
     const int r = e & 63, kk = e >> 6;
-    double v = (r < nr && kk < nc) ? src[(long long)r + (long long)kk * ld] : 0.0;
-    if constexpr (std::is_same<T, double>::value) sT[kk * BPAD + r] = v;
-    else sT[kk * BPAD + r] = to_df(v);
+    DF v;
+    v.h = 0.f;
+    v.l = 0.f;
+    if (r < nr && kk < nc) v = ld_df(src + (long long)r + (long long)kk * ld);
+    if constexpr (std::is_same<T, double>::value) sT[kk * BPAD + r] = df_to_f64(v);
+    else sT[kk * BPAD + r] = v;
   }
 }
 
@@ -307,7 +340,7 @@ __global__ void __launch_bounds__(BT) k_btrsm(const BSys* __restrict__ sys, cons
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int row = ty * 4 + i, col = tx * 4 + j;
-      if (row < nr && col < nb) Ab[(long long)(r0 + row) + (long long)(kb + col) * lda] = acc[i][j];
+      if (row < nr && col < nb) st_df(Ab + (long long)(r0 + row) + (long long)(kb + col) * lda, to_df(acc[i][j]));
     }
 }
 
@@ -352,7 +385,7 @@ __global__ void __launch_bounds__(BT) k_bsyrk(const BSys* __restrict__ sys, cons
           const int row = ty * 4 + i, col = tx * 4 + j;
           if (row < nr && col < nc && (ti != tj || row >= col)) {
             double* p = Ab + (long long)(r0 + row) + (long long)(c0 + col) * lda;
-            *p -= acc[i][j];
+            st_df(p, to_df(df_to_f64(ld_df(p)) - acc[i][j]));
           }
         }
     } else {
@@ -365,7 +398,10 @@ __global__ void __launch_bounds__(BT) k_bsyrk(const BSys* __restrict__ sys, cons
           const int row = ty * 4 + i, col = tx * 4 + j;
           if (row < nr && col < nc && (ti != tj || row >= col)) {
             double* p = Ab + (long long)(r0 + row) + (long long)(c0 + col) * lda;
-            *p -= (double)sh[i][j] + (double)sl[i][j];
+            // renormalise the accumulator, then C - acc in double-float
+            const float h = sh[i][j] + sl[i][j];
+            const float l = sl[i][j] - (h - sh[i][j]);
+            st_df(p, df_sub(ld_df(p), h, l));
           }
         }
     }
@@ -406,12 +442,16 @@ __global__ void __launch_bounds__(BT) k_bsolve_diag(const BSys* __restrict__ sys
 }
 
 // Forward: V_r -= L(r, k) V_k for r > k.  Backward: V_r -= L(k, r)^T V_k for r < k.
+// The products run in double-float on the FP32 pipe (the factor is stored
+// that way; V_k is split once per tile), the subtraction from V_r in FP64:
+// these are correction solves inside FP64 refinement, where 2^-48 products
+// are ample, and FP64 arithmetic here would run at 1/64 of the FP32 rate.
 template <bool TRANS>
 __global__ void __launch_bounds__(BT) k_bsolve_upd(const BSys* __restrict__ sys, const long long* __restrict__ pre,
                                                    int cnt, int k, int nrhs, const double* __restrict__ A,
                                                    double* __restrict__ V) {
-  __shared__ double sT[BNB * BPAD];   // sT[kk][row] = multiplier (row of the target, kk of V_k)
-  __shared__ double sX[BNB * BMAX_RHS];
+  __shared__ DF sT[BNB * BPAD];   // sT[kk][row] = multiplier (row of the target, kk of V_k)
+  __shared__ DF sX[BNB * BMAX_RHS];
   const long long t = blockIdx.x;
   int s, r;
   if (!TRANS) {
@@ -433,21 +473,36 @@ __global__ void __launch_bounds__(BT) k_bsolve_upd(const BSys* __restrict__ sys,
     // sT[kk][row] = L(kb+kk, r0+row): read the tile (kb rows, r0 cols) coalesced along kk
     for (int e = threadIdx.x; e < BNB * BNB; e += BT) {
       const int kk = e & 63, row = e >> 6;
-      sT[kk * BPAD + row] = (kk < nb && row < nr) ? Ab[(long long)(kb + kk) + (long long)(r0 + row) * lda] : 0.0;
+      DF v;
+      v.h = 0.f;
+      v.l = 0.f;
+      if (kk < nb && row < nr) v = ld_df(Ab + (long long)(kb + kk) + (long long)(r0 + row) * lda);
+      sT[kk * BPAD + row] = v;
     }
   }
   for (int e = threadIdx.x; e < BNB * nrhs; e += BT) {
     const int i = e % BNB, rr = e / BNB;
-    sX[e] = (i < nb) ? Vb[(long long)(kb + i) + (long long)rr * q.n] : 0.0;
+    sX[e] = to_df((i < nb) ? Vb[(long long)(kb + i) + (long long)rr * q.n] : 0.0);
   }
   __syncthreads();
   for (int e = threadIdx.x; e < BNB * nrhs; e += BT) {
     const int row = e % BNB, rr = e / BNB;
     if (row >= nr) continue;
-    double acc = 0.0;
-#pragma unroll 8
-    for (int kk = 0; kk < BNB; ++kk) acc = fma(sT[kk * BPAD + row], sX[rr * BNB + kk], acc);
-    Vb[(long long)(r0 + row) + (long long)rr * q.n] -= acc;
+    float sh = 0.f, sl = 0.f;
+#pragma unroll 4
+    for (int kk = 0; kk < BNB; ++kk) {
+      const DF a = sT[kk * BPAD + row], b = sX[rr * BNB + kk];
+      const float ph = a.h * b.h;
+      float pl = fmaf(a.h, b.h, -ph);
+      pl = fmaf(a.h, b.l, pl);
+      pl = fmaf(a.l, b.h, pl);
+      const float tt = sh + ph;
+      const float bp = tt - sh;
+      const float er = (sh - (tt - bp)) + (ph - bp);
+      sh = tt;
+      sl += er + pl;
+    }
+    Vb[(long long)(r0 + row) + (long long)rr * q.n] -= (double)sh + (double)sl;
   }
 }
 
