@@ -203,9 +203,17 @@ def bench_batch(args) -> int:
     import torch
     from mpdok_gb300 import configs
     from mpdok_gb300.batch import BatchedRBFSolver, pack_coords, pack_rhs
+    from mpdok_gb300.replicas import max_over_ranks, shard_imbalance, shard_systems
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     rank = int(os.environ.get("RANK", "0"))
-    systems = configs.c4(n_systems=args.systems)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    all_systems = configs.c4(n_systems=args.systems)
+    # the systems are independent: each rank solves its share (by N^3 cost), no data-path collective
+    parts = shard_systems([q.n for q in all_systems], world)
+    systems = [all_systems[i] for i in parts[rank]]
     sizes = [q.n for q in systems]
     eps = np.array([np.sqrt(q.gamma) for q in systems])
     C = pack_coords([q.coords for q in systems])
@@ -224,19 +232,27 @@ def bench_batch(args) -> int:
         lam = solver.solve(G, refine=1)
         return solver.adjoint(Xbuf, lam)
 
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
     e0.record()
     for _ in range(args.steps):
         grads = step()
     e1.record()
     torch.cuda.synchronize()
+    barrier()
     ck = clocks.stop()
-    per = e0.elapsed_time(e1) / 1e3 / args.steps
+    per = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, device="cuda")
     # factor alone, for the roofline of the trailing update
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record()
@@ -251,7 +267,7 @@ def bench_batch(args) -> int:
     ach = flops / t_factor / 1e12                     # Cholesky: sum n^3 / 3 flops
     # plain FP64 GPU solve: the vendor Cholesky per system (torch.linalg) + triangular solves
     base = None
-    if not args.no_fp64_baseline:
+    if not args.no_fp64_baseline and world == 1:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         worst = 0.0
@@ -269,7 +285,7 @@ def bench_batch(args) -> int:
         base = {"seconds_factor_solve": time.perf_counter() - t0, "relres_max": worst,
                 "method": "torch.linalg.cholesky + cholesky_solve (FP64, vendor library) per system, assembly inside"}
     cpu = None
-    if not args.no_cpu and rank == 0:
+    if not args.no_cpu and rank == 0 and world == 1:
         pick = list(range(0, len(systems), max(1, len(systems) // 12)))
         try:
             threads = len(os.sched_getaffinity(0))
@@ -289,14 +305,16 @@ def bench_batch(args) -> int:
     h2d = C.numel() * 8 + B.numel() * 8
     line = {
         "metric": "C4 batched solve + adjoint time per step (256 Gaussian RBF systems, 8 RHS)", "value": per,
-        "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": per * 1e3,
-        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (double-float update)",
+        "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": per * 1e3,
+        "higher_is_better": False, "scaling": "strong", "vs_baseline": None, "dtype": "f64 (double-float update)",
         "data": "synthetic (seeded NumPy, C4)",
         "config": {"workload": f"C4: {len(sizes)} systems, N in [{min(sizes)}, {max(sizes)}], sum N = {sum(sizes)}, "
                                "2-D uniform centres, eps~U(2,8), nugget 1e-8, 8 RHS; step = graph(factor + solve + "
                                "2 FP64 IR) + adjoint (solve + contraction)",
                    "l2": "inputs larger than L2 (A: %.1f GB FP64)" % (sum(n * n for n in sizes) * 8 / 1e9),
-                   "grid_mult": solver.grid_mult, "autotune": tune},
+                   "grid_mult": solver.grid_mult, "autotune": tune,
+                   "parallelism": f"{world} rank(s), systems sharded by N^3 (LPT), imbalance "
+                                  f"{shard_imbalance([q.n for q in all_systems], parts):.3f}"},
         "relres_max": float(relres.max()), "relres_median": float(np.median(relres)),
         "factor_seconds": t_factor,
         "roofline": {"bound": "fp32 pipe (double-float trailing update)", "achieved": ach,
@@ -324,10 +342,15 @@ def bench_batch(args) -> int:
         torch.cuda.synchronize()
         if i > 0:
             times.append(time.perf_counter() - t0)
-    line["e2e"] = {"value": sum(times) / len(times), "unit": "s", "h2d_bytes_per_step": h2d,
+    line["e2e"] = {"value": max_over_ranks(sum(times) / len(times), device="cuda"), "unit": "s",
+                   "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": sum(o.numel() * 8 for o in out),
                    "api": "BatchedRBFSolver.load + run_graph + solve + adjoint from pinned host coords/B"}
-    print(json.dumps(line))
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
     return 0
 
 
