@@ -240,6 +240,17 @@ MPDOK_API int mpdok_lu_ir_solve(const double* A, long long lda, long long n, con
 /* Three-precision GMRES-IR: the LU (BF16/FP16) preconditions FP32 GMRES on
  * the FP32 copy of A (right preconditioning), FP64 residual r = b - A x and
  * FP64 update x += d, FP64 Hessenberg / Givens. */
+/* LU-IR on nrhs <= 8 right-hand sides together (the reference's
+ * LUIRSolver.solve_factored, mpdok_ops.py:280-320, batched over the fields of
+ * its time-series use): X = LU^-1 B, then R = B - A X in FP64 (one multi-RHS
+ * GEMV) and X += LU^-1 R (one multi-RHS triangular sweep pair, each factor
+ * tile read once for all columns) until max_k ||R_k|| / ||B_k|| < tol or
+ * maxiter_outer corrections.  info->relres is the worst column. */
+MPDOK_API size_t mpdok_lu_ir_multi_work_size(long long n, int nrhs);
+MPDOK_API int mpdok_lu_ir_solve_multi(const double* A, long long lda, long long n, const void* factors, int fdtype,
+                                      int nrhs, const double* B, long long ldb, double* X, long long ldx, double tol,
+                                      int maxiter_outer, void* work, size_t work_bytes, mpdok_solve_info* info,
+                                      cudaStream_t stream);
 MPDOK_API size_t mpdok_lu_gmres_ir_work_size(long long n, int restart);
 MPDOK_API int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* A32, long long lda32, long long n,
                                 const void* factors, int fdtype, const double* b, double* x, double tol,

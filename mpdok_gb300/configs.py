@@ -101,3 +101,25 @@ def c5(n: int = 250000) -> RBFSystem:
 
 def by_name(name: str, **kw):
     return {"C1": c1, "C2": c2, "C3": c3, "HEADLINE": headline, "C4": c4, "C5": c5}[name.upper()](**kw)
+
+
+def time_series_fields(n: int = 8192, steps: int = 24, seed: int = 42):
+    """Factor-once / many-RHS workload: n sensors uniform in a 100 x 100 square
+    (seed), three smooth fields sampled at `steps` times (3 * steps RHS).
+
+    Seeded synthetic stand-in with the shape of the reference's time-series
+    demo (rbf_demo.ipynb cells 3-7: N=8192, 3 fields x 24 steps, reg 1e-2,
+    tol 1e-5); the field formulas are this module's own.
+    """
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(0.0, 100.0, size=(n, 2))
+    x, y = X[:, 0] / 100.0, X[:, 1] / 100.0
+    cols = []
+    for t in range(steps):
+        ph = 2.0 * np.pi * t / steps
+        temp = 15.0 + 5.0 * np.sin(2 * np.pi * x + ph) * np.cos(2 * np.pi * y) + 0.1 * rng.standard_normal(n)
+        pres = 10.0 * np.cos(2 * np.pi * (x + y) - ph) + 0.05 * rng.standard_normal(n)
+        hum = 40.0 + 30.0 * np.exp(-((x - 0.5 - 0.2 * np.sin(ph)) ** 2 + (y - 0.5) ** 2) / 0.08) \
+            + 0.5 * rng.standard_normal(n)
+        cols += [temp, pres, hum]
+    return X, np.stack(cols, axis=1)

@@ -27,6 +27,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 namespace mpdok {
 
@@ -639,6 +640,116 @@ __global__ void k_scale_out(const float* __restrict__ z, const float* __restrict
     out[i] = z[i] * d[i];
 }
 
+// Triangular solve with K right-hand sides (columns of rhs / out, leading
+// dimension ld), the chained block sweep of k_trsv: each 128 x 128 factor
+// tile is loaded once into registers and applied to all K columns, so the
+// factor bytes per right-hand side drop by K.
+template <typename F, bool LOWER, int K>
+__global__ void __launch_bounds__(256)
+k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, long long n, int nblk,
+             const float* __restrict__ rhs, long long ld, const float* __restrict__ dsc, float* out, int* flags,
+             int* ticket, int* err) {
+  extern __shared__ float sDi[];      // 128 x 128 diagonal-block inverse (column-major)
+  __shared__ int s_t;
+  __shared__ int s_abort;
+  __shared__ float s_x[2][K][LNB];
+  __shared__ float s_part[16][LNB + 1];
+  __shared__ float s_a[K][LNB];
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    s_t = atomicAdd(ticket, 1);
+    s_abort = 0;
+  }
+  __syncthreads();
+  const int tk = s_t;
+  if (tk >= nblk) return;
+  const int t = LOWER ? tk : (nblk - 1 - tk);
+  const long long r0 = (long long)t * LNB;
+  const int rows = (int)min((long long)LNB, n - r0);
+  const float* Di = Dinv + (long long)t * LNB * LNB;
+  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) sDi[idx] = __ldg(Di + idx);
+  const int rg = tid % 16, cg = tid / 16;
+  const long long rbase = r0 + rg * 8;
+  float acc[K][8];
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) acc[k][v] = 0.f;
+  const int cnt = LOWER ? t : (nblk - 1 - t);
+  for (int q = 0; q < cnt; ++q) {
+    const int j = LOWER ? q : (nblk - 1 - q);
+    const long long c0 = (long long)j * LNB;
+    const int cols = (int)min((long long)LNB, n - c0);
+    TileRegs<F> T;
+    tile_load<F>(T, LU, ldf, c0, cols, rbase, n, cg);
+    if (tid < LNB) {
+      bool ok = true;
+      long long it = 0;
+      while (ld_acquire(flags + j) == 0) {
+        if (++it > SPIN_LIMIT) { ok = false; break; }
+        if (it > 256) __nanosleep(32);
+      }
+      if (!ok) {
+        s_abort = 1;
+        atomicExch(err, 2);
+      }
+#pragma unroll
+      for (int k = 0; k < K; ++k) s_x[q & 1][k][tid] = (tid < cols) ? __ldcg(out + (long long)k * ld + c0 + tid) : 0.f;
+    }
+    __syncthreads();
+    if (s_abort) return;
+#pragma unroll
+    for (int k = 0; k < K; ++k) tile_fma<F>(T, s_x[q & 1][k], cg, acc[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    __syncthreads();
+#pragma unroll
+    for (int v = 0; v < 8; ++v) s_part[cg][rg * 8 + v] = acc[k][v];
+    __syncthreads();
+    if (tid < LNB) {
+      float sum = 0.f;
+#pragma unroll
+      for (int g = 0; g < 16; ++g) sum += s_part[g][tid];
+      float r = 0.f;
+      if (tid < rows) {
+        const float b = rhs[(long long)k * ld + r0 + tid];
+        r = LOWER ? b * dsc[r0 + tid] : b;
+      }
+      s_a[k][tid] = r - sum;
+    }
+  }
+  __syncthreads();
+  // y = Dinv a for every column: thread (row, column group)
+  for (int e = tid; e < LNB * K; e += blockDim.x) {
+    const int row = e % LNB, k = e / LNB;
+    float y = 0.f;
+    if (LOWER) {
+#pragma unroll 8
+      for (int c = 0; c < LNB; ++c) if (c <= row) y = fmaf(sDi[c * LNB + row], s_a[k][c], y);
+    } else {
+#pragma unroll 8
+      for (int c = 0; c < LNB; ++c) if (c >= row) y = fmaf(sDi[c * LNB + row], s_a[k][c], y);
+    }
+    if (row < rows) out[(long long)k * ld + r0 + row] = y;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(flags + t), "r"(1) : "memory");
+  }
+}
+
+// out[:, k] = z[:, k] * d for K columns (leading dimension ld).
+__global__ void k_scale_out_multi(const float* __restrict__ z, const float* __restrict__ d, float* __restrict__ out,
+                                  long long n, long long ld, int K) {
+  const long long total = n * K;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const long long i = e % n, k = e / n;
+    out[k * ld + i] = z[k * ld + i] * d[i];
+  }
+}
+
 // ---------------------------------------------------------------- host side
 
 static unsigned grid_for(long long n, int per = 256) {
@@ -1055,6 +1166,187 @@ extern "C" int mpdok_lu_ir_solve(const double* A, long long lda, long long n, co
   }
   if (info) { info->converged = conv ? 1 : 0; info->inner_iters = it + 1; }
   MPDOK_LAUNCH_CHECK("lu_ir");
+  return MPDOK_OK;
+}
+
+// ---------------------------------------------------- multi-RHS LU-IR
+struct MultiWork {
+  size_t off_y = 0, off_z = 0, off_v = 0, off_flags = 0, off_tk = 0, off_err = 0, off_r = 0, off_nrm = 0,
+         off_g = 0, total = 0;
+};
+
+static MultiWork multi_layout(long long n, int K) {
+  MultiWork m;
+  const int nblk = (int)((n + LNB - 1) / LNB);
+  size_t off = 0;
+  auto take = [&](size_t b) { size_t o = off; off = align_up(off + b, 256); return o; };
+  const size_t nv = (size_t)std::max(1LL, n) * K;
+  m.off_y = take(nv * sizeof(float));
+  m.off_z = take(nv * sizeof(float));
+  m.off_v = take(nv * sizeof(float));
+  m.off_flags = take((size_t)2 * std::max(1, nblk) * sizeof(int));
+  m.off_tk = take(4 * sizeof(int));
+  m.off_err = take(16);
+  m.off_r = take(nv * sizeof(double));
+  m.off_nrm = take((size_t)K * sizeof(double));
+  m.off_g = take(gemv_workspace_bytes(MPDOK_F64, n, n, K, false));
+  m.total = off;
+  return m;
+}
+
+template <typename F, int K>
+static int lu_apply_multi_t(const void* fbuf, long long n, int fdtype, const float* v, float* z, void* work,
+                            cudaStream_t s) {
+  const LULayout L = lu_layout(n, fdtype);
+  const MultiWork mw = multi_layout(n, K);
+  const char* fb = (const char*)fbuf;
+  char* wb = (char*)work;
+  const F* LU = (const F*)(fb + L.off_lu);
+  const float* Linv = (const float*)(fb + L.off_linv);
+  const float* Uinv = (const float*)(fb + L.off_uinv);
+  const float* d = (const float*)(fb + L.off_d);
+  float* y = (float*)(wb + mw.off_y);
+  float* zz = (float*)(wb + mw.off_z);
+  int* flags = (int*)(wb + mw.off_flags);
+  int* tk = (int*)(wb + mw.off_tk);
+  int* err = (int*)(wb + mw.off_err);
+  MPDOK_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 2 * L.nblk, s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(tk, 0, sizeof(int) * 2, s));
+  const size_t smem = (size_t)LNB * LNB * sizeof(float);
+  static bool attr = false;
+  if (!attr) {
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv_multi<F, true, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv_multi<F, false, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  const int slot = prof_start(MPDOK_PROF_TRSV, s);
+  launch(k_trsv_multi<F, true, K>, L.nblk, 256, smem, s, LU, L.ldf, Linv, n, L.nblk, v, n, d, y, flags, tk, err);
+  launch(k_trsv_multi<F, false, K>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, n, L.nblk, (const float*)y, n, d, zz,
+         flags + L.nblk, tk + 1, err);
+  launch(k_scale_out_multi, grid_for(n * K), 256, 0, s, (const float*)zz, d, z, n, n, K);
+  prof_stop(slot, s, (double)n * (double)n * sizeof(F));
+  MPDOK_LAUNCH_CHECK("lu apply multi");
+  return MPDOK_OK;
+}
+
+template <typename F>
+static int lu_apply_multi_f(const void* fbuf, long long n, int fdtype, int K, const float* v, float* z, void* work,
+                            cudaStream_t s) {
+  switch (K) {
+    case 1: return lu_apply_multi_t<F, 1>(fbuf, n, fdtype, v, z, work, s);
+    case 2: return lu_apply_multi_t<F, 2>(fbuf, n, fdtype, v, z, work, s);
+    case 3: return lu_apply_multi_t<F, 3>(fbuf, n, fdtype, v, z, work, s);
+    case 4: return lu_apply_multi_t<F, 4>(fbuf, n, fdtype, v, z, work, s);
+    case 5: return lu_apply_multi_t<F, 5>(fbuf, n, fdtype, v, z, work, s);
+    case 6: return lu_apply_multi_t<F, 6>(fbuf, n, fdtype, v, z, work, s);
+    case 7: return lu_apply_multi_t<F, 7>(fbuf, n, fdtype, v, z, work, s);
+    default: return lu_apply_multi_t<F, 8>(fbuf, n, fdtype, v, z, work, s);
+  }
+}
+
+static int lu_apply_multi(const void* fbuf, long long n, int fdtype, int K, const float* v, float* z, void* work,
+                          cudaStream_t s) {
+  switch (fdtype) {
+    case MPDOK_BF16: return lu_apply_multi_f<__nv_bfloat16>(fbuf, n, fdtype, K, v, z, work, s);
+    case MPDOK_F16: return lu_apply_multi_f<__half>(fbuf, n, fdtype, K, v, z, work, s);
+    default: return lu_apply_multi_f<float>(fbuf, n, fdtype, K, v, z, work, s);
+  }
+}
+
+__global__ void k_f64_to_f32_cols(const double* __restrict__ a, long long lda, float* __restrict__ b, long long n,
+                                  int K) {
+  const long long total = n * K;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const long long i = e % n, k = e / n;
+    b[e] = (float)a[k * lda + i];
+  }
+}
+
+__global__ void k_add_f32_cols(const float* __restrict__ e32, double* __restrict__ x, long long ldx, long long n, int K,
+                               int assign) {
+  const long long total = n * K;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const long long i = e % n, k = e / n;
+    x[k * ldx + i] = assign ? (double)e32[e] : x[k * ldx + i] + (double)e32[e];
+  }
+}
+
+extern "C" size_t mpdok_lu_ir_multi_work_size(long long n, int nrhs) {
+  if (n < 0 || nrhs < 1 || nrhs > 8) return 0;
+  return multi_layout(n, nrhs).total + 256;
+}
+
+// LU-IR on nrhs <= 8 right-hand sides together: X = LU^-1 B, then until every
+// column meets tol: R = B - A X (one FP64 multi-RHS GEMV), X += LU^-1 R (one
+// multi-RHS triangular sweep pair).  The per-solve form of the reference's
+// LUIRSolver.solve_factored (mpdok_ops.py:280-320), batched over right-hand
+// sides the way its time-series use (factor once, many fields) calls it.
+extern "C" int mpdok_lu_ir_solve_multi(const double* A, long long lda, long long n, const void* factors, int fdtype,
+                                       int nrhs, const double* B, long long ldb, double* X, long long ldx, double tol,
+                                       int maxiter_outer, void* work, size_t work_bytes, mpdok_solve_info* info,
+                                       cudaStream_t s) {
+  if (info) std::memset(info, 0, sizeof(*info));
+  MPDOK_ARG_CHECK(n >= 0 && nrhs >= 1 && nrhs <= 8, "n >= 0 and nrhs in [1, 8]");
+  if (n == 0) { if (info) info->converged = 1; return MPDOK_OK; }
+  MPDOK_ARG_CHECK(A && factors && B && X && work, "null pointer");
+  MPDOK_ARG_CHECK(lda >= n && ldb >= n && ldx >= n, "leading dimensions must be >= n");
+  MPDOK_ARG_CHECK(work_bytes >= mpdok_lu_ir_multi_work_size(n, nrhs), "multi-RHS LU-IR work buffer too small");
+  LUMeta hm;
+  MPDOK_TRY(read_meta(factors, n, fdtype, &hm, s));
+  if (!hm.valid || hm.fdtype != fdtype || hm.n_lo != (int)(n & 0x7fffffff)) {
+    set_error("no factorization of this size / type in the factor buffer");
+    return MPDOK_ERR_NOT_FACTORED;
+  }
+  const MultiWork mw = multi_layout(n, nrhs);
+  char* wb = (char*)work;
+  float* v32 = (float*)(wb + mw.off_v);  // FP32 right-hand sides in, corrections out (in place)
+  double* R = (double*)(wb + mw.off_r);
+  double* nrm = (double*)(wb + mw.off_nrm);
+  void* gw = wb + mw.off_g;
+  const size_t gbytes = gemv_workspace_bytes(MPDOK_F64, n, n, nrhs, false);
+  float* zout = v32;  // the sweeps run through the y / z buffers of the workspace; the scaled result lands in v32
+  std::vector<double> bn(nrhs), rn(nrhs);
+  MPDOK_TRY(colnorms_f64(B, n, nrhs, ldb, nrm, s));
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(bn.data(), nrm, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int k = 0; k < nrhs; ++k) bn[k] = std::sqrt(bn[k]);
+  if (info) info->bnorm = *std::max_element(bn.begin(), bn.end());
+  const unsigned g = grid_for(n * nrhs);
+  launch(k_f64_to_f32_cols, g, 256, 0, s, B, ldb, v32, n, nrhs);
+  MPDOK_TRY(lu_apply_multi(factors, n, fdtype, nrhs, v32, zout, wb, s));
+  launch(k_add_f32_cols, g, 256, 0, s, (const float*)zout, X, ldx, n, nrhs, 1);
+  bool conv = false;
+  int it = 0;
+  double worst = 0.0;
+  for (it = 0; it <= maxiter_outer; ++it) {
+    MPDOK_TRY(gemv_launch(MPDOK_F64, false, A, lda, n, n, X, ldx, nrhs, R, n, -1.0, 1.0, B, ldb, nullptr, gw, gbytes,
+                          s, true, nullptr));
+    MPDOK_TRY(colnorms_f64(R, n, nrhs, n, nrm, s));
+    MPDOK_CUDA_TRY(cudaMemcpyAsync(rn.data(), nrm, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+    MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+    worst = 0.0;
+    for (int k = 0; k < nrhs; ++k) {
+      const double rel = bn[k] > 0.0 ? std::sqrt(rn[k]) / bn[k] : std::sqrt(rn[k]);
+      if (!std::isfinite(rel)) { set_error("multi-RHS LU-IR: non-finite residual"); return MPDOK_ERR_NONFINITE; }
+      worst = std::max(worst, rel);
+    }
+    if (info && info->n_history < MPDOK_HISTORY_MAX) {
+      info->hist_iter[info->n_history] = it;
+      info->history[info->n_history++] = worst;
+    }
+    if (worst < tol) { conv = true; break; }
+    if (it == maxiter_outer) break;
+    launch(k_f64_to_f32_cols, g, 256, 0, s, (const double*)R, n, v32, n, nrhs);
+    MPDOK_TRY(lu_apply_multi(factors, n, fdtype, nrhs, v32, zout, wb, s));
+    launch(k_add_f32_cols, g, 256, 0, s, (const float*)zout, X, ldx, n, nrhs, 0);
+    if (info) info->outer_iters = it + 1;
+  }
+  if (info) {
+    info->relres = worst;
+    info->converged = conv ? 1 : 0;
+    info->inner_iters = it + 1;
+  }
+  MPDOK_LAUNCH_CHECK("lu_ir multi");
   return MPDOK_OK;
 }
 

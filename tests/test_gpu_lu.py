@@ -172,3 +172,28 @@ def test_mixed_solver_fp32_factors_on_moderate_mq():
     xh = x.cpu().numpy()
     assert O.relres(A64, xh, b) <= 10 * floor
     assert np.linalg.norm(xh - x_ref) / np.linalg.norm(x_ref) < 1e-8
+
+
+@pytest.mark.parametrize("fdtype", ["fp32", "bf16"])
+@pytest.mark.parametrize("n,k", [(1000, 1), (1500, 8), (777, 19)])
+def test_lu_ir_many_rhs_matches_single_rhs_and_oracle(fdtype, n, k):
+    """Multi-RHS LU-IR (one triangular sweep pair for up to 8 columns) against
+    the FP64 LU oracle, and column by column against the single-RHS LU-IR."""
+    from mpdok_gb300.lu import LUFactorization
+    rng = np.random.default_rng(n + k)
+    X = rng.uniform(0, 1, (n, 2))
+    A64 = O.rbf_matrix(X, gamma=1600.0, reg=1e-1)  # kappa ~ 20: plain refinement converges with BF16 factors
+    B = rng.standard_normal((n, k))
+    A = torch.from_numpy(np.asfortranarray(A64)).cuda()
+    lu = LUFactorization(A, dtype=fdtype)
+    Xg, info = lu.solve_ir_many(A, torch.from_numpy(B).cuda(), tol=1e-12, maxiter_outer=10)
+    assert info["converged"]
+    Xh = Xg.cpu().numpy().reshape(n, k)
+    Xref = np.linalg.solve(A64, B)
+    for j in range(k):
+        rel = O.relres(A64, Xh[:, j], B[:, j])
+        assert rel < 1e-12
+        assert np.linalg.norm(Xh[:, j] - Xref[:, j]) / np.linalg.norm(Xref[:, j]) < 1e-10
+    xs, d = lu.solve_ir(A, torch.from_numpy(B[:, 0].copy()).cuda(), tol=1e-12, maxiter_outer=10)
+    assert d["converged"]
+    np.testing.assert_allclose(Xh[:, 0], xs.cpu().numpy(), rtol=1e-9, atol=1e-12 * np.abs(Xh[:, 0]).max())
