@@ -366,6 +366,10 @@ MPDOK_API void py_gmres_ir(double* A, double* b, double* x, float* A_fp32, int N
                  int restart, int* converged_out);
 /* mpdok_ops.py:375-382: (N, N) FP64 managed allocation, kept until
  * py_free_managed(). */
+/* Placement of the last py_alloc_managed / py_lu_alloc_managed buffer: 0 device
+ * memory (the normal case on GB300), 1 managed memory placed on the device
+ * (when a device allocation of that size failed), -1 failure. */
+MPDOK_API int mpdok_managed_kind(void);
 MPDOK_API void py_alloc_managed(int N, void** ptr_out);
 MPDOK_API void py_free_managed(void);
 

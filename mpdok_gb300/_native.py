@@ -147,6 +147,7 @@ _SIGS = {
                                    c_double, c_int, c_int, c_double, c_void_p, c_size_t, ctypes.POINTER(SolveInfo),
                                    c_void_p]),
     "mpdok_profile_skipped": (c_ll, [c_int]),
+    "mpdok_managed_kind": (c_int, []),
     "mpdok_lu_ir_multi_work_size": (c_size_t, [c_ll, c_int]),
     "mpdok_lu_ir_solve_multi": (c_int, [c_void_p, c_ll, c_ll, c_void_p, c_int, c_int, c_void_p, c_ll, c_void_p, c_ll,
                                         c_double, c_int, c_void_p, c_size_t, ctypes.POINTER(SolveInfo), c_void_p]),

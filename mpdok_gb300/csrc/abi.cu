@@ -59,6 +59,39 @@ extern "C" void py_gmres_ir(double* A, double* b, double* x, float* A_fp32, int 
   if (s == MPDOK_OK && converged_out) *converged_out = info.converged;
 }
 
+// Storage behind py_alloc_managed / py_lu_alloc_managed (mpdok_ops.py:34-66,
+// :147-174, :388-418).  The reference uses managed memory so that an 8 GB card
+// can hold A beyond its memory, at the price of page migration (thrashing
+// once A exceeds the device).  With 280 GB of HBM, A (N x N FP64) fits up to
+// N ~ 180000: the buffer is plain device memory, and only when that
+// allocation fails is it managed memory placed on the device (preferred
+// location + prefetch), so that it still runs from HBM as far as it fits.
+// Returns 0 for device memory, 1 for managed, -1 on failure.
+static int alloc_matrix(size_t bytes, void** p) {
+  *p = nullptr;
+  if (cudaMalloc(p, bytes) == cudaSuccess) return 0;
+  cudaGetLastError();  // clear the allocation failure
+  cudaError_t e = cudaMallocManaged(p, bytes, cudaMemAttachGlobal);
+  if (e != cudaSuccess) {
+    cuda_status(e, "managed allocation");
+    *p = nullptr;
+    return -1;
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaMemLocation loc;
+  loc.type = cudaMemLocationTypeDevice;
+  loc.id = dev;
+  cudaMemAdvise(*p, bytes, cudaMemAdviseSetPreferredLocation, loc);
+  cudaMemPrefetchAsync(*p, bytes, loc, 0, (cudaStream_t)0);
+  cudaGetLastError();  // advice and prefetch are hints
+  return 1;
+}
+
+static int g_last_alloc_kind = -1;
+
+extern "C" int mpdok_managed_kind(void) { return g_last_alloc_kind; }
+
 extern "C" void py_alloc_managed(int N, void** ptr_out) {
   if (!ptr_out) return;
   *ptr_out = nullptr;
@@ -70,11 +103,8 @@ extern "C" void py_alloc_managed(int N, void** ptr_out) {
     st.managed = nullptr;
   }
   void* p = nullptr;
-  cudaError_t e = cudaMallocManaged(&p, (size_t)N * (size_t)N * sizeof(double), cudaMemAttachGlobal);
-  if (e != cudaSuccess) {
-    cuda_status(e, "py_alloc_managed");
-    return;
-  }
+  g_last_alloc_kind = alloc_matrix((size_t)N * (size_t)N * sizeof(double), &p);
+  if (!p) return;
   st.managed = p;
   *ptr_out = p;
 }
@@ -194,11 +224,8 @@ extern "C" void py_lu_alloc_managed(int N, void** ptr_out) {
     st.managed = nullptr;
   }
   void* p = nullptr;
-  cudaError_t e = cudaMallocManaged(&p, (size_t)N * (size_t)N * sizeof(double), cudaMemAttachGlobal);
-  if (e != cudaSuccess) {
-    cuda_status(e, "py_lu_alloc_managed");
-    return;
-  }
+  g_last_alloc_kind = alloc_matrix((size_t)N * (size_t)N * sizeof(double), &p);
+  if (!p) return;
   st.managed = p;
   *ptr_out = p;
 }

@@ -104,7 +104,8 @@ class MPDOKSolver:
 
     # -- managed memory ---------------------------------------------------
     def alloc_managed(self, N_):
-        """(N, N) FP64 matrix in CUDA managed memory (py_alloc_managed)."""
+        """(N, N) FP64 matrix for the solver (py_alloc_managed): device memory on
+        GB300, managed memory placed on the device only if that does not fit."""
         p = ctypes.c_void_p()
         self._lib.py_alloc_managed(ctypes.c_int(N_), ctypes.byref(p))
         if not p.value:

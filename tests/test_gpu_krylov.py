@@ -154,3 +154,24 @@ def test_cg_on_spd_rbf_reaches_fp32_floor():
     assert c and c_or
     assert abs(len(h) - len(h_or)) <= 1
     assert O.relres(A64, _np(x), b) < 1e-5
+
+
+def test_alloc_managed_is_device_memory_and_solves():
+    """py_alloc_managed / py_lu_alloc_managed keep the reference's API but hand
+    out device memory (no page migration); the solvers run on it."""
+    from mpdok_gb300 import _native as N
+    from mpdok_gb300.mpdok_ops import LUIRSolver, MPDOKSolver
+    rng = np.random.default_rng(12)
+    n = 700
+    X = rng.uniform(0, 1, (n, 2))
+    A64 = O.rbf_matrix(X, gamma=400.0, reg=1e-2)
+    b = rng.standard_normal(n)
+    for cls in (MPDOKSolver, LUIRSolver):
+        s = cls()
+        M = s.alloc_managed(n)
+        assert N.load().mpdok_managed_kind() == 0
+        M[:, :] = torch.from_numpy(A64).cuda()
+        kw = {"maxiter_outer": 20, "restart": 50} if cls is MPDOKSolver else {"maxiter_outer": 5}
+        x = s.solve(M.array, torch.from_numpy(b).cuda(), tol=1e-12, **kw).cpu().numpy()
+        assert O.relres(A64, x, b) < 1e-11
+        s.free_managed()
