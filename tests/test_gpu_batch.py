@@ -189,3 +189,36 @@ def test_batch_rejects_bad_arguments():
         s.factor()
     with pytest.raises(ValueError):
         s.load([np.zeros((10, 2)), np.zeros((19, 2))], 3.0, 1e-6)
+
+
+def test_c1_as_specified_reaches_the_fp64_floor():
+    """C1 (N=2000, eps=3, nugget 1e-10, kappa ~ 5e12): 1e-12 is out of reach even
+    for FP64 LU (its relres ~ 2e-7).  The double-float Cholesky with FP64
+    refinement reaches the oracle's own floor."""
+    from mpdok_gb300 import configs
+    from mpdok_gb300.batch import BatchedRBFSolver
+    c1 = configs.c1()
+    s = BatchedRBFSolver([c1.n], dim=2, nrhs=1, grid_mult=2)
+    s.load([c1.coords], [3.0], c1.reg).factor()
+    x = s.solve([np.asarray(c1.b).reshape(-1, 1)], refine=3).cpu().numpy()
+    x_ref, rel_ref = R.solve(c1.coords, 3.0, c1.reg, np.asarray(c1.b))
+    A = R.rbf(c1.coords, 3.0, c1.reg)
+    rel = np.linalg.norm(c1.b - A @ x) / np.linalg.norm(c1.b)
+    assert rel <= 10 * rel_ref, (rel, rel_ref)
+
+
+def test_c2_family_reaches_the_fp64_floor_with_four_rhs():
+    """C2 family at N=5000 (3-D, eps=5, nugget 1e-6, 4 RHS, kappa ~ 1.8e8): no FP32
+    Krylov body converges here; the batched Cholesky reaches the FP64 floor."""
+    from mpdok_gb300 import configs
+    from mpdok_gb300.batch import BatchedRBFSolver, unpack_rhs
+    c2 = configs.c2(n=5000)
+    B = np.asarray(c2.b)
+    s = BatchedRBFSolver([c2.n], dim=3, nrhs=4, grid_mult=2)
+    s.load([c2.coords], [5.0], c2.reg).factor()
+    X = unpack_rhs(s.solve([B], refine=3), [c2.n], 4)[0].cpu().numpy()
+    x_ref, rel_ref = R.solve(c2.coords, 5.0, c2.reg, B)
+    A = R.rbf(c2.coords, 5.0, c2.reg)
+    rel = np.max(np.linalg.norm(B - A @ X, axis=0) / np.linalg.norm(B, axis=0))
+    assert rel <= 10 * rel_ref, (rel, rel_ref)
+    assert np.linalg.norm(X - x_ref) / np.linalg.norm(x_ref) < 1e-3
