@@ -407,8 +407,10 @@ def bench_ooc(args) -> int:
     e1.record()
     torch.cuda.synchronize()
     mf_ms = e0.elapsed_time(e1) / args.steps
+    import tempfile
     ssd = None
-    path = ROOT / "gpurun_out" / "ooc_store.bin" if (ROOT / "gpurun_out").exists() else Path("/tmp/ooc_store.bin")
+    tmpdir = tempfile.mkdtemp(prefix="mpdok_ooc_")
+    path = Path(tmpdir) / "ooc_store.bin"
     try:
         n2 = min(n, 16384)
         s2 = MPDOKOOCSolver(tile_rows=2048)
@@ -427,6 +429,7 @@ def bench_ooc(args) -> int:
     finally:
         if path.exists():
             path.unlink()
+        os.rmdir(tmpdir)
     line = {"metric": "OOC streamed FP32 matvec rate (C5 layout, pinned host RAM store)", "value": gbs, "unit": "GB/s",
             "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",

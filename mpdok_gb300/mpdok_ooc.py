@@ -118,8 +118,15 @@ class MPDOKOOCSolver:
 
     def free(self):
         """Release the store and the device buffers."""
-        if self._h:
+        if getattr(self, "_h", None):
             N.load().mpdok_ooc_destroy(self._h)
         self._h = None
         self._coords = None
         self._ws.release()
+
+    def __del__(self):
+        # the pinned host store can be tens of GB: release it with the object
+        try:
+            self.free()
+        except Exception:
+            pass
