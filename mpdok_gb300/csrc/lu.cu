@@ -40,7 +40,7 @@ static int fsize(int fdtype) { return fdtype == MPDOK_F32 ? 4 : 2; }
 struct LULayout {
   long long n = 0, ldf = 0;
   int nblk = 0, fdtype = MPDOK_BF16;
-  size_t off_lu = 0, off_linv = 0, off_uinv = 0, off_d = 0, off_meta = 0, total = 0;
+  size_t off_lu = 0, off_linv = 0, off_uinv = 0, off_ml = 0, off_mu = 0, off_d = 0, off_meta = 0, total = 0;
 };
 
 struct LUMeta {
@@ -62,6 +62,9 @@ static LULayout lu_layout(long long n, int fdtype) {
   L.off_lu = take((size_t)L.ldf * n * fsize(fdtype));
   L.off_linv = take((size_t)L.nblk * LNB * LNB * sizeof(float));
   L.off_uinv = take((size_t)L.nblk * LNB * LNB * sizeof(float));
+  // chain tiles of the triangular solves: Ml_t = Linv_t L(t, t-1), Mu_t = Uinv_t U(t, t+1)
+  L.off_ml = take((size_t)L.nblk * LNB * LNB * sizeof(float));
+  L.off_mu = take((size_t)L.nblk * LNB * LNB * sizeof(float));
   L.off_d = take((size_t)std::max(1LL, n) * sizeof(float));
   L.off_meta = take(sizeof(LUMeta));
   L.total = off;
@@ -549,17 +552,49 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
   return v;
 }
 
+// Outputs of the triangular solves start as this bit pattern (a NaN that
+// GPU arithmetic never produces: generated NaNs are 0x7fffffff); a consumer
+// polls the values themselves instead of a separate ready flag.
+constexpr unsigned TRSV_EMPTY = 0xffffffffu;
+
+__device__ __forceinline__ float ld_relaxed_f(const float* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return __uint_as_float(v);
+}
+__device__ __forceinline__ void st_relaxed_f(float* p, float x) {
+  asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(__float_as_uint(x)) : "memory");
+}
+// Spin until out[i] holds a value; false when the limit ran out.
+__device__ __forceinline__ bool wait_value(const float* p, float& v) {
+  for (long long it = 0; it < SPIN_LIMIT; ++it) {
+    v = ld_relaxed_f(p);
+    if (__float_as_uint(v) != TRSV_EMPTY) return true;
+    if (it > 256) __nanosleep(32);
+  }
+  return false;
+}
+
+// Blocked triangular solve, one CTA per 128-row block, blocks taken in
+// dependency order through a ticket.  Block t needs x_j for all j before it
+// (after it, for the upper solve).  The last of them, x_{t-1}, is the chain:
+//   x_t = Dinv_t (b_t - sum_{j<t-1} L_tj x_j) - M_t x_{t-1},  M_t = Dinv_t L_{t,t-1}
+// The first part (every earlier tile, the reduction and the 128-long
+// diagonal-block product) is formed while block t-1 is still being solved;
+// once x_{t-1} arrives, one 128 x 128 product with M_t (held in registers,
+// two threads per row) finishes the block.  Values are published by relaxed
+// stores and consumed by polling them (TRSV_EMPTY marks "not yet").
 template <typename F, bool LOWER>
 __global__ void __launch_bounds__(256)
-k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, long long n, int nblk,
-       const float* __restrict__ rhs, const float* __restrict__ dsc, float* out, int* flags, int* ticket, int* err,
-       const int* skip) {
+k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, const float* __restrict__ Mt,
+       long long n, int nblk, const float* __restrict__ rhs, const float* __restrict__ dsc, float* out, int* ticket,
+       int* err, const int* skip) {
   extern __shared__ float sDi[];      // 128 x 128 diagonal-block inverse (column-major)
   __shared__ int s_t;
   __shared__ int s_abort;
   __shared__ float s_x[2][LNB];
   __shared__ float s_part[16][LNB + 1];
-  __shared__ float s_a[LNB];
+  __shared__ float s_y[LNB];
   if (skip != nullptr && *skip) return;
   const int tid = threadIdx.x;
   if (tid == 0) {
@@ -572,6 +607,15 @@ k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, 
   const int t = LOWER ? tk : (nblk - 1 - tk);
   const long long r0 = (long long)t * LNB;
   const int rows = (int)min((long long)LNB, n - r0);
+  const int cnt = LOWER ? t : (nblk - 1 - t);
+  // chain tile M_t: thread (row = tid / 2, half = tid % 2) holds M_t(row, 64 half .. 64 half + 63)
+  const int mrow = tid >> 1, mhalf = tid & 1;
+  float m[64];
+  if (cnt > 0) {
+    const float* M = Mt + (long long)t * LNB * LNB;
+#pragma unroll
+    for (int c = 0; c < 64; ++c) m[c] = __ldg(M + (long long)(mhalf * 64 + c) * LNB + mrow);
+  }
   const float* Di = Dinv + (long long)t * LNB * LNB;
   for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) sDi[idx] = __ldg(Di + idx);
   const int rg = tid % 16, cg = tid / 16;
@@ -579,25 +623,20 @@ k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, 
   float acc[8];
 #pragma unroll
   for (int v = 0; v < 8; ++v) acc[v] = 0.f;
-  const int cnt = LOWER ? t : (nblk - 1 - t);
-  for (int q = 0; q < cnt; ++q) {
+  // every tile except the chain tile
+  for (int q = 0; q + 1 < cnt; ++q) {
     const int j = LOWER ? q : (nblk - 1 - q);
     const long long c0 = (long long)j * LNB;
     const int cols = (int)min((long long)LNB, n - c0);
     TileRegs<F> T;
     tile_load<F>(T, LU, ldf, c0, cols, rbase, n, cg);
     if (tid < LNB) {
-      bool ok = true;
-      long long it = 0;
-      while (ld_acquire(flags + j) == 0) {
-        if (++it > SPIN_LIMIT) { ok = false; break; }
-        if (it > 256) __nanosleep(32);
-      }
-      if (!ok) {
+      float v = 0.f;
+      if (tid < cols && !wait_value(out + c0 + tid, v)) {
         s_abort = 1;
         atomicExch(err, 2);
       }
-      s_x[q & 1][tid] = (tid < cols) ? __ldcg(out + c0 + tid) : 0.f;
+      s_x[q & 1][tid] = v;
     }
     __syncthreads();
     if (s_abort) return;
@@ -612,25 +651,90 @@ k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, 
     for (int g = 0; g < 16; ++g) sum += s_part[g][tid];
     float r = 0.f;
     if (tid < rows) r = LOWER ? rhs[r0 + tid] * dsc[r0 + tid] : rhs[r0 + tid];
-    s_a[tid] = r - sum;
+    s_x[0][tid] = r - sum;  // a_t
   }
   __syncthreads();
   if (tid < LNB) {
     float y = 0.f;
     if (LOWER) {
 #pragma unroll 8
-      for (int c = 0; c < LNB; ++c) if (c <= tid) y = fmaf(sDi[c * LNB + tid], s_a[c], y);
+      for (int c = 0; c < LNB; ++c) if (c <= tid) y = fmaf(sDi[c * LNB + tid], s_x[0][c], y);
     } else {
 #pragma unroll 8
-      for (int c = 0; c < LNB; ++c) if (c >= tid) y = fmaf(sDi[c * LNB + tid], s_a[c], y);
+      for (int c = 0; c < LNB; ++c) if (c >= tid) y = fmaf(sDi[c * LNB + tid], s_x[0][c], y);
     }
-    if (tid < rows) out[r0 + tid] = y;
+    s_y[tid] = y;
   }
-  __threadfence();
+  if (cnt == 0) {
+    if (tid < rows) st_relaxed_f(out + r0 + tid, s_y[tid]);
+    return;
+  }
+  // the chain: x_prev = x_{t-1} (x_{t+1} for the upper solve)
+  const int jp = LOWER ? t - 1 : t + 1;
+  const long long cp = (long long)jp * LNB;
+  const int colsp = (int)min((long long)LNB, n - cp);
+  if (tid < LNB) {
+    float v = 0.f;
+    if (tid < colsp && !wait_value(out + cp + tid, v)) {
+      s_abort = 1;
+      atomicExch(err, 2);
+    }
+    s_x[1][tid] = v;
+  }
   __syncthreads();
-  if (tid == 0) {
-    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(flags + t), "r"(1) : "memory");
+  if (s_abort) return;
+  float z = 0.f;
+#pragma unroll
+  for (int c = 0; c < 64; ++c) z = fmaf(m[c], s_x[1][mhalf * 64 + c], z);
+  z += __shfl_xor_sync(0xffffffffu, z, 1);
+  if (mhalf == 0 && mrow < rows) st_relaxed_f(out + r0 + mrow, s_y[mrow] - z);
+}
+
+// Chain tiles of the triangular solves (one CTA per (block, triangle)):
+//   Ml_t = Linv_t L(t, t-1)   (t >= 1),   Mu_t = Uinv_t U(t, t+1)   (t < nblk - 1),
+// from the stored factors, so the solves multiply by exactly these values.
+template <typename F>
+__global__ void __launch_bounds__(256)
+k_trsv_chain_tiles(const F* __restrict__ LU, long long ldf, const float* __restrict__ Linv,
+                   const float* __restrict__ Uinv, float* __restrict__ Ml, float* __restrict__ Mu, long long n,
+                   int nblk) {
+  extern __shared__ float sm[];
+  float* sI = sm;                   // inverse, column-major [c * 128 + r]
+  float* sT = sm + LNB * LNB;       // factor tile, column-major
+  const int t = blockIdx.x, upper = blockIdx.y;
+  if (upper ? t >= nblk - 1 : t == 0) return;
+  const int tt = upper ? t + 1 : t - 1;  // column block of the off-diagonal tile
+  const long long r0 = (long long)t * LNB, c0 = (long long)tt * LNB;
+  const float* I = (upper ? Uinv : Linv) + (long long)t * LNB * LNB;
+  for (int e = threadIdx.x; e < LNB * LNB; e += blockDim.x) {
+    sI[e] = I[e];
+    const int r = e % LNB, c = e / LNB;
+    sT[e] = (r0 + r < n && c0 + c < n) ? to_f32<F>(LU[(r0 + r) + (c0 + c) * ldf]) : 0.f;
   }
+  __syncthreads();
+  // out(r, c) = sum_k I(r, k) T(k, c); thread: 8 rows x 8 columns
+  const int tr = threadIdx.x % 16, tc = threadIdx.x / 16;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  for (int k = 0; k < LNB; ++k) {
+    float a[8], b[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = sI[k * LNB + tr * 8 + i];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) b[j] = sT[(tc * 8 + j) * LNB + k];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+  }
+  float* M = (upper ? Mu : Ml) + (long long)t * LNB * LNB;
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) M[(tc * 8 + j) * LNB + tr * 8 + i] = acc[i][j];
 }
 
 __global__ void k_scale_out(const float* __restrict__ z, const float* __restrict__ d, float* __restrict__ out,
@@ -733,9 +837,11 @@ k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ 
     }
     if (row < rows) out[(long long)k * ld + r0 + row] = y;
   }
-  __threadfence();
+  // publish: the barrier orders every thread's stores of this block before
+  // thread 0's GPU-scope fence, which (cumulative) orders them before the flag
   __syncthreads();
   if (tid == 0) {
+    __threadfence();
     asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(flags + t), "r"(1) : "memory");
   }
 }
@@ -786,12 +892,15 @@ static int lu_apply_t(const void* fbuf, long long n, int fdtype, const float* v,
   const float* Linv = (const float*)(fb + L.off_linv);
   const float* Uinv = (const float*)(fb + L.off_uinv);
   const float* d = (const float*)(fb + L.off_d);
+  const float* Ml = (const float*)(fb + L.off_ml);
+  const float* Mu = (const float*)(fb + L.off_mu);
   float* y = (float*)(wb + aw.off_y);
   float* zz = (float*)(wb + aw.off_z);
-  int* flags = (int*)(wb + aw.off_flags);
   int* tk = (int*)(wb + aw.off_tk);
   int* err = (int*)(wb + aw.off_err);
-  MPDOK_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 2 * L.nblk, s));
+  // outputs start empty (TRSV_EMPTY in every word): the solves poll them
+  MPDOK_CUDA_TRY(cudaMemsetAsync(y, 0xff, sizeof(float) * n, s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(zz, 0xff, sizeof(float) * n, s));
   MPDOK_CUDA_TRY(cudaMemsetAsync(tk, 0, sizeof(int) * 2, s));
   const int slot = prof_start(MPDOK_PROF_TRSV, s);
   const size_t smem = (size_t)LNB * LNB * sizeof(float);
@@ -801,9 +910,9 @@ static int lu_apply_t(const void* fbuf, long long n, int fdtype, const float* v,
     MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv<F, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  launch(k_trsv<F, true>, L.nblk, 256, smem, s, LU, L.ldf, Linv, n, L.nblk, v, d, y, flags, tk, err, skip);
-  launch(k_trsv<F, false>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, n, L.nblk, (const float*)y, d, zz,
-         flags + L.nblk, tk + 1, err, skip);
+  launch(k_trsv<F, true>, L.nblk, 256, smem, s, LU, L.ldf, Linv, Ml, n, L.nblk, v, d, y, tk, err, skip);
+  launch(k_trsv<F, false>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, Mu, n, L.nblk, (const float*)y, d, zz, tk + 1,
+         err, skip);
   launch(k_scale_out, grid_for(n), 256, 0, s, (const float*)zz, d, z, n, skip);
   prof_stop(slot, s, (double)n * (double)n * sizeof(F), skip);
   MPDOK_LAUNCH_CHECK("lu apply");
@@ -992,6 +1101,18 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     cleanup();
   }
   if (bst < 0) return bst;
+  {
+    const size_t smem_ct = 2 * (size_t)LNB * LNB * sizeof(float);
+    static bool attr_ct = false;
+    if (!attr_ct) {
+      MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv_chain_tiles<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem_ct));
+      attr_ct = true;
+    }
+    launch(k_trsv_chain_tiles<F>, dim3(L.nblk, 2), 256, smem_ct, s, (const F*)LU, L.ldf, (const float*)Linv,
+           (const float*)Uinv, (float*)(fb + L.off_ml), (float*)(fb + L.off_mu), n, L.nblk);
+    MPDOK_LAUNCH_CHECK("lu chain tiles");
+  }
   int herr[2] = {0, 0};
   MPDOK_CUDA_TRY(cudaMemcpyAsync(herr, errw, sizeof(herr), cudaMemcpyDeviceToHost, s));
   MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
