@@ -745,20 +745,22 @@ __global__ void k_scale_out(const float* __restrict__ z, const float* __restrict
 }
 
 // Triangular solve with K right-hand sides (columns of rhs / out, leading
-// dimension ld), the chained block sweep of k_trsv: each 128 x 128 factor
-// tile is loaded once into registers and applied to all K columns, so the
-// factor bytes per right-hand side drop by K.
+// dimension ld), the chained block sweep of k_trsv: each factor tile is
+// loaded once into registers and applied to all K columns, so the factor
+// bytes per right-hand side drop by K; the chain tile M_t (registers) and the
+// value polling are those of k_trsv.
 template <typename F, bool LOWER, int K>
 __global__ void __launch_bounds__(256)
-k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, long long n, int nblk,
-             const float* __restrict__ rhs, long long ld, const float* __restrict__ dsc, float* out, int* flags,
-             int* ticket, int* err) {
+k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, const float* __restrict__ Mt,
+             long long n, int nblk, const float* __restrict__ rhs, long long ld, const float* __restrict__ dsc,
+             float* out, int* ticket, int* err) {
   extern __shared__ float sDi[];      // 128 x 128 diagonal-block inverse (column-major)
   __shared__ int s_t;
   __shared__ int s_abort;
   __shared__ float s_x[2][K][LNB];
   __shared__ float s_part[16][LNB + 1];
   __shared__ float s_a[K][LNB];
+  __shared__ float s_y[K][LNB];
   const int tid = threadIdx.x;
   if (tid == 0) {
     s_t = atomicAdd(ticket, 1);
@@ -770,6 +772,7 @@ k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ 
   const int t = LOWER ? tk : (nblk - 1 - tk);
   const long long r0 = (long long)t * LNB;
   const int rows = (int)min((long long)LNB, n - r0);
+  const int cnt = LOWER ? t : (nblk - 1 - t);
   const float* Di = Dinv + (long long)t * LNB * LNB;
   for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) sDi[idx] = __ldg(Di + idx);
   const int rg = tid % 16, cg = tid / 16;
@@ -779,26 +782,22 @@ k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ 
   for (int k = 0; k < K; ++k)
 #pragma unroll
     for (int v = 0; v < 8; ++v) acc[k][v] = 0.f;
-  const int cnt = LOWER ? t : (nblk - 1 - t);
-  for (int q = 0; q < cnt; ++q) {
+  for (int q = 0; q + 1 < cnt; ++q) {
     const int j = LOWER ? q : (nblk - 1 - q);
     const long long c0 = (long long)j * LNB;
     const int cols = (int)min((long long)LNB, n - c0);
     TileRegs<F> T;
     tile_load<F>(T, LU, ldf, c0, cols, rbase, n, cg);
     if (tid < LNB) {
-      bool ok = true;
-      long long it = 0;
-      while (ld_acquire(flags + j) == 0) {
-        if (++it > SPIN_LIMIT) { ok = false; break; }
-        if (it > 256) __nanosleep(32);
-      }
-      if (!ok) {
-        s_abort = 1;
-        atomicExch(err, 2);
-      }
 #pragma unroll
-      for (int k = 0; k < K; ++k) s_x[q & 1][k][tid] = (tid < cols) ? __ldcg(out + (long long)k * ld + c0 + tid) : 0.f;
+      for (int k = 0; k < K; ++k) {
+        float v = 0.f;
+        if (tid < cols && !wait_value(out + (long long)k * ld + c0 + tid, v)) {
+          s_abort = 1;
+          atomicExch(err, 2);
+        }
+        s_x[q & 1][k][tid] = v;
+      }
     }
     __syncthreads();
     if (s_abort) return;
@@ -824,7 +823,6 @@ k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ 
     }
   }
   __syncthreads();
-  // y = Dinv a for every column: thread (row, column group)
   for (int e = tid; e < LNB * K; e += blockDim.x) {
     const int row = e % LNB, k = e / LNB;
     float y = 0.f;
@@ -835,14 +833,48 @@ k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ 
 #pragma unroll 8
       for (int c = 0; c < LNB; ++c) if (c >= row) y = fmaf(sDi[c * LNB + row], s_a[k][c], y);
     }
-    if (row < rows) out[(long long)k * ld + r0 + row] = y;
+    s_y[k][row] = y;
   }
-  // publish: the barrier orders every thread's stores of this block before
-  // thread 0's GPU-scope fence, which (cumulative) orders them before the flag
   __syncthreads();
-  if (tid == 0) {
-    __threadfence();
-    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(flags + t), "r"(1) : "memory");
+  if (cnt == 0) {
+    for (int e = tid; e < LNB * K; e += blockDim.x) {
+      const int row = e % LNB, k = e / LNB;
+      if (row < rows) st_relaxed_f(out + (long long)k * ld + r0 + row, s_y[k][row]);
+    }
+    return;
+  }
+  // chain tile into registers now that the tile registers and accumulators are
+  // dead (still before the predecessor's values can arrive)
+  const int mrow = tid >> 1, mhalf = tid & 1;
+  float m[64];
+  {
+    const float* M = Mt + (long long)t * LNB * LNB;
+#pragma unroll
+    for (int c = 0; c < 64; ++c) m[c] = __ldg(M + (long long)(mhalf * 64 + c) * LNB + mrow);
+  }
+  const int jp = LOWER ? t - 1 : t + 1;
+  const long long cp = (long long)jp * LNB;
+  const int colsp = (int)min((long long)LNB, n - cp);
+  if (tid < LNB) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      float v = 0.f;
+      if (tid < colsp && !wait_value(out + (long long)k * ld + cp + tid, v)) {
+        s_abort = 1;
+        atomicExch(err, 2);
+      }
+      s_x[1][k][tid] = v;
+    }
+  }
+  __syncthreads();
+  if (s_abort) return;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float z = 0.f;
+#pragma unroll
+    for (int c = 0; c < 64; ++c) z = fmaf(m[c], s_x[1][k][mhalf * 64 + c], z);
+    z += __shfl_xor_sync(0xffffffffu, z, 1);
+    if (mhalf == 0 && mrow < rows) st_relaxed_f(out + (long long)k * ld + r0 + mrow, s_y[k][mrow] - z);
   }
 }
 
@@ -864,17 +896,15 @@ static unsigned grid_for(long long n, int per = 256) {
 }
 
 struct ApplyWork {
-  size_t off_y = 0, off_z = 0, off_flags = 0, off_tk = 0, off_err = 0, total = 0;
+  size_t off_y = 0, off_z = 0, off_tk = 0, off_err = 0, total = 0;
 };
 
 static ApplyWork apply_layout(long long n) {
   ApplyWork a;
-  const int nblk = (int)((n + LNB - 1) / LNB);
   size_t off = 0;
   auto take = [&](size_t b) { size_t o = off; off = align_up(off + b, 256); return o; };
   a.off_y = take((size_t)std::max(1LL, n) * sizeof(float));
   a.off_z = take((size_t)std::max(1LL, n) * sizeof(float));
-  a.off_flags = take((size_t)2 * std::max(1, nblk) * sizeof(int));
   a.off_tk = take(4 * sizeof(int));
   a.off_err = take(16);
   a.total = off;
@@ -1292,20 +1322,18 @@ extern "C" int mpdok_lu_ir_solve(const double* A, long long lda, long long n, co
 
 // ---------------------------------------------------- multi-RHS LU-IR
 struct MultiWork {
-  size_t off_y = 0, off_z = 0, off_v = 0, off_flags = 0, off_tk = 0, off_err = 0, off_r = 0, off_nrm = 0,
+  size_t off_y = 0, off_z = 0, off_v = 0, off_tk = 0, off_err = 0, off_r = 0, off_nrm = 0,
          off_g = 0, total = 0;
 };
 
 static MultiWork multi_layout(long long n, int K) {
   MultiWork m;
-  const int nblk = (int)((n + LNB - 1) / LNB);
   size_t off = 0;
   auto take = [&](size_t b) { size_t o = off; off = align_up(off + b, 256); return o; };
   const size_t nv = (size_t)std::max(1LL, n) * K;
   m.off_y = take(nv * sizeof(float));
   m.off_z = take(nv * sizeof(float));
   m.off_v = take(nv * sizeof(float));
-  m.off_flags = take((size_t)2 * std::max(1, nblk) * sizeof(int));
   m.off_tk = take(4 * sizeof(int));
   m.off_err = take(16);
   m.off_r = take(nv * sizeof(double));
@@ -1326,12 +1354,14 @@ static int lu_apply_multi_t(const void* fbuf, long long n, int fdtype, const flo
   const float* Linv = (const float*)(fb + L.off_linv);
   const float* Uinv = (const float*)(fb + L.off_uinv);
   const float* d = (const float*)(fb + L.off_d);
+  const float* Ml = (const float*)(fb + L.off_ml);
+  const float* Mu = (const float*)(fb + L.off_mu);
   float* y = (float*)(wb + mw.off_y);
   float* zz = (float*)(wb + mw.off_z);
-  int* flags = (int*)(wb + mw.off_flags);
   int* tk = (int*)(wb + mw.off_tk);
   int* err = (int*)(wb + mw.off_err);
-  MPDOK_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 2 * L.nblk, s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(y, 0xff, sizeof(float) * n * K, s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(zz, 0xff, sizeof(float) * n * K, s));
   MPDOK_CUDA_TRY(cudaMemsetAsync(tk, 0, sizeof(int) * 2, s));
   const size_t smem = (size_t)LNB * LNB * sizeof(float);
   static bool attr = false;
@@ -1341,9 +1371,9 @@ static int lu_apply_multi_t(const void* fbuf, long long n, int fdtype, const flo
     attr = true;
   }
   const int slot = prof_start(MPDOK_PROF_TRSV, s);
-  launch(k_trsv_multi<F, true, K>, L.nblk, 256, smem, s, LU, L.ldf, Linv, n, L.nblk, v, n, d, y, flags, tk, err);
-  launch(k_trsv_multi<F, false, K>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, n, L.nblk, (const float*)y, n, d, zz,
-         flags + L.nblk, tk + 1, err);
+  launch(k_trsv_multi<F, true, K>, L.nblk, 256, smem, s, LU, L.ldf, Linv, Ml, n, L.nblk, v, n, d, y, tk, err);
+  launch(k_trsv_multi<F, false, K>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, Mu, n, L.nblk, (const float*)y, n, d, zz,
+         tk + 1, err);
   launch(k_scale_out_multi, grid_for(n * K), 256, 0, s, (const float*)zz, d, z, n, n, K);
   prof_stop(slot, s, (double)n * (double)n * sizeof(F));
   MPDOK_LAUNCH_CHECK("lu apply multi");
