@@ -113,49 +113,94 @@ __global__ void k_scaled_copy(const double* __restrict__ A, long long lda, long 
 // the unit-lower and upper triangles), Tmp (products of the doubling steps).
 constexpr int DP = LNB + 1;
 constexpr size_t DIAG_SMEM = (size_t)(3 * LNB * DP + 64 * 65) * sizeof(float);
+constexpr int DIAG_THREADS = 1024;
 
 // One doubling step of the triangular inverses for diagonal blocks of size
-// SZ (a compile-time power of two, so the index arithmetic is shifts):
+// SZ (a compile-time power of two):
 //   lower  X21 = -X22 (L21 X11),   upper  X12 = -X11 (U12 X22).
+// Each of the 1024 threads forms U = PER / 1024 outputs at once with
+// independent accumulators.  For SZ = 64 the four outputs of a thread share
+// their column c, so the column operand is loaded once for four FMAs; the
+// triangular operands are zero outside their triangle, so the k ranges run to
+// the widest of the four rows.
 template <int SZ>
 __device__ __forceinline__ void inverse_doubling(const float* T, float* XL, float* XU, float* Tmp) {
   constexpr int NP = LNB / (2 * SZ);
   constexpr int PER = NP * SZ * SZ;
+  constexpr int U = PER / DIAG_THREADS;  // outputs per thread: 2 (SZ 32) or 4 (SZ 64)
+  static_assert(PER % DIAG_THREADS == 0, "doubling step must split evenly");
   const int tid = threadIdx.x;
-  for (int idx = tid; idx < PER; idx += blockDim.x) {
-    const int pr = idx / (SZ * SZ), e = idx % (SZ * SZ), r = e / SZ, c = e % SZ;
-    const int R = (2 * pr + 1) * SZ, C = 2 * pr * SZ;
-    float a = 0.f;
-#pragma unroll 8
-    for (int k = c; k < SZ; ++k) a = fmaf(T[(R + r) * DP + C + k], XL[(C + k) * DP + C + c], a);
-    Tmp[(pr * SZ + r) * 65 + c] = a;
+  int pr[U], r[U];
+  const int c = tid % SZ;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int idx = tid + u * DIAG_THREADS;
+    pr[u] = idx / (SZ * SZ);
+    r[u] = (idx % (SZ * SZ)) / SZ;
+  }
+  float a[U];
+  // lower: Tmp = L21 X11, k in [c, SZ)
+#pragma unroll
+  for (int u = 0; u < U; ++u) a[u] = 0.f;
+  for (int k = c; k < SZ; ++k) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int R = (2 * pr[u] + 1) * SZ, C = 2 * pr[u] * SZ;
+      a[u] = fmaf(T[(R + r[u]) * DP + C + k], XL[(C + k) * DP + C + c], a[u]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) Tmp[(pr[u] * SZ + r[u]) * 65 + c] = a[u];
+  __syncthreads();
+  // lower: X21 = -X22 Tmp, k in [0, r] (X22 lower triangular)
+  int rmax = 0, rmin = SZ;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    rmax = max(rmax, r[u]);
+    rmin = min(rmin, r[u]);
+    a[u] = 0.f;
+  }
+  for (int k = 0; k <= rmax; ++k) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int R = (2 * pr[u] + 1) * SZ;
+      a[u] = fmaf(XL[(R + r[u]) * DP + R + k], Tmp[(pr[u] * SZ + k) * 65 + c], a[u]);
+    }
   }
   __syncthreads();
-  for (int idx = tid; idx < PER; idx += blockDim.x) {
-    const int pr = idx / (SZ * SZ), e = idx % (SZ * SZ), r = e / SZ, c = e % SZ;
-    const int R = (2 * pr + 1) * SZ, C = 2 * pr * SZ;
-    float a = 0.f;
-#pragma unroll 8
-    for (int k = 0; k <= r; ++k) a = fmaf(XL[(R + r) * DP + R + k], Tmp[(pr * SZ + k) * 65 + c], a);
-    XL[(R + r) * DP + C + c] = -a;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int R = (2 * pr[u] + 1) * SZ, C = 2 * pr[u] * SZ;
+    XL[(R + r[u]) * DP + C + c] = -a[u];
+  }
+  // upper: Tmp = U12 X22, k in [0, c]
+#pragma unroll
+  for (int u = 0; u < U; ++u) a[u] = 0.f;
+  for (int k = 0; k <= c; ++k) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int R = 2 * pr[u] * SZ, C = (2 * pr[u] + 1) * SZ;
+      a[u] = fmaf(T[(R + r[u]) * DP + C + k], XU[(C + k) * DP + C + c], a[u]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) Tmp[(pr[u] * SZ + r[u]) * 65 + c] = a[u];
+  __syncthreads();
+  // upper: X12 = -X11 Tmp, k in [r, SZ) (X11 upper triangular)
+#pragma unroll
+  for (int u = 0; u < U; ++u) a[u] = 0.f;
+  for (int k = rmin; k < SZ; ++k) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int R = 2 * pr[u] * SZ;
+      a[u] = fmaf(XU[(R + r[u]) * DP + R + k], Tmp[(pr[u] * SZ + k) * 65 + c], a[u]);
+    }
   }
   __syncthreads();
-  for (int idx = tid; idx < PER; idx += blockDim.x) {
-    const int pr = idx / (SZ * SZ), e = idx % (SZ * SZ), r = e / SZ, c = e % SZ;
-    const int R = 2 * pr * SZ, C = (2 * pr + 1) * SZ;
-    float a = 0.f;
-#pragma unroll 8
-    for (int k = 0; k <= c; ++k) a = fmaf(T[(R + r) * DP + C + k], XU[(C + k) * DP + C + c], a);
-    Tmp[(pr * SZ + r) * 65 + c] = a;
-  }
-  __syncthreads();
-  for (int idx = tid; idx < PER; idx += blockDim.x) {
-    const int pr = idx / (SZ * SZ), e = idx % (SZ * SZ), r = e / SZ, c = e % SZ;
-    const int R = 2 * pr * SZ, C = (2 * pr + 1) * SZ;
-    float a = 0.f;
-#pragma unroll 8
-    for (int k = r; k < SZ; ++k) a = fmaf(XU[(R + r) * DP + R + k], Tmp[(pr * SZ + k) * 65 + c], a);
-    XU[(R + r) * DP + C + c] = -a;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int R = 2 * pr[u] * SZ, C = (2 * pr[u] + 1) * SZ;
+    XU[(R + r[u]) * DP + C + c] = -a[u];
   }
   __syncthreads();
 }
@@ -195,7 +240,6 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
   inverse_doubling<64>(T, XL, XU, Tmp);
 }
 
-constexpr int DIAG_THREADS = 1024;
 
 // Blocked LU of the 128 x 128 diagonal block in four 32-column sub-panels.
 // The kernel is issue-bound on its single SM, so the work is arranged for
@@ -277,14 +321,34 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
       for (int i = 1; i < 32; ++i) T[(c0 + i) * DP + c] = u[i];
     }
     __syncthreads();
-    // ---- C: A22 -= L21 U12 over rows and columns [c1, 128), K = 32
+    // ---- C: A22 -= L21 U12 over rows and columns [c1, 128), K = 32.  Thread
+    // (row group g, column c) forms rows c1 + g, c1 + g + G, ...: the column
+    // operand U12(k, c) is loaded once per k for all of them.
     const int m = LNB - c1;
-    for (int e = tid; e < m * m; e += blockDim.x) {
-      const int i = c1 + e / m, c = c1 + e % m;
-      float acc = T[i * DP + c];
+    const int G = DIAG_THREADS / m;  // row groups: 10, 16 or 32
+    if (tid < G * m) {
+      const int c = c1 + tid % m, g = tid / m;
+      constexpr int RMAX = 10;       // ceil(96 / 10)
+      float acc[RMAX];
 #pragma unroll
-      for (int k = 0; k < 32; ++k) acc = fmaf(-T[i * DP + c0 + k], T[(c0 + k) * DP + c], acc);
-      T[i * DP + c] = acc;
+      for (int s2 = 0; s2 < RMAX; ++s2) {
+        const int i = c1 + g + s2 * G;
+        acc[s2] = (i < LNB) ? T[i * DP + c] : 0.f;
+      }
+#pragma unroll 4
+      for (int k = 0; k < 32; ++k) {
+        const float b = T[(c0 + k) * DP + c];
+#pragma unroll
+        for (int s2 = 0; s2 < RMAX; ++s2) {
+          const int i = c1 + g + s2 * G;
+          if (i < LNB) acc[s2] = fmaf(-T[i * DP + c0 + k], b, acc[s2]);
+        }
+      }
+#pragma unroll
+      for (int s2 = 0; s2 < RMAX; ++s2) {
+        const int i = c1 + g + s2 * G;
+        if (i < LNB) T[i * DP + c] = acc[s2];
+      }
     }
     __syncthreads();
   }
