@@ -321,34 +321,14 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
       for (int i = 1; i < 32; ++i) T[(c0 + i) * DP + c] = u[i];
     }
     __syncthreads();
-    // ---- C: A22 -= L21 U12 over rows and columns [c1, 128), K = 32.  Thread
-    // (row group g, column c) forms rows c1 + g, c1 + g + G, ...: the column
-    // operand U12(k, c) is loaded once per k for all of them.
+    // ---- C: A22 -= L21 U12 over rows and columns [c1, 128), K = 32
     const int m = LNB - c1;
-    const int G = DIAG_THREADS / m;  // row groups: 10, 16 or 32
-    if (tid < G * m) {
-      const int c = c1 + tid % m, g = tid / m;
-      constexpr int RMAX = 10;       // ceil(96 / 10)
-      float acc[RMAX];
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      const int i = c1 + e / m, c = c1 + e % m;
+      float acc = T[i * DP + c];
 #pragma unroll
-      for (int s2 = 0; s2 < RMAX; ++s2) {
-        const int i = c1 + g + s2 * G;
-        acc[s2] = (i < LNB) ? T[i * DP + c] : 0.f;
-      }
-#pragma unroll 4
-      for (int k = 0; k < 32; ++k) {
-        const float b = T[(c0 + k) * DP + c];
-#pragma unroll
-        for (int s2 = 0; s2 < RMAX; ++s2) {
-          const int i = c1 + g + s2 * G;
-          if (i < LNB) acc[s2] = fmaf(-T[i * DP + c0 + k], b, acc[s2]);
-        }
-      }
-#pragma unroll
-      for (int s2 = 0; s2 < RMAX; ++s2) {
-        const int i = c1 + g + s2 * G;
-        if (i < LNB) T[i * DP + c] = acc[s2];
-      }
+      for (int k = 0; k < 32; ++k) acc = fmaf(-T[i * DP + c0 + k], T[(c0 + k) * DP + c], acc);
+      T[i * DP + c] = acc;
     }
     __syncthreads();
   }
