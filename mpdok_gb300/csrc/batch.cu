@@ -64,7 +64,7 @@ struct BatchPlan {
   std::vector<long long> preT, preS;  // per level: prefix sums (act[k] + 1 entries each)
   std::vector<long long> preT_off, preS_off;
   std::vector<long long> preRow;      // prefix of nblk over all systems (row-tile tasks)
-  long long total_rows = 0, total_x = 0, total_c = 0;
+  long long total_x = 0, total_c = 0;
   BSys* d_sys = nullptr;
   long long* d_pre = nullptr;         // preT | preS | preRow
   long long d_preS_base = 0, d_preRow_base = 0;
