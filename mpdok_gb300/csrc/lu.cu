@@ -32,7 +32,7 @@
 namespace mpdok {
 
 constexpr int LNB = 128;          // panel width / TRSV block
-constexpr int SPW = 512;          // super-panel width: K of the far trailing update
+constexpr int SPW = 1024;         // super-panel width: K of the far trailing update
 constexpr long long SPIN_LIMIT = 1LL << 24;
 
 static int fsize(int fdtype) { return fdtype == MPDOK_F32 ? 4 : 2; }
@@ -114,6 +114,24 @@ __global__ void k_scaled_copy(const double* __restrict__ A, long long lda, long 
 constexpr int DP = LNB + 1;
 constexpr size_t DIAG_SMEM = (size_t)(3 * LNB * DP + 64 * 65) * sizeof(float);
 constexpr int DIAG_THREADS = 1024;
+constexpr int TRSM_THREADS = 256;
+
+// Copy TOTAL elements, element e = tid + u * THREADS, from global memory into
+// shared memory: ld(e) reads one, st(e, v) stores it.  The strides are
+// compile-time, so BATCH loads per thread are in flight before their shared
+// stores and a tile costs TOTAL / (THREADS * BATCH) memory round trips.
+template <int TOTAL, int THREADS, int BATCH, typename Ld, typename St>
+__device__ __forceinline__ void stage_tile(int tid, Ld ld, St st) {
+  static_assert(TOTAL % (THREADS * BATCH) == 0, "tile must split into whole batches");
+#pragma unroll
+  for (int u0 = 0; u0 < TOTAL / THREADS; u0 += BATCH) {
+    float v[BATCH];
+#pragma unroll
+    for (int u = 0; u < BATCH; ++u) v[u] = ld(tid + (u0 + u) * THREADS);
+#pragma unroll
+    for (int u = 0; u < BATCH; ++u) st(tid + (u0 + u) * THREADS, v[u]);
+  }
+}
 
 // One doubling step of the triangular inverses for diagonal blocks of size
 // SZ (a compile-time power of two):
@@ -261,7 +279,7 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
   float* Tmp = sm + 3 * LNB * DP;
   __shared__ float prow[2][32];
   const int tid = threadIdx.x;
-  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
+  for (int idx = tid; idx < LNB * LNB; idx += DIAG_THREADS) {
     const int r = idx % LNB, c = idx / LNB;
     T[r * DP + c] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
   }
@@ -360,14 +378,16 @@ __device__ __forceinline__ void trsm_right_body(const float* __restrict__ W, lon
   const int tid = threadIdx.x;
   const long long r0 = r_begin + (long long)bid * 64;
   const int rows = (int)min(64LL, n - r0);
-  for (int idx = tid; idx < 64 * LNB; idx += blockDim.x) {
-    const int r = idx % 64, c = idx / 64;
-    Xs[r * XP + c] = (r < rows) ? W[(r0 + r) + (j0 + c) * ldw] : 0.f;
-  }
-  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
-    const int k = idx % LNB, c = idx / LNB;  // Uinv column-major: [c*128 + k]
-    Ts[k * TSP + c] = Uinv[c * LNB + k];
-  }
+  stage_tile<64 * LNB, TRSM_THREADS, 32>(
+      tid,
+      [&](int idx) {
+        const int r = idx % 64, c = idx / 64;
+        return (r < rows) ? W[(r0 + r) + (j0 + c) * ldw] : 0.f;
+      },
+      [&](int idx, float v) { Xs[(idx % 64) * XP + idx / 64] = v; });
+  // Uinv column-major: [c*128 + k]
+  stage_tile<LNB * LNB, TRSM_THREADS, 32>(
+      tid, [&](int idx) { return Uinv[idx]; }, [&](int idx, float v) { Ts[(idx % LNB) * TSP + idx / LNB] = v; });
   __syncthreads();
   const int ty = tid / 16, tx = tid % 16;
   float acc[4][8];
@@ -420,14 +440,16 @@ __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long
   const int tid = threadIdx.x;
   const long long c0 = c_begin + (long long)bid * 64;
   const int cols = (int)min(64LL, n - c0);
-  for (int idx = tid; idx < LNB * 64; idx += blockDim.x) {
-    const int k = idx % LNB, c = idx / LNB;
-    Xs[k * XP + c] = (c < cols) ? W[(j0 + k) + (c0 + c) * ldw] : 0.f;
-  }
-  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
-    const int r = idx % LNB, k = idx / LNB;  // Linv column-major [k*128 + r]
-    Ts[r * TP + k] = Linv[k * LNB + r];
-  }
+  stage_tile<LNB * 64, TRSM_THREADS, 32>(
+      tid,
+      [&](int idx) {
+        const int k = idx % LNB, c = idx / LNB;
+        return (c < cols) ? W[(j0 + k) + (c0 + c) * ldw] : 0.f;
+      },
+      [&](int idx, float v) { Xs[(idx % LNB) * XP + idx / LNB] = v; });
+  // Linv column-major [k*128 + r]
+  stage_tile<LNB * LNB, TRSM_THREADS, 32>(
+      tid, [&](int idx) { return Linv[idx]; }, [&](int idx, float v) { Ts[(idx % LNB) * TP + idx / LNB] = v; });
   __syncthreads();
   const int ty = tid / 16, tx = tid % 16;
   float acc[8][4];
@@ -467,7 +489,7 @@ __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long
 // L21 = W21 Uinv (64 rows each), the rest U12 = Linv W12 (64 columns each);
 // they write disjoint outputs, so they run side by side.
 template <typename F>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(TRSM_THREADS)
 k_trsm_pair(const float* __restrict__ W, long long ldw, long long j0, long long begin, long long n,
             const float* __restrict__ Uinv, const float* __restrict__ Linv, F* __restrict__ Lp, F* __restrict__ Up,
             long long pitch, long long base0, int koff, F* __restrict__ LU, long long ldf, int nb) {
@@ -1059,11 +1081,13 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     }
     return gemm_update(C, w.ldw, Ab, Bb, SPW, (int)m, (int)nn, K, fdtype, MPDOK_ENGINE_TENSOR, errw, st);
   };
-  // Two-level right-looking LU.  Super-panel [J, Jend) of <= 512 columns is
+  // Two-level right-looking LU.  Super-panel [J, Jend) of <= 1024 columns is
   // factored with 128-wide panels whose updates are confined to the
   // super-panel's row strip (rows < Jend, all columns right of the panel) and
   // column strip (rows >= Jend, columns < Jend); the far trailing matrix
-  // (rows, columns >= Jend) then receives all of them at once, K = 512.
+  // (rows, columns >= Jend) then receives all of them at once, K = 1024.
+  // (K = 1024 halves the FP32 read-modify-write of the far matrix against
+  // K = 512; at K = 2048 the longer inner strips cost more than that saves.)
   //
   // Look-ahead: super-panels are factored on a high-priority side stream.
   // The far update of super-panel J runs on the caller's stream in two parts:
@@ -1073,29 +1097,51 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   // concurrently with it.  The two touch disjoint parts of W: the inner loop
   // of J + 1 writes rows < Jn or columns < Jn only.  Operands alternate between
   // two buffers, so (b) of J still reads its own while J + 1 writes the other.
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_ready = nullptr, ev_panel = nullptr;
+  //
+  // Inside a super-panel the panels are pipelined over two more high-priority
+  // streams.  The chain stream (sa) runs, per panel p with columns
+  // [jp, r1 = jp + 128): the diagonal-block LU; the panel solve of the next
+  // panel's own block rows and columns [r1, nxt); the update of the next
+  // diagonal block [r1, nxt)^2 by panel p; then the next diagonal LU.  The
+  // strip stream (sb) runs the rest of panel p's solve (rows and columns >=
+  // nxt) and its updates outside that diagonal block:
+  //   rows [r1, nxt) x columns [nxt, n), rows [nxt, Jend) x columns [r1, n),
+  //   rows [Jend, n) x columns [r1, Jend).
+  // The chain stream waits for the strips of panel p - 1 before its solve of
+  // panel p's next block (that solve reads rows and columns the strips
+  // update), so the diagonal LU of panel p + 1 overlaps the strips of p.
+  cudaStream_t side = nullptr, strip = nullptr;
+  cudaEvent_t ev_ready = nullptr, ev_panel = nullptr, ev_a = nullptr, ev_b = nullptr;
   auto cleanup = [&]() {
     if (ev_ready) cudaEventDestroy(ev_ready);
     if (ev_panel) cudaEventDestroy(ev_panel);
+    if (ev_a) cudaEventDestroy(ev_a);
+    if (ev_b) cudaEventDestroy(ev_b);
     if (side) cudaStreamDestroy(side);
+    if (strip) cudaStreamDestroy(strip);
   };
   const bool lookahead = n > SPW;
-  if (lookahead) {
+  const bool split = n > LNB;
+  if (split) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    cudaError_t e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi);
+    cudaError_t e = cudaStreamCreateWithPriority(&strip, cudaStreamNonBlocking, hi);
+    if (e == cudaSuccess && lookahead) e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_panel, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_a, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_b, cudaEventDisableTiming);
     if (e != cudaSuccess) {
       cleanup();
-      return cuda_status(e, "lu look-ahead stream / events");
+      return cuda_status(e, "lu look-ahead streams / events");
     }
-    e = cudaEventRecord(ev_ready, s);  // scaling and the working copy are done
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev_ready, 0);
-    if (e != cudaSuccess) {
-      cleanup();
-      return cuda_status(e, "lu look-ahead start");
+    if (lookahead) {
+      e = cudaEventRecord(ev_ready, s);  // scaling and the working copy are done
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev_ready, 0);
+      if (e != cudaSuccess) {
+        cleanup();
+        return cuda_status(e, "lu look-ahead start");
+      }
     }
   }
   auto body = [&]() -> int {
@@ -1104,33 +1150,53 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
       const int buf = (int)((J / SPW) & 1);
       F* Lp = Lp2 + (size_t)buf * opsz;
       F* Up = Up2 + (size_t)buf * opsz;
-      cudaStream_t ps_stream = lookahead ? side : s;
+      cudaStream_t sa = lookahead ? side : s;
+      cudaStream_t sb = split ? strip : sa;
       for (long long jp = J; jp < Jend; jp += LNB) {
         const int k = (int)(jp / LNB);
         const int p = (int)((jp - J) / LNB);
         const int nbk = (int)std::min<long long>(LNB, n - jp);
-        const long long below = n - jp - nbk;
-        const int ps = prof_start(MPDOK_PROF_LU_PANEL, ps_stream);
-        launch(k_lu_diag<F>, 1, DIAG_THREADS, smem_diag, ps_stream, W, w.ldw, jp, nbk, LU, L.ldf,
+        const long long r1 = jp + LNB;                         // first row / column after the panel
+        const long long nxt = std::min<long long>(r1 + LNB, Jend);  // end of the next panel of J
+        const bool has_next = r1 < Jend;
+        const F* Lr = Lp + p * LNB;  // K-slot of panel p: row r of L21 at Lr + (r - J) * SPW
+        const F* Uc = Up + p * LNB;  // column c of U12 at Uc + (c - J) * SPW
+        auto solve = [&](long long begin, long long end, cudaStream_t st) {
+          const int nb = (int)((end - begin + 63) / 64);
+          launch(k_trsm_pair<F>, (unsigned)(2 * nb), TRSM_THREADS, smem_tp, st, (const float*)W, w.ldw, jp, begin,
+                 end, (const float*)(Uinv + (size_t)k * LNB * LNB), (const float*)(Linv + (size_t)k * LNB * LNB), Lp,
+                 Up, (long long)SPW, J, p * LNB, LU, L.ldf, nb);
+        };
+        // chain: diagonal LU, then the next panel's own block rows / columns
+        const int ps = prof_start(MPDOK_PROF_LU_PANEL, sa);
+        launch(k_lu_diag<F>, 1, DIAG_THREADS, smem_diag, sa, W, w.ldw, jp, nbk, LU, L.ldf,
                Linv + (size_t)k * LNB * LNB, Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
-        if (below > 0) {
-          const int nb = (int)((below + 63) / 64);
-          launch(k_trsm_pair<F>, (unsigned)(2 * nb), 256, smem_tp, ps_stream, (const float*)W, w.ldw, jp, jp + LNB, n,
-                 (const float*)(Uinv + (size_t)k * LNB * LNB), (const float*)(Linv + (size_t)k * LNB * LNB), Lp, Up,
-                 (long long)SPW, J, p * LNB, LU, L.ldf, nb);
+        if (has_next) {
+          if (split && jp > J) MPDOK_CUDA_TRY(cudaStreamWaitEvent(sa, ev_b, 0));  // strips of panel p - 1
+          solve(r1, nxt, sa);
         }
-        prof_stop(ps, ps_stream, 2.0 * 2.0 * (double)below * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
+        prof_stop(ps, sa, 2.0 * 2.0 * (double)(nxt - std::min(r1, nxt)) * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
         MPDOK_LAUNCH_CHECK("lu panel");
-        if (below > 0) {
-          const long long r1 = jp + LNB;
-          // row strip of the super-panel: rows [r1, Jend), columns [r1, n)
-          MPDOK_TRY(update(r1, r1, Jend - r1, n - r1, Lp + (r1 - J) * SPW + p * LNB,
-                           Up + (r1 - J) * SPW + p * LNB, LNB, ps_stream));
-          // column strip below the super-panel: rows [Jend, n), columns [r1, Jend)
-          MPDOK_TRY(update(Jend, r1, n - Jend, Jend - r1, Lp + (Jend - J) * SPW + p * LNB,
-                           Up + (r1 - J) * SPW + p * LNB, LNB, ps_stream));
+        if (split) MPDOK_CUDA_TRY(cudaEventRecord(ev_a, sa));
+        if (has_next)
+          MPDOK_TRY(update(r1, r1, nxt - r1, nxt - r1, Lr + (r1 - J) * SPW, Uc + (r1 - J) * SPW, LNB, sa));
+        // strips: the rest of the panel solve and of panel p's updates
+        if (split) MPDOK_CUDA_TRY(cudaStreamWaitEvent(sb, ev_a, 0));
+        const long long begin = has_next ? nxt : r1;
+        if (begin < n) {
+          const int ps2 = prof_start(MPDOK_PROF_LU_PANEL, sb);
+          solve(begin, n, sb);
+          prof_stop(ps2, sb, 2.0 * 2.0 * (double)(n - begin) * LNB * LNB);
+          MPDOK_LAUNCH_CHECK("lu panel solve");
         }
+        if (has_next) {
+          MPDOK_TRY(update(r1, nxt, nxt - r1, n - nxt, Lr + (r1 - J) * SPW, Uc + (nxt - J) * SPW, LNB, sb));
+          MPDOK_TRY(update(nxt, r1, Jend - nxt, n - r1, Lr + (nxt - J) * SPW, Uc + (r1 - J) * SPW, LNB, sb));
+          MPDOK_TRY(update(Jend, r1, n - Jend, Jend - r1, Lr + (Jend - J) * SPW, Uc + (r1 - J) * SPW, LNB, sb));
+        }
+        if (split) MPDOK_CUDA_TRY(cudaEventRecord(ev_b, sb));
       }
+      if (split) MPDOK_CUDA_TRY(cudaStreamWaitEvent(sa, ev_b, 0));  // join the strips
       if (lookahead) {
         MPDOK_CUDA_TRY(cudaEventRecord(ev_panel, side));
         MPDOK_CUDA_TRY(cudaStreamWaitEvent(s, ev_panel, 0));
@@ -1164,13 +1230,17 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     return MPDOK_OK;
   };
   const int bst = body();
-  if (lookahead) {
-    // the caller's stream owns the result: join the side stream
+  if (split) {
+    // the caller's stream owns the result: join the side streams (the strip
+    // stream was joined into the chain stream after every super-panel)
     if (bst == MPDOK_OK) {
-      cudaEventRecord(ev_panel, side);
-      cudaStreamWaitEvent(s, ev_panel, 0);
+      if (lookahead) {
+        cudaEventRecord(ev_panel, side);
+        cudaStreamWaitEvent(s, ev_panel, 0);
+      }
     } else {
-      cudaStreamSynchronize(side);
+      cudaStreamSynchronize(strip);
+      if (side) cudaStreamSynchronize(side);
     }
     cleanup();
   }
