@@ -357,6 +357,12 @@ MPDOK_API long long mpdok_profile_skipped(int kernel_class);
 /* Algorithmic bytes of a class whose work counts flops (MPDOK_PROF_LU_GEMM:
  * the FP32 C tile read and written plus the operands), for its HBM roofline. */
 MPDOK_API double mpdok_profile_bytes(int kernel_class);
+/* Timeline of every timed launch since mpdok_profile_enable, in launch order:
+ * out[4 i .. 4 i + 3] = (class, start ms, end ms, work), times relative to the
+ * first launch's start event, each on its own stream.  Writes at most
+ * max_records records (out may be NULL) and returns the number of records,
+ * or a negative MPDOK status. */
+MPDOK_API long long mpdok_profile_timeline(double* out, long long max_records);
 
 /* ------------------------------------------- reference ctypes ABI (mpdok.so)
  * mpdok_ops.py:362-373: A (N x N FP64, Fortran order), b, x (FP64, x is the

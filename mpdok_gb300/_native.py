@@ -152,6 +152,7 @@ _SIGS = {
     "mpdok_lu_ir_solve_multi": (c_int, [c_void_p, c_ll, c_ll, c_void_p, c_int, c_int, c_void_p, c_ll, c_void_p, c_ll,
                                         c_double, c_int, c_void_p, c_size_t, ctypes.POINTER(SolveInfo), c_void_p]),
     "mpdok_profile_bytes": (c_double, [c_int]),
+    "mpdok_profile_timeline": (c_ll, [ctypes.POINTER(c_double), c_ll]),
     "mpdok_batch_create": (c_int, [c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, ctypes.POINTER(c_void_p)]),
     "mpdok_batch_destroy": (c_int, [c_void_p]),
     "mpdok_batch_bytes": (c_size_t, [c_void_p]),
@@ -256,6 +257,16 @@ def profile_bytes(cls: int) -> float:
 def profile_skipped(cls: int) -> int:
     """Launches of one class that a device skip flag turned off."""
     return int(load().mpdok_profile_skipped(cls))
+
+
+def profile_timeline() -> np.ndarray:
+    """(records, 4) array of (class, start ms, end ms, work) of every timed
+    launch since profile_enable(), in launch order."""
+    lib = load()
+    n = check(int(lib.mpdok_profile_timeline(None, 0)), "profile_timeline")
+    out = np.zeros((max(n, 1), 4), dtype=np.float64)
+    check(int(lib.mpdok_profile_timeline(out.ctypes.data_as(ctypes.POINTER(c_double)), n)), "profile_timeline")
+    return out[:n]
 
 
 def launch_count() -> int:

@@ -32,7 +32,13 @@
 namespace mpdok {
 
 constexpr int LNB = 128;          // panel width / TRSV block
-constexpr int SPW = 1024;         // super-panel width: K of the far trailing update
+// Super-panel width: K of the far trailing update.  For 16-bit factors the
+// tensor-core update is HBM-bound on its FP32 C tile, and K = 1024 halves that
+// read-modify-write against K = 512 (at K = 2048 the longer inner strips cost
+// more than that saves).  The FP32 factors' CUDA-core update is compute-bound,
+// so there the narrower width, with twice the super-panels to overlap, is
+// faster.
+inline long long super_panel_width(int fdtype) { return fdtype == MPDOK_F32 ? 512 : 1024; }
 constexpr long long SPIN_LIMIT = 1LL << 24;
 
 static int fsize(int fdtype) { return fdtype == MPDOK_F32 ? 4 : 2; }
@@ -84,8 +90,8 @@ static LUWork lu_work_layout(long long n, int fdtype) {
   w.off_W = take((size_t)w.ldw * n * sizeof(float));
   // two operand buffers each: super-panel J + 1 is factored while the far
   // update of super-panel J still reads its own operands (look-ahead)
-  w.off_Lp = take(2 * (size_t)std::max(1LL, n) * SPW * fsize(fdtype));
-  w.off_Up = take(2 * (size_t)std::max(1LL, n) * SPW * fsize(fdtype));
+  w.off_Lp = take(2 * (size_t)std::max(1LL, n) * super_panel_width(fdtype) * fsize(fdtype));
+  w.off_Up = take(2 * (size_t)std::max(1LL, n) * super_panel_width(fdtype) * fsize(fdtype));
   w.off_err = take(64);
   w.total = off;
   return w;
@@ -661,6 +667,7 @@ k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, 
   __shared__ float s_x[2][LNB];
   __shared__ float s_part[16][LNB + 1];
   __shared__ float s_y[LNB];
+  __shared__ float s_rhs[LNB];
   if (skip != nullptr && *skip) return;
   const int tid = threadIdx.x;
   if (tid == 0) {
@@ -684,6 +691,9 @@ k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, 
   }
   const float* Di = Dinv + (long long)t * LNB * LNB;
   for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) sDi[idx] = __ldg(Di + idx);
+  // the block's right-hand side, staged now so that its latency stays off the
+  // path from x_{t-2} to y_t
+  if (tid < LNB) s_rhs[tid] = tid < rows ? (LOWER ? rhs[r0 + tid] * dsc[r0 + tid] : rhs[r0 + tid]) : 0.f;
   const int rg = tid % 16, cg = tid / 16;
   const long long rbase = r0 + rg * 8;
   float acc[8];
@@ -715,33 +725,36 @@ k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, 
     float sum = 0.f;
 #pragma unroll
     for (int g = 0; g < 16; ++g) sum += s_part[g][tid];
-    float r = 0.f;
-    if (tid < rows) r = LOWER ? rhs[r0 + tid] * dsc[r0 + tid] : rhs[r0 + tid];
-    s_x[0][tid] = r - sum;  // a_t
+    s_x[0][tid] = s_rhs[tid] - sum;  // a_t
   }
   __syncthreads();
+  // the chain input x_prev = x_{t-1} (x_{t+1} for the upper solve), read
+  // speculatively now: it is usually published by the time y_t is formed, and
+  // the read then overlaps the product below
+  const int jp = LOWER ? t - 1 : t + 1;
+  const long long cp = (long long)jp * LNB;
+  const int colsp = cnt > 0 ? (int)min((long long)LNB, n - cp) : 0;
+  float xs = 0.f;
+  if (tid < colsp) xs = ld_relaxed_f(out + cp + tid);
   if (tid < LNB) {
-    float y = 0.f;
-    if (LOWER) {
+    // y_t = Dinv_t a_t, four independent partial sums over the full tile
+    // (Dinv_t holds exact zeros outside its triangle, which add nothing)
+    float y[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 8
-      for (int c = 0; c < LNB; ++c) if (c <= tid) y = fmaf(sDi[c * LNB + tid], s_x[0][c], y);
-    } else {
-#pragma unroll 8
-      for (int c = 0; c < LNB; ++c) if (c >= tid) y = fmaf(sDi[c * LNB + tid], s_x[0][c], y);
+    for (int c0 = 0; c0 < LNB; c0 += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) y[u] = fmaf(sDi[(c0 + u) * LNB + tid], s_x[0][c0 + u], y[u]);
     }
-    s_y[tid] = y;
+    s_y[tid] = (y[0] + y[1]) + (y[2] + y[3]);
   }
   if (cnt == 0) {
     if (tid < rows) st_relaxed_f(out + r0 + tid, s_y[tid]);
     return;
   }
-  // the chain: x_prev = x_{t-1} (x_{t+1} for the upper solve)
-  const int jp = LOWER ? t - 1 : t + 1;
-  const long long cp = (long long)jp * LNB;
-  const int colsp = (int)min((long long)LNB, n - cp);
+  // the chain: x_t = y_t - M_t x_prev
   if (tid < LNB) {
-    float v = 0.f;
-    if (tid < colsp && !wait_value(out + cp + tid, v)) {
+    float v = xs;
+    if (tid < colsp && __float_as_uint(v) == TRSV_EMPTY && !wait_value(out + cp + tid, v)) {
       s_abort = 1;
       atomicExch(err, 2);
     }
@@ -841,6 +854,17 @@ k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ 
   const int cnt = LOWER ? t : (nblk - 1 - t);
   const float* Di = Dinv + (long long)t * LNB * LNB;
   for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) sDi[idx] = __ldg(Di + idx);
+  // the block's right-hand sides, staged now so that their latency stays off
+  // the path from x_{t-2} to y_t
+  for (int e = tid; e < LNB * K; e += blockDim.x) {
+    const int row = e % LNB, k = e / LNB;
+    float r = 0.f;
+    if (row < rows) {
+      const float b = rhs[(long long)k * ld + r0 + row];
+      r = LOWER ? b * dsc[r0 + row] : b;
+    }
+    s_a[k][row] = r;
+  }
   const int rg = tid % 16, cg = tid / 16;
   const long long rbase = r0 + rg * 8;
   float acc[K][8];
@@ -880,26 +904,20 @@ k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ 
       float sum = 0.f;
 #pragma unroll
       for (int g = 0; g < 16; ++g) sum += s_part[g][tid];
-      float r = 0.f;
-      if (tid < rows) {
-        const float b = rhs[(long long)k * ld + r0 + tid];
-        r = LOWER ? b * dsc[r0 + tid] : b;
-      }
-      s_a[k][tid] = r - sum;
+      s_a[k][tid] -= sum;
     }
   }
   __syncthreads();
   for (int e = tid; e < LNB * K; e += blockDim.x) {
     const int row = e % LNB, k = e / LNB;
-    float y = 0.f;
-    if (LOWER) {
+    // Dinv_t holds exact zeros outside its triangle, which add nothing
+    float y[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 8
-      for (int c = 0; c < LNB; ++c) if (c <= row) y = fmaf(sDi[c * LNB + row], s_a[k][c], y);
-    } else {
-#pragma unroll 8
-      for (int c = 0; c < LNB; ++c) if (c >= row) y = fmaf(sDi[c * LNB + row], s_a[k][c], y);
+    for (int c0 = 0; c0 < LNB; c0 += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) y[u] = fmaf(sDi[(c0 + u) * LNB + row], s_a[k][c0 + u], y[u]);
     }
-    s_y[k][row] = y;
+    s_y[k][row] = (y[0] + y[1]) + (y[2] + y[3]);
   }
   __syncthreads();
   if (cnt == 0) {
@@ -1040,7 +1058,8 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   float* W = (float*)(wb + w.off_W);
   F* Lp2 = (F*)(wb + w.off_Lp);
   F* Up2 = (F*)(wb + w.off_Up);
-  const size_t opsz = (size_t)std::max(1LL, n) * SPW;  // elements of one operand buffer
+  const long long spw = super_panel_width(fdtype);
+  const size_t opsz = (size_t)std::max(1LL, n) * spw;  // elements of one operand buffer
   int* errw = (int*)(wb + w.off_err);
   MPDOK_CUDA_TRY(cudaMemsetAsync(errw, 0, 64, s));
   MPDOK_CUDA_TRY(cudaMemsetAsync(meta, 0, sizeof(LUMeta), s));
@@ -1072,22 +1091,20 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     if (fdtype == MPDOK_F32) {
       const int gs = prof_start(MPDOK_PROF_LU_GEMM, st);
       dim3 gg((unsigned)((m + 127) / 128), (unsigned)((nn + 127) / 128));
-      launch(k_gemm_update_f32, gg, 256, 0, st, C, w.ldw, (const float*)Ab, (const float*)Bb, (long long)SPW,
+      launch(k_gemm_update_f32, gg, 256, 0, st, C, w.ldw, (const float*)Ab, (const float*)Bb, spw,
              (int)m, (int)nn, K);
       prof_stop(gs, st, 2.0 * (double)m * (double)nn * K);
       prof_stop_bytes(gs, 8.0 * (double)m * (double)nn + 4.0 * (double)K * ((double)m + (double)nn));
       MPDOK_LAUNCH_CHECK("lu gemm f32");
       return MPDOK_OK;
     }
-    return gemm_update(C, w.ldw, Ab, Bb, SPW, (int)m, (int)nn, K, fdtype, MPDOK_ENGINE_TENSOR, errw, st);
+    return gemm_update(C, w.ldw, Ab, Bb, spw, (int)m, (int)nn, K, fdtype, MPDOK_ENGINE_TENSOR, errw, st);
   };
-  // Two-level right-looking LU.  Super-panel [J, Jend) of <= 1024 columns is
+  // Two-level right-looking LU.  Super-panel [J, Jend) of <= spw columns is
   // factored with 128-wide panels whose updates are confined to the
   // super-panel's row strip (rows < Jend, all columns right of the panel) and
   // column strip (rows >= Jend, columns < Jend); the far trailing matrix
-  // (rows, columns >= Jend) then receives all of them at once, K = 1024.
-  // (K = 1024 halves the FP32 read-modify-write of the far matrix against
-  // K = 512; at K = 2048 the longer inner strips cost more than that saves.)
+  // (rows, columns >= Jend) then receives all of them at once, K = spw.
   //
   // Look-ahead: super-panels are factored on a high-priority side stream.
   // The far update of super-panel J runs on the caller's stream in two parts:
@@ -1120,7 +1137,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     if (side) cudaStreamDestroy(side);
     if (strip) cudaStreamDestroy(strip);
   };
-  const bool lookahead = n > SPW;
+  const bool lookahead = n > spw;
   const bool split = n > LNB;
   if (split) {
     int lo = 0, hi = 0;
@@ -1145,9 +1162,9 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     }
   }
   auto body = [&]() -> int {
-    for (long long J = 0; J < n; J += SPW) {
-      const long long Jend = std::min<long long>(n, J + SPW);
-      const int buf = (int)((J / SPW) & 1);
+    for (long long J = 0; J < n; J += spw) {
+      const long long Jend = std::min<long long>(n, J + spw);
+      const int buf = (int)((J / spw) & 1);
       F* Lp = Lp2 + (size_t)buf * opsz;
       F* Up = Up2 + (size_t)buf * opsz;
       cudaStream_t sa = lookahead ? side : s;
@@ -1159,13 +1176,13 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
         const long long r1 = jp + LNB;                         // first row / column after the panel
         const long long nxt = std::min<long long>(r1 + LNB, Jend);  // end of the next panel of J
         const bool has_next = r1 < Jend;
-        const F* Lr = Lp + p * LNB;  // K-slot of panel p: row r of L21 at Lr + (r - J) * SPW
-        const F* Uc = Up + p * LNB;  // column c of U12 at Uc + (c - J) * SPW
+        const F* Lr = Lp + p * LNB;  // K-slot of panel p: row r of L21 at Lr + (r - J) * spw
+        const F* Uc = Up + p * LNB;  // column c of U12 at Uc + (c - J) * spw
         auto solve = [&](long long begin, long long end, cudaStream_t st) {
           const int nb = (int)((end - begin + 63) / 64);
           launch(k_trsm_pair<F>, (unsigned)(2 * nb), TRSM_THREADS, smem_tp, st, (const float*)W, w.ldw, jp, begin,
                  end, (const float*)(Uinv + (size_t)k * LNB * LNB), (const float*)(Linv + (size_t)k * LNB * LNB), Lp,
-                 Up, (long long)SPW, J, p * LNB, LU, L.ldf, nb);
+                 Up, spw, J, p * LNB, LU, L.ldf, nb);
         };
         // chain: diagonal LU, then the next panel's own block rows / columns
         const int ps = prof_start(MPDOK_PROF_LU_PANEL, sa);
@@ -1179,7 +1196,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
         MPDOK_LAUNCH_CHECK("lu panel");
         if (split) MPDOK_CUDA_TRY(cudaEventRecord(ev_a, sa));
         if (has_next)
-          MPDOK_TRY(update(r1, r1, nxt - r1, nxt - r1, Lr + (r1 - J) * SPW, Uc + (r1 - J) * SPW, LNB, sa));
+          MPDOK_TRY(update(r1, r1, nxt - r1, nxt - r1, Lr + (r1 - J) * spw, Uc + (r1 - J) * spw, LNB, sa));
         // strips: the rest of the panel solve and of panel p's updates
         if (split) MPDOK_CUDA_TRY(cudaStreamWaitEvent(sb, ev_a, 0));
         const long long begin = has_next ? nxt : r1;
@@ -1190,9 +1207,9 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
           MPDOK_LAUNCH_CHECK("lu panel solve");
         }
         if (has_next) {
-          MPDOK_TRY(update(r1, nxt, nxt - r1, n - nxt, Lr + (r1 - J) * SPW, Uc + (nxt - J) * SPW, LNB, sb));
-          MPDOK_TRY(update(nxt, r1, Jend - nxt, n - r1, Lr + (nxt - J) * SPW, Uc + (r1 - J) * SPW, LNB, sb));
-          MPDOK_TRY(update(Jend, r1, n - Jend, Jend - r1, Lr + (Jend - J) * SPW, Uc + (r1 - J) * SPW, LNB, sb));
+          MPDOK_TRY(update(r1, nxt, nxt - r1, n - nxt, Lr + (r1 - J) * spw, Uc + (nxt - J) * spw, LNB, sb));
+          MPDOK_TRY(update(nxt, r1, Jend - nxt, n - r1, Lr + (nxt - J) * spw, Uc + (r1 - J) * spw, LNB, sb));
+          MPDOK_TRY(update(Jend, r1, n - Jend, Jend - r1, Lr + (Jend - J) * spw, Uc + (r1 - J) * spw, LNB, sb));
         }
         if (split) MPDOK_CUDA_TRY(cudaEventRecord(ev_b, sb));
       }
@@ -1203,15 +1220,15 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
       }
       if (Jend < n) {
         const int K = (int)(Jend - J);
-        const F* La = Lp + (Jend - J) * SPW;
-        const F* Ua = Up + (Jend - J) * SPW;
+        const F* La = Lp + (Jend - J) * spw;
+        const F* Ua = Up + (Jend - J) * spw;
         if (!lookahead) {
           MPDOK_TRY(update(Jend, Jend, n - Jend, n - Jend, La, Ua, K, s));
         } else {
-          const long long Jn = std::min<long long>(n, Jend + SPW);
+          const long long Jn = std::min<long long>(n, Jend + spw);
           // (a) what super-panel J + 1 reads and writes first
           MPDOK_TRY(update(Jend, Jend, Jn - Jend, n - Jend, La, Ua, K, s));
-          MPDOK_TRY(update(Jn, Jend, n - Jn, Jn - Jend, Lp + (Jn - J) * SPW, Ua, K, s));
+          MPDOK_TRY(update(Jn, Jend, n - Jn, Jn - Jend, Lp + (Jn - J) * spw, Ua, K, s));
           MPDOK_CUDA_TRY(cudaEventRecord(ev_ready, s));
           MPDOK_CUDA_TRY(cudaStreamWaitEvent(side, ev_ready, 0));
           // (b) the rest of the trailing matrix, concurrent with J + 1, in up to
@@ -1222,7 +1239,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
           const long long chunk = std::max<long long>(2048, (rest / 4 + 255) / 256 * 256);
           for (long long c = Jn; c < n; c += chunk) {
             const long long w = std::min<long long>(chunk, n - c);
-            MPDOK_TRY(update(Jn, c, n - Jn, w, Lp + (Jn - J) * SPW, Up + (c - J) * SPW, K, s));
+            MPDOK_TRY(update(Jn, c, n - Jn, w, Lp + (Jn - J) * spw, Up + (c - J) * spw, K, s));
           }
         }
       }

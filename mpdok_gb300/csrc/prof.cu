@@ -148,3 +148,29 @@ extern "C" long long mpdok_profile_skipped(int cls) {
   }
   return n;
 }
+
+// Timeline of the closed records in launch order: out[4 i .. 4 i + 3] =
+// (class, start ms, end ms, work), the times relative to the first record's
+// start.  Writes at most max_records records and returns how many there are.
+extern "C" long long mpdok_profile_timeline(double* out, long long max_records) {
+  std::lock_guard<std::mutex> lk(g_pmu);
+  long long n = 0;
+  cudaEvent_t t0 = nullptr;
+  for (size_t i = 0; i < g_recs.size(); ++i) {
+    const ProfRec& r = g_recs[i];
+    if (!r.closed) continue;
+    if (!t0) t0 = r.a;
+    if (out && n < max_records) {
+      float a = 0.f, b = 0.f;
+      cudaError_t e = cudaEventElapsedTime(&a, t0, r.a);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&b, t0, r.b);
+      if (e != cudaSuccess) return cuda_status(e, "mpdok_profile_timeline");
+      out[4 * n] = (double)r.cls;
+      out[4 * n + 1] = (double)a;
+      out[4 * n + 2] = (double)b;
+      out[4 * n + 3] = r.work;
+    }
+    ++n;
+  }
+  return n;
+}

@@ -197,3 +197,36 @@ def test_lu_ir_many_rhs_matches_single_rhs_and_oracle(fdtype, n, k):
     xs, d = lu.solve_ir(A, torch.from_numpy(B[:, 0].copy()).cuda(), tol=1e-12, maxiter_outer=10)
     assert d["converged"]
     np.testing.assert_allclose(Xh[:, 0], xs.cpu().numpy(), rtol=1e-9, atol=1e-12 * np.abs(Xh[:, 0]).max())
+
+
+def test_profile_timeline_matches_class_totals():
+    """The per-launch timeline of an LU factorization (chain, strip and far
+    streams) agrees with the per-class totals of the same records."""
+    from mpdok_gb300 import _native as N
+    from mpdok_gb300.lu import LUFactorization
+    X, A, b = _rbf(3000, 1600.0, 1e-2, seed=5)
+    N.profile_enable(True)
+    try:
+        LUFactorization(A, dtype="fp16")
+        torch.cuda.synchronize()
+        tl = N.profile_timeline()
+        totals = {c: N.profile_query(c) for c in range(8)}
+    finally:
+        N.profile_enable(False)
+    assert len(tl) == sum(cnt for _, cnt, _ in totals.values())
+    assert np.all(tl[:, 2] >= tl[:, 1]) and np.all(tl[:, 1] >= 0.0)
+    for c in (N.PROF_LU_PANEL, N.PROF_LU_GEMM):
+        rows = tl[tl[:, 0] == c]
+        ms, cnt, work = totals[c]
+        assert len(rows) == cnt > 0
+        assert np.isclose(rows[:, 3].sum(), work, rtol=1e-12)
+        assert np.isclose((rows[:, 2] - rows[:, 1]).sum(), ms, rtol=1e-3, atol=1e-3)
+    # a record per 128-column panel on the chain stream, and one on the strip
+    # stream where rows remain below the panel's next block (super-panels of 1024)
+    n, expect = 3000, 0
+    for jp in range(0, n, 128):
+        jend = min(n, (jp // 1024 + 1) * 1024)
+        r1 = jp + 128
+        begin = min(r1 + 128, jend) if r1 < jend else r1
+        expect += 1 + (begin < n)
+    assert len(tl[tl[:, 0] == N.PROF_LU_PANEL]) == expect
