@@ -274,6 +274,29 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
 //   B  U12 = L11^-1 A12 by column-parallel forward substitution (one thread
 //      per trailing column, the column in registers);
 //   C  A22 -= L21 U12 (K = 32) by all 1024 threads.
+// Elimination step K of a 32 x 32 block held one row per lane (the warp's
+// rows in registers): the pivot row is read by shuffle from lane K, a pivot
+// below tau in magnitude is replaced by +-tau (counted), and steps K >=
+// active are skipped.  Recursion over K keeps every register index static.
+template <int K>
+__device__ __forceinline__ void top_block_step(float (&row)[32], int lane, int active, float tau, int* nperturb) {
+  if (K < active) {  // uniform across the warp
+    if (lane == K && !(fabsf(row[K]) >= tau)) {
+      row[K] = (row[K] < 0.f) ? -tau : tau;
+      atomicAdd(nperturb, 1);
+    }
+    const float pinv = __frcp_rn(__shfl_sync(0xffffffffu, row[K], K));
+    const float l = row[K] * pinv;  // within 1.5 ulp of row[K] / pivot
+#pragma unroll
+    for (int c = K + 1; c < 32; ++c) {
+      const float u = __shfl_sync(0xffffffffu, row[c], K);
+      if (lane > K) row[c] = fmaf(-l, u, row[c]);
+    }
+    if (lane > K) row[K] = l;
+  }
+  if constexpr (K + 1 < 32) top_block_step<K + 1>(row, lane, active, tau, nperturb);
+}
+
 template <typename F>
 __global__ void __launch_bounds__(DIAG_THREADS, 1)
 k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __restrict__ LU, long long ldf,
@@ -283,7 +306,12 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
   float* XL = sm + LNB * DP;
   float* XU = sm + 2 * LNB * DP;
   float* Tmp = sm + 3 * LNB * DP;
-  __shared__ float prow[2][32];
+  // phase A's copy of the top block's U rows (pitch UBP, 16-byte aligned) and
+  // pivot reciprocals (row 32), in Tmp, which is free until the inverses
+  constexpr int UBP = 36;
+  float* Ub = Tmp;
+  static_assert(33 * UBP <= 64 * 65, "the U copy must fit in Tmp");
+  static_assert((3 * LNB * DP) % 4 == 0, "Tmp must be 16-byte aligned");
   const int tid = threadIdx.x;
   for (int idx = tid; idx < LNB * LNB; idx += DIAG_THREADS) {
     const int r = idx % LNB, c = idx / LNB;
@@ -291,36 +319,44 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
   }
   __syncthreads();
   for (int c0 = 0; c0 < nbk; c0 += 32) {
-    // ---- A: sub-panel columns [c0, c0 + 32), rows [c0, 128)
+    // ---- A: sub-panel columns [c0, c0 + 32), rows [c0, 128), one row per
+    // thread.  The 32 x 32 top block lives in warp c0 / 32 and is factored
+    // warp-synchronously (pivot rows by shuffle); the rows below then apply
+    // its 32 U rows with no further barrier.  Every row sees the same
+    // operations in the same order as a step-by-step elimination.
     if (tid < LNB) {
-      const int r = tid;
+      const int r = tid, lane = tid & 31;
       float row[32];
 #pragma unroll
       for (int c = 0; c < 32; ++c) row[c] = (r >= c0) ? T[r * DP + c0 + c] : 0.f;
+      if ((r >> 5) == (c0 >> 5)) {
+        top_block_step<0>(row, lane, nbk - c0, tau, nperturb);
 #pragma unroll
-      for (int jj = 0; jj < 32; ++jj) {
-        const int j = c0 + jj;
-        if (j >= nbk) break;  // uniform across the 128 threads
-        float* pr = prow[jj & 1];
-        if (r == j) {
-          float p = row[jj];
-          if (!(fabsf(p) >= tau)) {
-            p = (p < 0.f) ? -tau : tau;
-            row[jj] = p;
-            atomicAdd(nperturb, 1);
-          }
+        for (int c = 0; c < 32; ++c) T[r * DP + c0 + c] = row[c];
+        // U rows again at a 16-byte-aligned pitch, and the pivot reciprocals
 #pragma unroll
-          for (int c = 0; c < 32; ++c) pr[c] = row[c];
-        }
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        if (r > j) {
-          const float l = row[jj] * __frcp_rn(pr[jj]);  // within 1.5 ulp of row[jj] / pivot
-          row[jj] = l;
-#pragma unroll
-          for (int c = jj + 1; c < 32; ++c) row[c] = fmaf(-l, pr[c], row[c]);
-        }
+        for (int c = 0; c < 32; c += 4)
+          *reinterpret_cast<float4*>(Ub + lane * UBP + c) = make_float4(row[c], row[c + 1], row[c + 2], row[c + 3]);
+        Ub[32 * UBP + lane] = __frcp_rn(T[r * DP + c0 + lane]);  // the pivot, as the steps above used it
       }
-      if (r >= c0) {
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // the top block's U rows are in T and Ub
+      if ((r >> 5) > (c0 >> 5)) {
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+          if (c0 + k < nbk) {
+            const float l = row[k] * Ub[32 * UBP + k];
+            row[k] = l;
+            const float* urow = Ub + k * UBP;
+#pragma unroll
+            for (int c4 = (k + 1) & ~3; c4 < 32; c4 += 4) {
+              const float4 u = *reinterpret_cast<const float4*>(urow + c4);
+              if (c4 + 0 > k) row[c4 + 0] = fmaf(-l, u.x, row[c4 + 0]);
+              if (c4 + 1 > k) row[c4 + 1] = fmaf(-l, u.y, row[c4 + 1]);
+              if (c4 + 2 > k) row[c4 + 2] = fmaf(-l, u.z, row[c4 + 2]);
+              if (c4 + 3 > k) row[c4 + 3] = fmaf(-l, u.w, row[c4 + 3]);
+            }
+          }
+        }
 #pragma unroll
         for (int c = 0; c < 32; ++c) T[r * DP + c0 + c] = row[c];
       }
