@@ -816,15 +816,15 @@ def main():
         if cnt == 0 or ms <= 0:
             continue
         if name in ("lu_gemm",):
-            # K <= 512 with an FP32 C read and written: 2K / 8 <= 128 flop per byte, below the
-            # ridge point (bf16 peak / HBM ~ 286), so the binding roofline is HBM; the tensor
+            # K <= 1024 with an FP32 C read and written: 2K / 8 <= 256 flop per byte, at or below
+            # the ridge point (bf16 peak / HBM ~ 286), so the binding roofline is HBM; the tensor
             # view is kept beside it
             tflops = work / (ms / 1e3) / 1e12
             byts = prof_bytes[name]
             gbs = byts / (ms / 1e3) / 1e9
             tr = None
-            if traffic.get("lu_gemm_bytes_per_flop"):
-                tr = traffic["lu_gemm_bytes_per_flop"] * work / cnt
+            if traffic.get("lu_gemm_bytes_per_byte"):
+                tr = traffic["lu_gemm_bytes_per_byte"] * byts / cnt
             rooflines[name] = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
                                "traffic": tr, "launches": cnt, "avg_launch_ms": ms / cnt,
                                "work_per_launch": byts / cnt, "flops_per_launch": work / cnt,
