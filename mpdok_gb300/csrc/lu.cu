@@ -319,46 +319,49 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
   }
   __syncthreads();
   for (int c0 = 0; c0 < nbk; c0 += 32) {
-    // ---- A: sub-panel columns [c0, c0 + 32), rows [c0, 128), one row per
-    // thread.  The 32 x 32 top block lives in warp c0 / 32 and is factored
-    // warp-synchronously (pivot rows by shuffle); the rows below then apply
-    // its 32 U rows with no further barrier.  Every row sees the same
+    // ---- A: sub-panel columns [c0, c0 + 32), rows [c0, 128).  The 32 x 32
+    // top block lives in warp c0 / 32, one row per lane, and is factored
+    // warp-synchronously (pivot rows by shuffle).  The rows below then take
+    // eight threads each (four columns per thread, warps 4 and up) and apply
+    // the block's U rows from an aligned copy.  Every entry sees the same
     // operations in the same order as a step-by-step elimination.
-    if (tid < LNB) {
+    if ((tid >> 5) == (c0 >> 5)) {
       const int r = tid, lane = tid & 31;
       float row[32];
 #pragma unroll
-      for (int c = 0; c < 32; ++c) row[c] = (r >= c0) ? T[r * DP + c0 + c] : 0.f;
-      if ((r >> 5) == (c0 >> 5)) {
-        top_block_step<0>(row, lane, nbk - c0, tau, nperturb);
+      for (int c = 0; c < 32; ++c) row[c] = T[r * DP + c0 + c];
+      top_block_step<0>(row, lane, nbk - c0, tau, nperturb);
 #pragma unroll
-        for (int c = 0; c < 32; ++c) T[r * DP + c0 + c] = row[c];
-        // U rows again at a 16-byte-aligned pitch, and the pivot reciprocals
+      for (int c = 0; c < 32; ++c) T[r * DP + c0 + c] = row[c];
+      // U rows again at a 16-byte-aligned pitch, and the pivot reciprocals
 #pragma unroll
-        for (int c = 0; c < 32; c += 4)
-          *reinterpret_cast<float4*>(Ub + lane * UBP + c) = make_float4(row[c], row[c + 1], row[c + 2], row[c + 3]);
-        Ub[32 * UBP + lane] = __frcp_rn(T[r * DP + c0 + lane]);  // the pivot, as the steps above used it
-      }
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // the top block's U rows are in T and Ub
-      if ((r >> 5) > (c0 >> 5)) {
+      for (int c = 0; c < 32; c += 4)
+        *reinterpret_cast<float4*>(Ub + lane * UBP + c) = make_float4(row[c], row[c + 1], row[c + 2], row[c + 3]);
+      Ub[32 * UBP + lane] = __frcp_rn(T[r * DP + c0 + lane]);  // the pivot, as the steps above used it
+    }
+    __syncthreads();
+    {
+      const int u = tid - LNB;  // whole warps: the rows below come in multiples of four
+      const int r = c0 + 32 + (u >> 3), g = u & 7;
+      if (u >= 0 && r < LNB) {
+        float v[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) v[i] = T[r * DP + c0 + 4 * g + i];
+        const int src = (tid & 31) & ~7;  // lane of this row's columns 0..3
 #pragma unroll
         for (int k = 0; k < 32; ++k) {
-          if (c0 + k < nbk) {
-            const float l = row[k] * Ub[32 * UBP + k];
-            row[k] = l;
-            const float* urow = Ub + k * UBP;
-#pragma unroll
-            for (int c4 = (k + 1) & ~3; c4 < 32; c4 += 4) {
-              const float4 u = *reinterpret_cast<const float4*>(urow + c4);
-              if (c4 + 0 > k) row[c4 + 0] = fmaf(-l, u.x, row[c4 + 0]);
-              if (c4 + 1 > k) row[c4 + 1] = fmaf(-l, u.y, row[c4 + 1]);
-              if (c4 + 2 > k) row[c4 + 2] = fmaf(-l, u.z, row[c4 + 2]);
-              if (c4 + 3 > k) row[c4 + 3] = fmaf(-l, u.w, row[c4 + 3]);
-            }
+          if (c0 + k < nbk) {  // uniform
+            const float l = __shfl_sync(0xffffffffu, v[k & 3], src | (k >> 2)) * Ub[32 * UBP + k];
+            if (g == (k >> 2)) v[k & 3] = l;
+            const float4 uu = *reinterpret_cast<const float4*>(Ub + k * UBP + 4 * g);
+            if (4 * g + 0 > k) v[0] = fmaf(-l, uu.x, v[0]);
+            if (4 * g + 1 > k) v[1] = fmaf(-l, uu.y, v[1]);
+            if (4 * g + 2 > k) v[2] = fmaf(-l, uu.z, v[2]);
+            if (4 * g + 3 > k) v[3] = fmaf(-l, uu.w, v[3]);
           }
         }
 #pragma unroll
-        for (int c = 0; c < 32; ++c) T[r * DP + c0 + c] = row[c];
+        for (int i = 0; i < 4; ++i) T[r * DP + c0 + 4 * g + i] = v[i];
       }
     }
     __syncthreads();
