@@ -409,83 +409,88 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
 }
 
 // --------------------------------------------------------------- TRSMs
-// L21 = W21 * Uinv.  Block: 64 rows x 128 columns; thread 4 rows x 8 columns.
-template <typename F>
+// L21 = W21 * Uinv.  Block: RB rows x 128 columns; thread RB / 16 rows x 8 columns.
+template <typename F, int RB>
 __device__ __forceinline__ void trsm_right_body(const float* __restrict__ W, long long ldw, long long j0,
                                                 long long r_begin, long long n, const float* __restrict__ Uinv,
                                                 F* __restrict__ Lp, long long lp_pitch, long long lp_row0, int koff,
                                                 F* __restrict__ LU, long long ldf, int bid) {
+  static_assert(RB % 16 == 0 && RB <= 64, "rows per block: a multiple of 16, at most 64");
+  constexpr int TR = RB / 16;     // rows per thread
   extern __shared__ float sm[];
   constexpr int XP = LNB + 1;     // odd pitch: the row-fastest staging writes hit distinct banks
   constexpr int TSP = LNB + 4;    // keeps the float4 reads of Ts aligned; staging writes 4-way at most
-  float* Xs = sm;                 // [64][XP]   rows of W21 (then the output tile)
-  float* Ts = sm + 64 * XP;       // [128][TSP] Uinv row-major [k][c]
+  static_assert((RB * XP) % 4 == 0, "Ts must be 16-byte aligned");
+  float* Xs = sm;                 // [RB][XP]   rows of W21 (then the output tile)
+  float* Ts = sm + RB * XP;       // [128][TSP] Uinv row-major [k][c]
   const int tid = threadIdx.x;
-  const long long r0 = r_begin + (long long)bid * 64;
-  const int rows = (int)min(64LL, n - r0);
-  stage_tile<64 * LNB, TRSM_THREADS, 32>(
+  const long long r0 = r_begin + (long long)bid * RB;
+  const int rows = (int)min((long long)RB, n - r0);
+  stage_tile<RB * LNB, TRSM_THREADS, (RB * LNB / TRSM_THREADS < 32 ? RB * LNB / TRSM_THREADS : 32)>(
       tid,
       [&](int idx) {
-        const int r = idx % 64, c = idx / 64;
+        const int r = idx % RB, c = idx / RB;
         return (r < rows) ? W[(r0 + r) + (j0 + c) * ldw] : 0.f;
       },
-      [&](int idx, float v) { Xs[(idx % 64) * XP + idx / 64] = v; });
+      [&](int idx, float v) { Xs[(idx % RB) * XP + idx / RB] = v; });
   // Uinv column-major: [c*128 + k]
   stage_tile<LNB * LNB, TRSM_THREADS, 32>(
       tid, [&](int idx) { return Uinv[idx]; }, [&](int idx, float v) { Ts[(idx % LNB) * TSP + idx / LNB] = v; });
   __syncthreads();
   const int ty = tid / 16, tx = tid % 16;
-  float acc[4][8];
+  float acc[TR][8];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < TR; ++i)
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
 #pragma unroll 4
   for (int k = 0; k < LNB; ++k) {
-    float a[4], b[8];
+    float a[TR], b[8];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) a[i] = Xs[(ty * 4 + i) * XP + k];
+    for (int i = 0; i < TR; ++i) a[i] = Xs[(ty * TR + i) * XP + k];
     const float4 b0 = *reinterpret_cast<const float4*>(&Ts[k * TSP + tx * 8]);
     const float4 b1 = *reinterpret_cast<const float4*>(&Ts[k * TSP + tx * 8 + 4]);
     b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w; b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < TR; ++i)
 #pragma unroll
       for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
   }
   __syncthreads();
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < TR; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) Xs[(ty * 4 + i) * XP + tx * 8 + j] = acc[i][j];
+    for (int j = 0; j < 8; ++j) Xs[(ty * TR + i) * XP + tx * 8 + j] = acc[i][j];
   __syncthreads();
   // K-major operand for the trailing GEMM: Lp[row][k]
-  for (int idx = tid; idx < 64 * LNB; idx += blockDim.x) {
+  for (int idx = tid; idx < RB * LNB; idx += TRSM_THREADS) {
     const int r = idx / LNB, c = idx % LNB;
     if (r < rows) Lp[(r0 - lp_row0 + r) * lp_pitch + koff + c] = from_f32<F>(Xs[r * XP + c]);
   }
   // column-major factor
-  for (int idx = tid; idx < 64 * LNB; idx += blockDim.x) {
-    const int r = idx % 64, c = idx / 64;
+  for (int idx = tid; idx < RB * LNB; idx += TRSM_THREADS) {
+    const int r = idx % RB, c = idx / RB;
     if (r < rows) LU[(r0 + r) + (j0 + c) * ldf] = from_f32<F>(Xs[r * XP + c]);
   }
 }
 
-// U12 = Linv * W12.  Block: 128 rows x 64 columns; thread 8 rows x 4 columns.
-template <typename F>
+// U12 = Linv * W12.  Block: 128 rows x RB columns; thread 8 rows x RB / 16 columns.
+template <typename F, int RB>
 __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long long ldw, long long j0,
                                                long long c_begin, long long n, const float* __restrict__ Linv,
                                                F* __restrict__ Up, long long up_pitch, long long up_col0, int koff,
                                                F* __restrict__ LU, long long ldf, int bid) {
+  static_assert(RB % 16 == 0 && RB <= 64, "columns per block: a multiple of 16, at most 64");
+  constexpr int TC = RB / 16;       // columns per thread
   extern __shared__ float sm[];
-  constexpr int XP = 64 + 4;
+  constexpr int XP = RB + 4;
   float* Xs = sm;                   // [128][XP]  W12 tile [k][c]
   float* Ts = sm + LNB * XP;        // [128][LNB+1] Linv row-major [r][k]
   constexpr int TP = LNB + 1;
   const int tid = threadIdx.x;
-  const long long c0 = c_begin + (long long)bid * 64;
-  const int cols = (int)min(64LL, n - c0);
-  stage_tile<LNB * 64, TRSM_THREADS, 32>(
+  const long long c0 = c_begin + (long long)bid * RB;
+  const int cols = (int)min((long long)RB, n - c0);
+  stage_tile<LNB * RB, TRSM_THREADS, (LNB * RB / TRSM_THREADS < 32 ? LNB * RB / TRSM_THREADS : 32)>(
       tid,
       [&](int idx) {
         const int k = idx % LNB, c = idx / LNB;
@@ -497,30 +502,35 @@ __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long
       tid, [&](int idx) { return Linv[idx]; }, [&](int idx, float v) { Ts[(idx % LNB) * TP + idx / LNB] = v; });
   __syncthreads();
   const int ty = tid / 16, tx = tid % 16;
-  float acc[8][4];
+  float acc[8][TC];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < TC; ++j) acc[i][j] = 0.f;
 #pragma unroll 4
   for (int k = 0; k < LNB; ++k) {
-    float a[8];
+    float a[8], bb[TC];
 #pragma unroll
     for (int i = 0; i < 8; ++i) a[i] = Ts[(ty * 8 + i) * TP + k];
-    const float4 b = *reinterpret_cast<const float4*>(&Xs[k * XP + tx * 4]);
-    const float bb[4] = {b.x, b.y, b.z, b.w};
+    if constexpr (TC == 4) {
+      const float4 b = *reinterpret_cast<const float4*>(&Xs[k * XP + tx * 4]);
+      bb[0] = b.x; bb[1] = b.y; bb[2] = b.z; bb[3] = b.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < TC; ++j) bb[j] = Xs[k * XP + tx * TC + j];
+    }
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
+      for (int j = 0; j < TC; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
   }
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) Xs[(ty * 8 + i) * XP + tx * 4 + j] = acc[i][j];
+    for (int j = 0; j < TC; ++j) Xs[(ty * 8 + i) * XP + tx * TC + j] = acc[i][j];
   __syncthreads();
-  for (int idx = tid; idx < LNB * 64; idx += blockDim.x) {
+  for (int idx = tid; idx < LNB * RB; idx += TRSM_THREADS) {
     const int r = idx % LNB, c = idx / LNB;
     if (c < cols) {
       const F v = from_f32<F>(Xs[r * XP + c]);
@@ -530,18 +540,27 @@ __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long
   }
 }
 
+// Shared memory of k_trsm_pair<F, RB>: the larger of its two bodies.
+constexpr size_t trsm_pair_smem(int rb) {
+  const size_t right = (size_t)(rb * (LNB + 1) + LNB * (LNB + 4)) * sizeof(float);
+  const size_t left = (size_t)(LNB * (rb + 4) + LNB * (LNB + 1)) * sizeof(float);
+  return right > left ? right : left;
+}
+
 // Both panel solves of one inner panel in one launch: blocks [0, nb) form
-// L21 = W21 Uinv (64 rows each), the rest U12 = Linv W12 (64 columns each);
-// they write disjoint outputs, so they run side by side.
-template <typename F>
+// L21 = W21 Uinv (RB rows each), the rest U12 = Linv W12 (RB columns each);
+// they write disjoint outputs, so they run side by side.  RB = 64 for the
+// strips; RB = 16 for the 128 rows and columns of the next panel, which sit
+// on the chain: four times the CTAs, a quarter of the work each.
+template <typename F, int RB>
 __global__ void __launch_bounds__(TRSM_THREADS)
 k_trsm_pair(const float* __restrict__ W, long long ldw, long long j0, long long begin, long long n,
             const float* __restrict__ Uinv, const float* __restrict__ Linv, F* __restrict__ Lp, F* __restrict__ Up,
             long long pitch, long long base0, int koff, F* __restrict__ LU, long long ldf, int nb) {
   if ((int)blockIdx.x < nb)
-    trsm_right_body<F>(W, ldw, j0, begin, n, Uinv, Lp, pitch, base0, koff, LU, ldf, (int)blockIdx.x);
+    trsm_right_body<F, RB>(W, ldw, j0, begin, n, Uinv, Lp, pitch, base0, koff, LU, ldf, (int)blockIdx.x);
   else
-    trsm_left_body<F>(W, ldw, j0, begin, n, Linv, Up, pitch, base0, koff, LU, ldf, (int)blockIdx.x - nb);
+    trsm_left_body<F, RB>(W, ldw, j0, begin, n, Linv, Up, pitch, base0, koff, LU, ldf, (int)blockIdx.x - nb);
 }
 
 // CUDA-core trailing update for FP32 factors: C -= A B^T, A (M x 128), B (N x 128) K-major FP32.
@@ -1108,17 +1127,18 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   MPDOK_LAUNCH_CHECK("lu scale");
 
   const size_t smem_diag = DIAG_SMEM;
-  const size_t smem_tr = (size_t)(64 * (LNB + 1) + LNB * (LNB + 4)) * sizeof(float);
-  const size_t smem_tl = (size_t)(LNB * (64 + 4) + LNB * (LNB + 1)) * sizeof(float);
-  const size_t smem_tp = std::max(smem_tr, smem_tl);
+  constexpr size_t smem_tp = trsm_pair_smem(64), smem_tp16 = trsm_pair_smem(16);
   static bool attrs = false;
   if (!attrs) {
     MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
     MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
     MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__nv_bfloat16, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__half, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<float, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__nv_bfloat16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp16));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__half, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp16));
+    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp16));
     attrs = true;
   }
   const float tau = 1e-6f;
@@ -1217,11 +1237,20 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
         const bool has_next = r1 < Jend;
         const F* Lr = Lp + p * LNB;  // K-slot of panel p: row r of L21 at Lr + (r - J) * spw
         const F* Uc = Up + p * LNB;  // column c of U12 at Uc + (c - J) * spw
-        auto solve = [&](long long begin, long long end, cudaStream_t st) {
-          const int nb = (int)((end - begin + 63) / 64);
-          launch(k_trsm_pair<F>, (unsigned)(2 * nb), TRSM_THREADS, smem_tp, st, (const float*)W, w.ldw, jp, begin,
-                 end, (const float*)(Uinv + (size_t)k * LNB * LNB), (const float*)(Linv + (size_t)k * LNB * LNB), Lp,
-                 Up, spw, J, p * LNB, LU, L.ldf, nb);
+        // panel solve of rows / columns [begin, end): 16-row blocks for the
+        // next panel's own block (on the chain), 64-row blocks for the rest
+        auto solve = [&](long long begin, long long end, cudaStream_t st, bool next_block) {
+          const float* ui = Uinv + (size_t)k * LNB * LNB;
+          const float* li = Linv + (size_t)k * LNB * LNB;
+          if (next_block) {
+            const int nb = (int)((end - begin + 15) / 16);
+            launch(k_trsm_pair<F, 16>, (unsigned)(2 * nb), TRSM_THREADS, smem_tp16, st, (const float*)W, w.ldw, jp,
+                   begin, end, ui, li, Lp, Up, spw, J, p * LNB, LU, L.ldf, nb);
+          } else {
+            const int nb = (int)((end - begin + 63) / 64);
+            launch(k_trsm_pair<F, 64>, (unsigned)(2 * nb), TRSM_THREADS, smem_tp, st, (const float*)W, w.ldw, jp,
+                   begin, end, ui, li, Lp, Up, spw, J, p * LNB, LU, L.ldf, nb);
+          }
         };
         // chain: diagonal LU, then the next panel's own block rows / columns
         const int ps = prof_start(MPDOK_PROF_LU_PANEL, sa);
@@ -1229,7 +1258,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
                Linv + (size_t)k * LNB * LNB, Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
         if (has_next) {
           if (split && jp > J) MPDOK_CUDA_TRY(cudaStreamWaitEvent(sa, ev_b, 0));  // strips of panel p - 1
-          solve(r1, nxt, sa);
+          solve(r1, nxt, sa, true);
         }
         prof_stop(ps, sa, 2.0 * 2.0 * (double)(nxt - std::min(r1, nxt)) * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
         MPDOK_LAUNCH_CHECK("lu panel");
@@ -1241,7 +1270,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
         const long long begin = has_next ? nxt : r1;
         if (begin < n) {
           const int ps2 = prof_start(MPDOK_PROF_LU_PANEL, sb);
-          solve(begin, n, sb);
+          solve(begin, n, sb, false);
           prof_stop(ps2, sb, 2.0 * 2.0 * (double)(n - begin) * LNB * LNB);
           MPDOK_LAUNCH_CHECK("lu panel solve");
         }
