@@ -1414,7 +1414,7 @@ extern "C" int mpdok_lu_factor(const double* A, long long lda, long long n, int 
                                size_t factor_bytes, void* work, size_t work_bytes, cudaStream_t s) {
   MPDOK_ARG_CHECK(n >= 0, "negative n");
   MPDOK_ARG_CHECK(fdtype == MPDOK_BF16 || fdtype == MPDOK_F16 || fdtype == MPDOK_F32, "factor dtype");
-  MPDOK_ARG_CHECK(pivoting == 0, "partial pivoting is not available in this build; use pivoting = 0");
+  MPDOK_ARG_CHECK(pivoting == 0, "partial pivoting is not implemented; use pivoting = 0");
   if (n == 0) return MPDOK_OK;
   MPDOK_ARG_CHECK(A && factors && work, "null pointer");
   MPDOK_ARG_CHECK(lda >= n, "lda < n");

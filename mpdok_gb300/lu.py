@@ -35,7 +35,7 @@ class LUFactorization:
 
     def __init__(self, A, dtype: str = "fp16", pivoting: bool = False, work: Workspace | None = None):
         if pivoting:
-            raise NotImplementedError("partial pivoting is not available in this build")
+            raise NotImplementedError("partial pivoting is not implemented: the LU is unpivoted with pivot perturbation")
         self.fdtype = DTYPES[dtype]
         self.dtype = dtype
         A64 = as_fortran(A, torch.float64)
