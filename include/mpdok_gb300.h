@@ -215,10 +215,12 @@ MPDOK_API int mpdok_mf_cg_ir(const double* coords, long long n, int dim, int ker
  * Sgetrf precision, benchmark_mpdok.ipynb:982-993).
  *
  * Factors live in a caller-owned device buffer of mpdok_lu_factor_size()
- * bytes; factorization scratch is mpdok_lu_work_size() bytes.  pivoting: 0 =
- * none (SPD / diagonally dominant systems, e.g. Gaussian RBF), 1 = partial
- * pivoting.  Return: 0 ok, > 0 number of pivots that had to be perturbed
- * away from zero (still a usable preconditioner), < 0 error. */
+ * bytes; factorization scratch is mpdok_lu_work_size() bytes.  pivoting must
+ * be 0: the LU is unpivoted (SPD / diagonally dominant systems, e.g. Gaussian
+ * RBF), with pivots below 1e-6 in magnitude replaced by +-1e-6; partial
+ * pivoting is not implemented (MPDOK_ERR_INVALID_ARG).  Return: 0 ok, > 0
+ * number of pivots that had to be perturbed away from zero (still a usable
+ * preconditioner), < 0 error. */
 enum { MPDOK_ENGINE_TENSOR = 0, MPDOK_ENGINE_SIMT = 1 };
 
 MPDOK_API int mpdok_gemm_update(float* C, long long ldc, const void* A, const void* B, int M, int N, int K,
@@ -227,6 +229,17 @@ MPDOK_API size_t mpdok_lu_factor_size(long long n, int fdtype);
 MPDOK_API size_t mpdok_lu_work_size(long long n, int fdtype);
 MPDOK_API int mpdok_lu_factor(const double* A, long long lda, long long n, int fdtype, int pivoting, void* factors,
                               size_t factor_bytes, void* work, size_t work_bytes, cudaStream_t stream);
+/* The launch schedule of mpdok_lu_factor for n and fdtype, host only (no
+ * device call): every launch, event record and event wait across its three
+ * streams (0 caller's, 1 chain, 2 strip), in issue order.  12 integers per
+ * step: kind (0 diagonal LU, 1 panel solve, 2 trailing update, 3 event record,
+ * 4 event wait, 5 / 6 profiling window start / stop), stream, J (super-panel
+ * start), jp (panel start), a, b (solve: rows and columns [a, b); update:
+ * first C row and column), m, nn (update extent), K, koff (update depth and
+ * operand K-slot), rb (solve rows per block), event.  Writes at most
+ * max_steps steps (out may be NULL); returns the number of steps or a
+ * negative status. */
+MPDOK_API long long mpdok_lu_schedule(long long n, int fdtype, long long* out, long long max_steps);
 /* z = (D U^-1 L^-1 P D) v: one application of the factorization (FP32 vectors). */
 MPDOK_API size_t mpdok_lu_apply_work_size(long long n);
 MPDOK_API int mpdok_lu_apply(const void* factors, long long n, int fdtype, const float* v, float* z, void* work,

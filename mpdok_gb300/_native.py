@@ -153,6 +153,7 @@ _SIGS = {
                                         c_double, c_int, c_void_p, c_size_t, ctypes.POINTER(SolveInfo), c_void_p]),
     "mpdok_profile_bytes": (c_double, [c_int]),
     "mpdok_profile_timeline": (c_ll, [ctypes.POINTER(c_double), c_ll]),
+    "mpdok_lu_schedule": (c_ll, [c_ll, c_int, ctypes.POINTER(c_ll), c_ll]),
     "mpdok_batch_create": (c_int, [c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, ctypes.POINTER(c_void_p)]),
     "mpdok_batch_destroy": (c_int, [c_void_p]),
     "mpdok_batch_bytes": (c_size_t, [c_void_p]),
@@ -257,6 +258,15 @@ def profile_bytes(cls: int) -> float:
 def profile_skipped(cls: int) -> int:
     """Launches of one class that a device skip flag turned off."""
     return int(load().mpdok_profile_skipped(cls))
+
+
+def lu_schedule(n: int, fdtype: int) -> np.ndarray:
+    """(steps, 12) int64 array: the launch schedule of mpdok_lu_factor (host only)."""
+    lib = load()
+    cnt = check(int(lib.mpdok_lu_schedule(n, fdtype, None, 0)), "lu_schedule")
+    out = np.zeros((max(cnt, 1), 12), dtype=np.int64)
+    check(int(lib.mpdok_lu_schedule(n, fdtype, out.ctypes.data_as(ctypes.POINTER(c_ll)), cnt)), "lu_schedule")
+    return out[:cnt]
 
 
 def profile_timeline() -> np.ndarray:

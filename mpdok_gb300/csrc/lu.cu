@@ -1101,6 +1101,168 @@ int lu_apply_any(const void* fbuf, long long n, int fdtype, const float* v, floa
   }
 }
 
+// ------------------------------------------------------ factorization schedule
+// Two-level right-looking LU.  Super-panel [J, Jend) of <= spw columns is
+// factored with 128-wide panels whose updates are confined to the
+// super-panel's row strip (rows < Jend, all columns right of the panel) and
+// column strip (rows >= Jend, columns < Jend); the far trailing matrix
+// (rows, columns >= Jend) then receives all of them at once, K = spw.
+//
+// Look-ahead: super-panels are factored on a high-priority side stream.
+// The far update of super-panel J runs on the caller's stream in two parts:
+// (a) the rows and columns of super-panel J + 1 (rows [Jend, Jn) x columns
+// >= Jend, and rows >= Jn x columns [Jend, Jn)), after which the side
+// stream may factor super-panel J + 1; (b) the rest, rows and columns >= Jn,
+// concurrently with it.  The two touch disjoint parts of W: the inner loop
+// of J + 1 writes rows < Jn or columns < Jn only.  Operands alternate between
+// two buffers, so (b) of J still reads its own while J + 1 writes the other.
+//
+// Inside a super-panel the panels are pipelined over two more high-priority
+// streams.  The chain stream (sa) runs, per panel p with columns
+// [jp, r1 = jp + 128): the diagonal-block LU; the panel solve of the next
+// panel's own block rows and columns [r1, nxt); the update of the next
+// diagonal block [r1, nxt)^2 by panel p; then the next diagonal LU.  The
+// strip stream (sb) runs the rest of panel p's solve (rows and columns >=
+// nxt) and its updates outside that diagonal block:
+//   rows [r1, nxt) x columns [nxt, n), rows [nxt, Jend) x columns [r1, n),
+//   rows [Jend, n) x columns [r1, Jend).
+// The chain stream waits for the strips of panel p - 1 before its solve of
+// panel p's next block (that solve reads rows and columns the strips
+// update), so the diagonal LU of panel p + 1 overlaps the strips of p.
+//
+// The schedule is data: lu_schedule lists every launch, event record and
+// event wait of one factorization in issue order, lu_factor_t executes the
+// list, and mpdok_lu_schedule exports it, so that a host-only check can verify
+// that every pair of launches touching the same data is ordered by the
+// streams and events.
+enum LuStream : int { LU_MAIN = 0, LU_CHAIN = 1, LU_STRIP = 2 };
+enum LuKind : int { LU_DIAG = 0, LU_SOLVE = 1, LU_UPDATE = 2, LU_RECORD = 3, LU_WAIT = 4, LU_PROF_START = 5,
+                    LU_PROF_STOP = 6 };
+enum LuEvent : int { LU_EV_READY = 0, LU_EV_PANEL = 1, LU_EV_A = 2, LU_EV_B = 3 };
+struct LuStep {
+  int kind = 0, stream = 0;
+  long long J = 0;           // super-panel start (operand buffer (J / spw) & 1)
+  long long jp = 0;          // DIAG, SOLVE: panel start
+  long long a = 0, b = 0;    // SOLVE: rows and columns [a, b); UPDATE: first C row and column
+  long long m = 0, nn = 0;   // UPDATE: C rows x columns (operand rows a.., b.. of L21, U12)
+  long long K = 0, koff = 0; // UPDATE: depth and first operand column (K-slot)
+  int rb = 0;                // SOLVE: rows per block
+  int event = 0;             // RECORD, WAIT: event; PROF_START, PROF_STOP: window
+  double work = 0.0;         // PROF_STOP: flops of the window
+};
+
+static std::vector<LuStep> lu_schedule(long long n, long long spw) {
+  std::vector<LuStep> v;
+  const bool lookahead = n > spw, split = n > LNB;
+  auto add = [&](int kind, int stream) {
+    LuStep st;
+    st.kind = kind;
+    st.stream = stream;
+    v.push_back(st);
+    return v.size() - 1;
+  };
+  auto record = [&](int stream, int ev) { v[add(LU_RECORD, stream)].event = ev; };
+  auto wait = [&](int stream, int ev) { v[add(LU_WAIT, stream)].event = ev; };
+  auto update = [&](int stream, long long J, long long koff, long long K, long long crow, long long ccol, long long m,
+                    long long nn) {
+    if (m <= 0 || nn <= 0) return;
+    LuStep& st = v[add(LU_UPDATE, stream)];
+    st.J = J;
+    st.koff = koff;
+    st.K = K;
+    st.a = crow;
+    st.b = ccol;
+    st.m = m;
+    st.nn = nn;
+  };
+  auto solve = [&](int stream, long long J, long long jp, long long begin, long long end, int rb) {
+    LuStep& st = v[add(LU_SOLVE, stream)];
+    st.J = J;
+    st.jp = jp;
+    st.a = begin;
+    st.b = end;
+    st.rb = rb;
+  };
+  auto prof = [&](int stream, int window, bool start, double work) {
+    LuStep& st = v[add(start ? LU_PROF_START : LU_PROF_STOP, stream)];
+    st.event = window;
+    st.work = work;
+  };
+  if (lookahead) {  // the chain stream starts after the scaling and the working copy
+    record(LU_MAIN, LU_EV_READY);
+    wait(LU_CHAIN, LU_EV_READY);
+  }
+  for (long long J = 0; J < n; J += spw) {
+    const long long Jend = std::min<long long>(n, J + spw);
+    const int sa = lookahead ? LU_CHAIN : LU_MAIN;
+    const int sb = split ? LU_STRIP : sa;
+    for (long long jp = J; jp < Jend; jp += LNB) {
+      const long long r1 = jp + LNB;                              // first row / column after the panel
+      const long long nxt = std::min<long long>(r1 + LNB, Jend);  // end of the next panel of J
+      const bool has_next = r1 < Jend;
+      const long long koff = jp - J;                              // the panel's K-slot in the operands
+      // chain: diagonal LU, then the next panel's own block rows / columns
+      prof(sa, 0, true, 0.0);
+      {
+        LuStep& st = v[add(LU_DIAG, sa)];
+        st.J = J;
+        st.jp = jp;
+      }
+      if (has_next) {
+        if (split && jp > J) wait(sa, LU_EV_B);  // strips of panel p - 1
+        solve(sa, J, jp, r1, nxt, 16);
+      }
+      prof(sa, 0, false, 2.0 * 2.0 * (double)(nxt - std::min(r1, nxt)) * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
+      if (split) record(sa, LU_EV_A);
+      if (has_next) update(sa, J, koff, LNB, r1, r1, nxt - r1, nxt - r1);
+      // strips: the rest of the panel solve and of panel p's updates
+      if (split) wait(sb, LU_EV_A);
+      const long long begin = has_next ? nxt : r1;
+      if (begin < n) {
+        prof(sb, 1, true, 0.0);
+        solve(sb, J, jp, begin, n, 64);
+        prof(sb, 1, false, 2.0 * 2.0 * (double)(n - begin) * LNB * LNB);
+      }
+      if (has_next) {
+        update(sb, J, koff, LNB, r1, nxt, nxt - r1, n - nxt);
+        update(sb, J, koff, LNB, nxt, r1, Jend - nxt, n - r1);
+        update(sb, J, koff, LNB, Jend, r1, n - Jend, Jend - r1);
+      }
+      if (split) record(sb, LU_EV_B);
+    }
+    if (split) wait(sa, LU_EV_B);  // join the strips
+    if (lookahead) {
+      record(LU_CHAIN, LU_EV_PANEL);
+      wait(LU_MAIN, LU_EV_PANEL);
+    }
+    if (Jend < n) {
+      const long long K = Jend - J;
+      if (!lookahead) {
+        update(LU_MAIN, J, 0, K, Jend, Jend, n - Jend, n - Jend);
+      } else {
+        const long long Jn = std::min<long long>(n, Jend + spw);
+        // (a) what super-panel J + 1 reads and writes first
+        update(LU_MAIN, J, 0, K, Jend, Jend, Jn - Jend, n - Jend);
+        update(LU_MAIN, J, 0, K, Jn, Jend, n - Jn, Jn - Jend);
+        record(LU_MAIN, LU_EV_READY);
+        wait(LU_CHAIN, LU_EV_READY);
+        // (b) the rest of the trailing matrix, concurrent with J + 1, in up to
+        // four column chunks: a kernel boundary on this stream drains the
+        // SMs, which lets the panel kernels (one of them needs a whole SM) in
+        // without waiting for the whole update
+        const long long rest = n - Jn;
+        const long long chunk = std::max<long long>(2048, (rest / 4 + 255) / 256 * 256);
+        for (long long c = Jn; c < n; c += chunk) update(LU_MAIN, J, 0, K, Jn, c, n - Jn, std::min(chunk, n - c));
+      }
+    }
+  }
+  if (lookahead) {  // the caller's stream owns the result
+    record(LU_CHAIN, LU_EV_PANEL);
+    wait(LU_MAIN, LU_EV_PANEL);
+  }
+  return v;
+}
+
 template <typename F>
 static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, int pivoting, void* fbuf,
                        void* work, cudaStream_t s, int* nperturb_host) {
@@ -1159,171 +1321,94 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     }
     return gemm_update(C, w.ldw, Ab, Bb, spw, (int)m, (int)nn, K, fdtype, MPDOK_ENGINE_TENSOR, errw, st);
   };
-  // Two-level right-looking LU.  Super-panel [J, Jend) of <= spw columns is
-  // factored with 128-wide panels whose updates are confined to the
-  // super-panel's row strip (rows < Jend, all columns right of the panel) and
-  // column strip (rows >= Jend, columns < Jend); the far trailing matrix
-  // (rows, columns >= Jend) then receives all of them at once, K = spw.
-  //
-  // Look-ahead: super-panels are factored on a high-priority side stream.
-  // The far update of super-panel J runs on the caller's stream in two parts:
-  // (a) the rows and columns of super-panel J + 1 (rows [Jend, Jn) x columns
-  // >= Jend, and rows >= Jn x columns [Jend, Jn)), after which the side
-  // stream may factor super-panel J + 1; (b) the rest, rows and columns >= Jn,
-  // concurrently with it.  The two touch disjoint parts of W: the inner loop
-  // of J + 1 writes rows < Jn or columns < Jn only.  Operands alternate between
-  // two buffers, so (b) of J still reads its own while J + 1 writes the other.
-  //
-  // Inside a super-panel the panels are pipelined over two more high-priority
-  // streams.  The chain stream (sa) runs, per panel p with columns
-  // [jp, r1 = jp + 128): the diagonal-block LU; the panel solve of the next
-  // panel's own block rows and columns [r1, nxt); the update of the next
-  // diagonal block [r1, nxt)^2 by panel p; then the next diagonal LU.  The
-  // strip stream (sb) runs the rest of panel p's solve (rows and columns >=
-  // nxt) and its updates outside that diagonal block:
-  //   rows [r1, nxt) x columns [nxt, n), rows [nxt, Jend) x columns [r1, n),
-  //   rows [Jend, n) x columns [r1, Jend).
-  // The chain stream waits for the strips of panel p - 1 before its solve of
-  // panel p's next block (that solve reads rows and columns the strips
-  // update), so the diagonal LU of panel p + 1 overlaps the strips of p.
+  const bool lookahead = n > spw;
+  const bool split = n > LNB;
   cudaStream_t side = nullptr, strip = nullptr;
-  cudaEvent_t ev_ready = nullptr, ev_panel = nullptr, ev_a = nullptr, ev_b = nullptr;
+  cudaEvent_t evs[4] = {nullptr, nullptr, nullptr, nullptr};
   auto cleanup = [&]() {
-    if (ev_ready) cudaEventDestroy(ev_ready);
-    if (ev_panel) cudaEventDestroy(ev_panel);
-    if (ev_a) cudaEventDestroy(ev_a);
-    if (ev_b) cudaEventDestroy(ev_b);
+    for (cudaEvent_t& e : evs)
+      if (e) cudaEventDestroy(e);
     if (side) cudaStreamDestroy(side);
     if (strip) cudaStreamDestroy(strip);
   };
-  const bool lookahead = n > spw;
-  const bool split = n > LNB;
   if (split) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     cudaError_t e = cudaStreamCreateWithPriority(&strip, cudaStreamNonBlocking, hi);
     if (e == cudaSuccess && lookahead) e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_panel, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_a, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_b, cudaEventDisableTiming);
+    for (cudaEvent_t& ev : evs)
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
       cleanup();
       return cuda_status(e, "lu look-ahead streams / events");
     }
-    if (lookahead) {
-      e = cudaEventRecord(ev_ready, s);  // scaling and the working copy are done
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev_ready, 0);
-      if (e != cudaSuccess) {
-        cleanup();
-        return cuda_status(e, "lu look-ahead start");
-      }
-    }
   }
+  const std::vector<LuStep> sched = lu_schedule(n, spw);
+  const cudaStream_t streams[3] = {s, side, strip};  // LU_MAIN, LU_CHAIN, LU_STRIP
+  int prof_window[2] = {-1, -1};
   auto body = [&]() -> int {
-    for (long long J = 0; J < n; J += spw) {
-      const long long Jend = std::min<long long>(n, J + spw);
-      const int buf = (int)((J / spw) & 1);
+    for (const LuStep& st : sched) {
+      if (st.stream != LU_MAIN && streams[st.stream] == nullptr) {
+        set_error("lu schedule: step on a stream that was not created");
+        return MPDOK_ERR_INVALID_ARG;
+      }
+      const cudaStream_t cs = streams[st.stream];
+      const int buf = (int)((st.J / spw) & 1);
       F* Lp = Lp2 + (size_t)buf * opsz;
       F* Up = Up2 + (size_t)buf * opsz;
-      cudaStream_t sa = lookahead ? side : s;
-      cudaStream_t sb = split ? strip : sa;
-      for (long long jp = J; jp < Jend; jp += LNB) {
-        const int k = (int)(jp / LNB);
-        const int p = (int)((jp - J) / LNB);
-        const int nbk = (int)std::min<long long>(LNB, n - jp);
-        const long long r1 = jp + LNB;                         // first row / column after the panel
-        const long long nxt = std::min<long long>(r1 + LNB, Jend);  // end of the next panel of J
-        const bool has_next = r1 < Jend;
-        const F* Lr = Lp + p * LNB;  // K-slot of panel p: row r of L21 at Lr + (r - J) * spw
-        const F* Uc = Up + p * LNB;  // column c of U12 at Uc + (c - J) * spw
-        // panel solve of rows / columns [begin, end): 16-row blocks for the
-        // next panel's own block (on the chain), 64-row blocks for the rest
-        auto solve = [&](long long begin, long long end, cudaStream_t st, bool next_block) {
+      switch (st.kind) {
+        case LU_DIAG: {
+          const int k = (int)(st.jp / LNB);
+          const int nbk = (int)std::min<long long>(LNB, n - st.jp);
+          launch(k_lu_diag<F>, 1, DIAG_THREADS, smem_diag, cs, W, w.ldw, st.jp, nbk, LU, L.ldf,
+                 Linv + (size_t)k * LNB * LNB, Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
+          MPDOK_LAUNCH_CHECK("lu diagonal block");
+          break;
+        }
+        case LU_SOLVE: {
+          const int k = (int)(st.jp / LNB);
+          const int koff = (int)(st.jp - st.J);
           const float* ui = Uinv + (size_t)k * LNB * LNB;
           const float* li = Linv + (size_t)k * LNB * LNB;
-          if (next_block) {
-            const int nb = (int)((end - begin + 15) / 16);
-            launch(k_trsm_pair<F, 16>, (unsigned)(2 * nb), TRSM_THREADS, smem_tp16, st, (const float*)W, w.ldw, jp,
-                   begin, end, ui, li, Lp, Up, spw, J, p * LNB, LU, L.ldf, nb);
+          if (st.rb == 16) {
+            const int nb = (int)((st.b - st.a + 15) / 16);
+            launch(k_trsm_pair<F, 16>, (unsigned)(2 * nb), TRSM_THREADS, smem_tp16, cs, (const float*)W, w.ldw, st.jp,
+                   st.a, st.b, ui, li, Lp, Up, spw, st.J, koff, LU, L.ldf, nb);
           } else {
-            const int nb = (int)((end - begin + 63) / 64);
-            launch(k_trsm_pair<F, 64>, (unsigned)(2 * nb), TRSM_THREADS, smem_tp, st, (const float*)W, w.ldw, jp,
-                   begin, end, ui, li, Lp, Up, spw, J, p * LNB, LU, L.ldf, nb);
+            const int nb = (int)((st.b - st.a + 63) / 64);
+            launch(k_trsm_pair<F, 64>, (unsigned)(2 * nb), TRSM_THREADS, smem_tp, cs, (const float*)W, w.ldw, st.jp,
+                   st.a, st.b, ui, li, Lp, Up, spw, st.J, koff, LU, L.ldf, nb);
           }
-        };
-        // chain: diagonal LU, then the next panel's own block rows / columns
-        const int ps = prof_start(MPDOK_PROF_LU_PANEL, sa);
-        launch(k_lu_diag<F>, 1, DIAG_THREADS, smem_diag, sa, W, w.ldw, jp, nbk, LU, L.ldf,
-               Linv + (size_t)k * LNB * LNB, Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
-        if (has_next) {
-          if (split && jp > J) MPDOK_CUDA_TRY(cudaStreamWaitEvent(sa, ev_b, 0));  // strips of panel p - 1
-          solve(r1, nxt, sa, true);
-        }
-        prof_stop(ps, sa, 2.0 * 2.0 * (double)(nxt - std::min(r1, nxt)) * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
-        MPDOK_LAUNCH_CHECK("lu panel");
-        if (split) MPDOK_CUDA_TRY(cudaEventRecord(ev_a, sa));
-        if (has_next)
-          MPDOK_TRY(update(r1, r1, nxt - r1, nxt - r1, Lr + (r1 - J) * spw, Uc + (r1 - J) * spw, LNB, sa));
-        // strips: the rest of the panel solve and of panel p's updates
-        if (split) MPDOK_CUDA_TRY(cudaStreamWaitEvent(sb, ev_a, 0));
-        const long long begin = has_next ? nxt : r1;
-        if (begin < n) {
-          const int ps2 = prof_start(MPDOK_PROF_LU_PANEL, sb);
-          solve(begin, n, sb, false);
-          prof_stop(ps2, sb, 2.0 * 2.0 * (double)(n - begin) * LNB * LNB);
           MPDOK_LAUNCH_CHECK("lu panel solve");
+          break;
         }
-        if (has_next) {
-          MPDOK_TRY(update(r1, nxt, nxt - r1, n - nxt, Lr + (r1 - J) * spw, Uc + (nxt - J) * spw, LNB, sb));
-          MPDOK_TRY(update(nxt, r1, Jend - nxt, n - r1, Lr + (nxt - J) * spw, Uc + (r1 - J) * spw, LNB, sb));
-          MPDOK_TRY(update(Jend, r1, n - Jend, Jend - r1, Lr + (Jend - J) * spw, Uc + (r1 - J) * spw, LNB, sb));
-        }
-        if (split) MPDOK_CUDA_TRY(cudaEventRecord(ev_b, sb));
-      }
-      if (split) MPDOK_CUDA_TRY(cudaStreamWaitEvent(sa, ev_b, 0));  // join the strips
-      if (lookahead) {
-        MPDOK_CUDA_TRY(cudaEventRecord(ev_panel, side));
-        MPDOK_CUDA_TRY(cudaStreamWaitEvent(s, ev_panel, 0));
-      }
-      if (Jend < n) {
-        const int K = (int)(Jend - J);
-        const F* La = Lp + (Jend - J) * spw;
-        const F* Ua = Up + (Jend - J) * spw;
-        if (!lookahead) {
-          MPDOK_TRY(update(Jend, Jend, n - Jend, n - Jend, La, Ua, K, s));
-        } else {
-          const long long Jn = std::min<long long>(n, Jend + spw);
-          // (a) what super-panel J + 1 reads and writes first
-          MPDOK_TRY(update(Jend, Jend, Jn - Jend, n - Jend, La, Ua, K, s));
-          MPDOK_TRY(update(Jn, Jend, n - Jn, Jn - Jend, Lp + (Jn - J) * spw, Ua, K, s));
-          MPDOK_CUDA_TRY(cudaEventRecord(ev_ready, s));
-          MPDOK_CUDA_TRY(cudaStreamWaitEvent(side, ev_ready, 0));
-          // (b) the rest of the trailing matrix, concurrent with J + 1, in up to
-          // four column chunks: a kernel boundary on this stream drains the
-          // SMs, which lets the side stream's panel kernels (one of them needs
-          // a whole SM) in without waiting for the whole update
-          const long long rest = n - Jn;
-          const long long chunk = std::max<long long>(2048, (rest / 4 + 255) / 256 * 256);
-          for (long long c = Jn; c < n; c += chunk) {
-            const long long w = std::min<long long>(chunk, n - c);
-            MPDOK_TRY(update(Jn, c, n - Jn, w, Lp + (Jn - J) * spw, Up + (c - J) * spw, K, s));
-          }
-        }
+        case LU_UPDATE:
+          MPDOK_TRY(update(st.a, st.b, st.m, st.nn, Lp + (st.a - st.J) * spw + st.koff,
+                           Up + (st.b - st.J) * spw + st.koff, (int)st.K, cs));
+          break;
+        case LU_RECORD:
+          MPDOK_CUDA_TRY(cudaEventRecord(evs[st.event], cs));
+          break;
+        case LU_WAIT:
+          MPDOK_CUDA_TRY(cudaStreamWaitEvent(cs, evs[st.event], 0));
+          break;
+        case LU_PROF_START:
+          prof_window[st.event] = prof_start(MPDOK_PROF_LU_PANEL, cs);
+          break;
+        case LU_PROF_STOP:
+          prof_stop(prof_window[st.event], cs, st.work);
+          break;
+        default:
+          set_error("lu schedule: unknown step");
+          return MPDOK_ERR_INVALID_ARG;
       }
     }
     return MPDOK_OK;
   };
   const int bst = body();
   if (split) {
-    // the caller's stream owns the result: join the side streams (the strip
-    // stream was joined into the chain stream after every super-panel)
-    if (bst == MPDOK_OK) {
-      if (lookahead) {
-        cudaEventRecord(ev_panel, side);
-        cudaStreamWaitEvent(s, ev_panel, 0);
-      }
-    } else {
+    // on an error the side streams may still hold work: let it finish first
+    if (bst != MPDOK_OK) {
       cudaStreamSynchronize(strip);
       if (side) cudaStreamSynchronize(side);
     }
@@ -1408,6 +1493,24 @@ extern "C" size_t mpdok_lu_work_size(long long n, int fdtype) {
 extern "C" size_t mpdok_lu_apply_work_size(long long n) {
   if (n < 0) return 0;
   return apply_layout(n).total;
+}
+
+extern "C" long long mpdok_lu_schedule(long long n, int fdtype, long long* out, long long max_steps) {
+  if (n < 0 || (fdtype != MPDOK_F32 && fdtype != MPDOK_BF16 && fdtype != MPDOK_F16)) {
+    set_error("invalid argument: mpdok_lu_schedule needs n >= 0 and an FP32 / BF16 / FP16 factor type");
+    return MPDOK_ERR_INVALID_ARG;
+  }
+  const std::vector<LuStep> v = lu_schedule(n, super_panel_width(fdtype));
+  if (out != nullptr) {
+    const long long cnt = std::min<long long>((long long)v.size(), std::max(0LL, max_steps));
+    for (long long i = 0; i < cnt; ++i) {
+      const LuStep& st = v[(size_t)i];
+      const long long row[12] = {st.kind, st.stream, st.J, st.jp, st.a, st.b, st.m, st.nn, st.K, st.koff, st.rb,
+                                 st.event};
+      for (int f = 0; f < 12; ++f) out[12 * i + f] = row[f];
+    }
+  }
+  return (long long)v.size();
 }
 
 extern "C" int mpdok_lu_factor(const double* A, long long lda, long long n, int fdtype, int pivoting, void* factors,
