@@ -676,12 +676,6 @@ __device__ __forceinline__ void tile_fma(const TileRegs<F>& T, const float* sx, 
   }
 }
 
-__device__ __forceinline__ int ld_acquire(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
 // Outputs of the triangular solves start as this bit pattern (a NaN that
 // GPU arithmetic never produces: generated NaNs are 0x7fffffff); a consumer
 // polls the values themselves instead of a separate ready flag.
