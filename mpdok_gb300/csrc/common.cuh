@@ -129,16 +129,6 @@ __device__ __forceinline__ void ordered_grid_sum(double v_block, double* parts, 
   }
 }
 
-// Bounded spin on a global word written by another block.  Returns true when
-// `*flag >= target`, false after `limit` polls (caller records a timeout).
-__device__ __forceinline__ bool spin_until_geq(const volatile int* flag, int target, long long limit) {
-  for (long long it = 0; it < limit; ++it) {
-    if (*flag >= target) return true;
-    __nanosleep(64);
-  }
-  return *flag >= target;
-}
-
 }  // namespace mpdok
 
 namespace mpdok {
