@@ -71,6 +71,21 @@ MPDOK_API int mpdok_version(void);
 MPDOK_API const char* mpdok_status_string(int status);
 /* Message of the last error raised on the calling host thread. */
 MPDOK_API const char* mpdok_last_error(void);
+/* Empty that message, so that a caller can tell whether the next call (for
+ * example a py_* entry point, which returns no status) raised an error. */
+MPDOK_API void mpdok_clear_error(void);
+
+/* Test hooks for the failure paths; no counterpart in the reference.
+ * MPDOK_DEBUG_WAIT_LIMIT: iteration limit of the triangular solves' bounded
+ *   waits on a predecessor block, on the current device (value <= 0 restores
+ *   the default).
+ * MPDOK_DEBUG_TRSV_FIRST_TICKET: first ticket that the next triangular solves
+ *   of this process hand out (0 = normal).  With a value above 0 no block ever
+ *   solves block 0, so the blocks that depend on it wait until their limit
+ *   runs out, return, and the solve reports MPDOK_ERR_TIMEOUT; the device
+ *   stays usable.  Returns a status. */
+enum { MPDOK_DEBUG_WAIT_LIMIT = 1, MPDOK_DEBUG_TRSV_FIRST_TICKET = 2 };
+MPDOK_API int mpdok_debug_set(int key, long long value);
 
 /* ------------------------------------------------------------ assembly
  * out(i, j) = phi(||rows_i - cols_j||) + reg * [i + diag_offset == j]
@@ -102,7 +117,9 @@ MPDOK_API int mpdok_gemv(int a_dtype, int trans, const void* A, long long lda, l
  * MPDOK_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the library until
  * the process exits; products that need more return MPDOK_ERR_INVALID_ARG.
  * The first call on a device looks up that array's device address (with the
- * device current), so make it before any stream capture.  All calls share
+ * device current), so make it before any stream capture.  The address is kept
+ * for the life of the process: after a cudaDeviceReset in the same process it
+ * is stale, so do not call this entry point again after a reset.  All calls share
  * the array: calls that overlap on the GPU (concurrent streams, or other host
  * threads) race on it and must be serialised by the caller.  Nothing is
  * allocated or freed. */

@@ -32,6 +32,7 @@ PROF_GEMV_F32, PROF_GEMV_F64, PROF_ASSEMBLE, PROF_LU_GEMM, PROF_TRSV, PROF_MATFR
 KERNEL_GAUSSIAN, KERNEL_MQ = 0, 1
 ENGINE_TENSOR, ENGINE_SIMT = 0, 1
 HISTORY_MAX = 256
+DEBUG_WAIT_LIMIT, DEBUG_TRSV_FIRST_TICKET = 1, 2
 NOALLOC_SCRATCH_BYTES = 16 << 20
 
 c_void_p = ctypes.c_void_p
@@ -74,6 +75,8 @@ _SIGS = {
     "mpdok_version": (c_int, []),
     "mpdok_status_string": (ctypes.c_char_p, [c_int]),
     "mpdok_last_error": (ctypes.c_char_p, []),
+    "mpdok_clear_error": (None, []),
+    "mpdok_debug_set": (c_int, [c_int, c_ll]),
     "mpdok_rbf_assemble": (c_int, [c_void_p, c_ll, c_void_p, c_ll, c_int, c_int, c_double, c_double, c_ll,
                                    c_int, c_void_p, c_ll, c_int, c_void_p]),
     "mpdok_convert": (c_int, [c_void_p, c_int, c_void_p, c_int, c_ll, c_void_p]),
@@ -214,6 +217,24 @@ def declared_symbols() -> list[str]:
 
 def last_error() -> str:
     msg = load().mpdok_last_error()
+    return msg.decode(errors="replace") if msg else ""
+
+
+def debug_set(key: int, value: int) -> None:
+    """Failure-path test hooks (DEBUG_WAIT_LIMIT, DEBUG_TRSV_FIRST_TICKET); see the header."""
+    check(int(load().mpdok_debug_set(int(key), int(value))), "debug_set")
+
+
+def call_error(lib) -> str:
+    """The library's error message for the call just made (empty when it raised none).
+
+    The reference-compatible py_* entry points return no status, so callers
+    clear the message before the call (``lib.mpdok_clear_error()``) and read it
+    afterwards to tell an error from plain non-convergence."""
+    fn = getattr(lib, "mpdok_last_error", None)
+    if fn is None:
+        return ""
+    msg = fn()
     return msg.decode(errors="replace") if msg else ""
 
 

@@ -120,6 +120,7 @@ extern "C" int mpdok_mf_cg_ir(const double* coords, long long n, int dim, int ke
   c.w32_bytes = matfree_work_bytes(n, n, nrhs, MPDOK_F32);
   c.w64 = base + align_up(c.w32_bytes, 256);
   c.w64_bytes = matfree_work_bytes(n, n, nrhs, MPDOK_F64);
-  return cg_ir_core(w, mf_op32(&c), mf_res64(&c), B, ldb, X, ldx, tol, maxiter_outer, inner_tol, inner_maxiter, nullptr,
-                    info, s);
+  MPDOK_TRY(mf_timeout_clear(&c, s));
+  return mf_timeout_finish(&c, cg_ir_core(w, mf_op32(&c), mf_res64(&c), B, ldb, X, ldx, tol, maxiter_outer, inner_tol,
+                                          inner_maxiter, nullptr, info, s), s);
 }

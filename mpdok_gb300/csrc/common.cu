@@ -4,7 +4,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <utility>
 
 namespace mpdok {
 
@@ -35,6 +37,19 @@ int num_sms() {
     cache[dev] = v;
   }
   return cache[dev];
+}
+
+int smem_attr(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  MPDOK_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& have = done[{func, dev}];
+  if (have >= bytes) return MPDOK_OK;
+  MPDOK_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  have = bytes;
+  return MPDOK_OK;
 }
 
 template <typename S, typename D>
@@ -122,6 +137,8 @@ using namespace mpdok;
 extern "C" int mpdok_version(void) { return 10000; }
 
 extern "C" const char* mpdok_last_error(void) { return g_last_error; }
+
+extern "C" void mpdok_clear_error(void) { g_last_error[0] = '\0'; }
 
 extern "C" const char* mpdok_status_string(int s) {
   switch (s) {

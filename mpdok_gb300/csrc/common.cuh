@@ -50,6 +50,13 @@ int cuda_status(cudaError_t e, const char* where);
   } while (0)
 
 int num_sms();             // SM count of the current device (cached per device)
+// Raise a kernel's dynamic shared-memory limit to `bytes` on the current
+// device.  The attribute is per device, so the set is remembered per (kernel,
+// device) under a lock: a second GPU in the same process, or two host threads
+// making their first calls together, each get it set before their launch.
+int smem_attr(const void* func, size_t bytes);
+template <typename K>
+inline int set_smem(K* kern, size_t bytes) { return smem_attr(reinterpret_cast<const void*>(kern), bytes); }
 int convert_any(const void* src, int sdt, void* dst, int ddt, long long n, cudaStream_t s);
 int convert_matrix_f64_f32(const double* src, long long lds, float* dst, long long ldd, long long m, long long n,
                            cudaStream_t s);

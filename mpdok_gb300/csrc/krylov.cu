@@ -758,6 +758,10 @@ static int host_bnorm(const KWs& ws, const double* b, double* bnorm, cudaStream_
   KScal hs;
   MPDOK_TRY(read_scal(ws, &hs, s));
   *bnorm = std::sqrt(hs.aux);
+  if (!std::isfinite(*bnorm)) {
+    set_error("the right-hand side has non-finite entries");
+    return MPDOK_ERR_NONFINITE;
+  }
   return MPDOK_OK;
 }
 
@@ -822,6 +826,10 @@ int gmres_ir_core(const KWs& ws, const Operator32& A, const Residual64& R, const
   const double bnorm = std::sqrt(h0.aux);
   const bool x_zero = h0.alpha == 0.0;
   if (info) info->bnorm = bnorm;
+  if (!std::isfinite(bnorm) || !std::isfinite(h0.alpha)) {
+    set_error("GMRES-IR: the right-hand side or the initial guess has non-finite entries");
+    return MPDOK_ERR_NONFINITE;
+  }
   if (bnorm == 0.0) {
     MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
     hist_push(info, 0, 0.0);
@@ -1041,7 +1049,13 @@ int cg_ir_core(const CgIrWs& w, const Operator32& A, const Residual64& R, const 
   std::vector<double> bn(K), rn(K);
   MPDOK_CUDA_TRY(cudaMemcpyAsync(bn.data(), w.nrm2, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
   MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
-  for (int j = 0; j < K; ++j) bn[j] = std::sqrt(bn[j]);  // colnorms_f64 returns squared norms
+  for (int j = 0; j < K; ++j) {
+    bn[j] = std::sqrt(bn[j]);  // colnorms_f64 returns squared norms
+    if (!std::isfinite(bn[j])) {
+      set_error("CG-IR: right-hand side %d has non-finite entries", j);
+      return MPDOK_ERR_NONFINITE;
+    }
+  }
   if (info) info->bnorm = *std::max_element(bn.begin(), bn.end());
   bool converged = false;
   int inner_total = 0;

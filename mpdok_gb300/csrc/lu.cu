@@ -689,9 +689,14 @@ __device__ __forceinline__ float ld_relaxed_f(const float* p) {
 __device__ __forceinline__ void st_relaxed_f(float* p, float x) {
   asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(__float_as_uint(x)) : "memory");
 }
+// Iteration limit of the triangular solves' waits on a predecessor block.  A
+// device variable so that a test can shorten it (mpdok_debug_set).
+__device__ long long g_spin_limit = SPIN_LIMIT;
+
 // Spin until out[i] holds a value; false when the limit ran out.
 __device__ __forceinline__ bool wait_value(const float* p, float& v) {
-  for (long long it = 0; it < SPIN_LIMIT; ++it) {
+  const long long limit = g_spin_limit;
+  for (long long it = 0; it < limit; ++it) {
     v = ld_relaxed_f(p);
     if (__float_as_uint(v) != TRSV_EMPTY) return true;
     if (it > 256) __nanosleep(32);
@@ -1026,6 +1031,41 @@ __global__ void k_scale_out_multi(const float* __restrict__ z, const float* __re
 
 // ---------------------------------------------------------------- host side
 
+// First ticket of the next triangular solves; 0 except under a test hook
+// (mpdok_debug_set), which raises it so that no block ever solves block 0.
+static int g_first_ticket = 0;
+
+static int reset_tickets(int* tk, cudaStream_t s) {
+  MPDOK_CUDA_TRY(cudaMemsetAsync(tk, 0, sizeof(int) * 2, s));
+  if (g_first_ticket != 0) {
+    const int t0 = g_first_ticket;
+    MPDOK_CUDA_TRY(cudaMemcpyAsync(tk, &t0, sizeof(int), cudaMemcpyHostToDevice, s));
+    MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  return MPDOK_OK;
+}
+
+// The triangular solves report a wait that ran out through an error word in
+// their workspace.  A solve clears it once at its start and reads it when it
+// ends: a timed-out block leaves its outputs unset (NaN), which the solve
+// would otherwise report as a non-finite residual or a stalled iteration.
+static int err_clear(int* err, cudaStream_t s) {
+  MPDOK_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int) * 4, s));
+  return MPDOK_OK;
+}
+
+static int err_finish(const int* err, int status, cudaStream_t s) {
+  if (status == MPDOK_ERR_CUDA || status == MPDOK_ERR_ALLOC) return status;
+  int h = 0;
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h != 0) {
+    set_error("triangular solve: a block's wait on its predecessor ran out (device wait limit)");
+    return MPDOK_ERR_TIMEOUT;
+  }
+  return status;
+}
+
 static unsigned grid_for(long long n, int per = 256) {
   long long b = (n + per - 1) / per;
   return (unsigned)std::max(1LL, std::min(b, (long long)num_sms() * 8));
@@ -1067,15 +1107,11 @@ static int lu_apply_t(const void* fbuf, long long n, int fdtype, const float* v,
   // outputs start empty (TRSV_EMPTY in every word): the solves poll them
   MPDOK_CUDA_TRY(cudaMemsetAsync(y, 0xff, sizeof(float) * n, s));
   MPDOK_CUDA_TRY(cudaMemsetAsync(zz, 0xff, sizeof(float) * n, s));
-  MPDOK_CUDA_TRY(cudaMemsetAsync(tk, 0, sizeof(int) * 2, s));
+  MPDOK_TRY(reset_tickets(tk, s));
   const int slot = prof_start(MPDOK_PROF_TRSV, s);
   const size_t smem = (size_t)LNB * LNB * sizeof(float);
-  static bool attr = false;
-  if (!attr) {
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv<F, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv<F, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  MPDOK_TRY(set_smem(k_trsv<F, true>, smem));
+  MPDOK_TRY(set_smem(k_trsv<F, false>, smem));
   launch(k_trsv<F, true>, L.nblk, 256, smem, s, LU, L.ldf, Linv, Ml, n, L.nblk, v, d, y, tk, err, skip);
   launch(k_trsv<F, false>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, Mu, n, L.nblk, (const float*)y, d, zz, tk + 1,
          err, skip);
@@ -1284,19 +1320,9 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
 
   const size_t smem_diag = DIAG_SMEM;
   constexpr size_t smem_tp = trsm_pair_smem(64), smem_tp16 = trsm_pair_smem(16);
-  static bool attrs = false;
-  if (!attrs) {
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diag));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__nv_bfloat16, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__half, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<float, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__nv_bfloat16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp16));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<__half, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp16));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsm_pair<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tp16));
-    attrs = true;
-  }
+  MPDOK_TRY(set_smem(k_lu_diag<F>, smem_diag));
+  MPDOK_TRY(set_smem(k_trsm_pair<F, 64>, smem_tp));
+  MPDOK_TRY(set_smem(k_trsm_pair<F, 16>, smem_tp16));
   const float tau = 1e-6f;
   // C -= A B^T on one strip: A rows / B rows at the given Lp / Up offsets.
   auto update = [&](long long crow, long long ccol, long long m, long long nn, const F* Ab, const F* Bb, int K,
@@ -1411,12 +1437,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   if (bst < 0) return bst;
   {
     const size_t smem_ct = 2 * (size_t)LNB * LNB * sizeof(float);
-    static bool attr_ct = false;
-    if (!attr_ct) {
-      MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv_chain_tiles<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem_ct));
-      attr_ct = true;
-    }
+    MPDOK_TRY(set_smem(k_trsv_chain_tiles<F>, smem_ct));
     launch(k_trsv_chain_tiles<F>, dim3(L.nblk, 2), 256, smem_ct, s, (const F*)LU, L.ldf, (const float*)Linv,
            (const float*)Uinv, (float*)(fb + L.off_ml), (float*)(fb + L.off_mu), n, L.nblk);
     MPDOK_LAUNCH_CHECK("lu chain tiles");
@@ -1473,6 +1494,23 @@ __global__ void k_add_f32_to_f64(const float* __restrict__ e, double* __restrict
 }  // namespace mpdok
 
 using namespace mpdok;
+
+extern "C" int mpdok_debug_set(int key, long long value) {
+  switch (key) {
+    case MPDOK_DEBUG_WAIT_LIMIT: {
+      const long long v = value > 0 ? value : SPIN_LIMIT;
+      MPDOK_CUDA_TRY(cudaMemcpyToSymbol(g_spin_limit, &v, sizeof(v)));
+      return MPDOK_OK;
+    }
+    case MPDOK_DEBUG_TRSV_FIRST_TICKET:
+      MPDOK_ARG_CHECK(value >= 0 && value < (1LL << 30), "first ticket out of range");
+      g_first_ticket = (int)value;
+      return MPDOK_OK;
+    default:
+      set_error("invalid argument: unknown debug key %d", key);
+      return MPDOK_ERR_INVALID_ARG;
+  }
+}
 
 extern "C" size_t mpdok_lu_factor_size(long long n, int fdtype) {
   if (n < 0) return 0;
@@ -1535,13 +1573,18 @@ extern "C" int mpdok_lu_apply(const void* factors, long long n, int fdtype, cons
   if (n == 0) return MPDOK_OK;
   MPDOK_ARG_CHECK(factors && v && z && work, "null pointer");
   MPDOK_ARG_CHECK(work_bytes >= apply_layout(n).total, "apply work buffer too small");
-  return lu_apply_any(factors, n, fdtype, v, z, work, s, nullptr);
+  int* err = (int*)((char*)work + apply_layout(n).off_err);
+  MPDOK_TRY(err_clear(err, s));
+  return err_finish(err, lu_apply_any(factors, n, fdtype, v, z, work, s, nullptr), s);
 }
 
 extern "C" size_t mpdok_lu_ir_work_size(long long n) {
   if (n < 0) return 0;
   return apply_layout(n).total + krylov_layout(n, 1, nullptr).total + 256;
 }
+
+static int lu_ir_body(const double* A, long long lda, long long n, const void* factors, int fdtype, const double* b,
+                      double* x, double tol, int maxiter_outer, char* wb, mpdok_solve_info* info, cudaStream_t s);
 
 extern "C" int mpdok_lu_ir_solve(const double* A, long long lda, long long n, const void* factors, int fdtype,
                                  const double* b, double* x, double tol, int maxiter_outer, void* work,
@@ -1557,8 +1600,15 @@ extern "C" int mpdok_lu_ir_solve(const double* A, long long lda, long long n, co
     set_error("no factorization of this size / type in the factor buffer");
     return MPDOK_ERR_NOT_FACTORED;
   }
-  const ApplyWork aw = apply_layout(n);
   char* wb = (char*)work;
+  int* aerr = (int*)(wb + apply_layout(n).off_err);
+  MPDOK_TRY(err_clear(aerr, s));
+  return err_finish(aerr, lu_ir_body(A, lda, n, factors, fdtype, b, x, tol, maxiter_outer, wb, info, s), s);
+}
+
+static int lu_ir_body(const double* A, long long lda, long long n, const void* factors, int fdtype, const double* b,
+                      double* x, double tol, int maxiter_outer, char* wb, mpdok_solve_info* info, cudaStream_t s) {
+  const ApplyWork aw = apply_layout(n);
   void* awork = wb;
   KWs ws = krylov_layout(n, 1, wb + align_up(aw.total, 256));
   MPDOK_CUDA_TRY(cudaMemsetAsync(ws.tickets, 0, sizeof(unsigned) * 8, s));
@@ -1571,6 +1621,10 @@ extern "C" int mpdok_lu_ir_solve(const double* A, long long lda, long long n, co
   MPDOK_TRY(read_scal(ws, &hs, s));
   const double bnorm = std::sqrt(hs.aux);
   if (info) info->bnorm = bnorm;
+  if (!std::isfinite(bnorm)) {
+    set_error("LU-IR: the right-hand side has non-finite entries");
+    return MPDOK_ERR_NONFINITE;
+  }
   if (bnorm == 0.0) {
     MPDOK_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
     if (info) { info->converged = 1; info->n_history = 1; info->history[0] = 0.0; }
@@ -1658,14 +1712,10 @@ static int lu_apply_multi_t(const void* fbuf, long long n, int fdtype, const flo
   int* err = (int*)(wb + mw.off_err);
   MPDOK_CUDA_TRY(cudaMemsetAsync(y, 0xff, sizeof(float) * n * K, s));
   MPDOK_CUDA_TRY(cudaMemsetAsync(zz, 0xff, sizeof(float) * n * K, s));
-  MPDOK_CUDA_TRY(cudaMemsetAsync(tk, 0, sizeof(int) * 2, s));
+  MPDOK_TRY(reset_tickets(tk, s));
   const size_t smem = (size_t)LNB * LNB * sizeof(float);
-  static bool attr = false;
-  if (!attr) {
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv_multi<F, true, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(k_trsv_multi<F, false, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  MPDOK_TRY(set_smem(k_trsv_multi<F, true, K>, smem));
+  MPDOK_TRY(set_smem(k_trsv_multi<F, false, K>, smem));
   const int slot = prof_start(MPDOK_PROF_TRSV, s);
   launch(k_trsv_multi<F, true, K>, L.nblk, 256, smem, s, LU, L.ldf, Linv, Ml, n, L.nblk, v, n, d, y, tk, err);
   launch(k_trsv_multi<F, false, K>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, Mu, n, L.nblk, (const float*)y, n, d, zz,
@@ -1746,6 +1796,9 @@ extern "C" int mpdok_lu_ir_solve_multi(const double* A, long long lda, long long
   }
   const MultiWork mw = multi_layout(n, nrhs);
   char* wb = (char*)work;
+  int* merr = (int*)(wb + mw.off_err);
+  MPDOK_TRY(err_clear(merr, s));
+  auto body = [&]() -> int {
   float* v32 = (float*)(wb + mw.off_v);  // FP32 right-hand sides in, corrections out (in place)
   double* R = (double*)(wb + mw.off_r);
   double* nrm = (double*)(wb + mw.off_nrm);
@@ -1756,7 +1809,13 @@ extern "C" int mpdok_lu_ir_solve_multi(const double* A, long long lda, long long
   MPDOK_TRY(colnorms_f64(B, n, nrhs, ldb, nrm, s));
   MPDOK_CUDA_TRY(cudaMemcpyAsync(bn.data(), nrm, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
   MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
-  for (int k = 0; k < nrhs; ++k) bn[k] = std::sqrt(bn[k]);
+  for (int k = 0; k < nrhs; ++k) {
+    bn[k] = std::sqrt(bn[k]);
+    if (!std::isfinite(bn[k])) {
+      set_error("multi-RHS LU-IR: right-hand side %d has non-finite entries", k);
+      return MPDOK_ERR_NONFINITE;
+    }
+  }
   if (info) info->bnorm = *std::max_element(bn.begin(), bn.end());
   const unsigned g = grid_for(n * nrhs);
   launch(k_f64_to_f32_cols, g, 256, 0, s, B, ldb, v32, n, nrhs);
@@ -1795,6 +1854,8 @@ extern "C" int mpdok_lu_ir_solve_multi(const double* A, long long lda, long long
   }
   MPDOK_LAUNCH_CHECK("lu_ir multi");
   return MPDOK_OK;
+  };
+  return err_finish(merr, body(), s);
 }
 
 extern "C" size_t mpdok_lu_gmres_ir_work_size(long long n, int restart) {
@@ -1821,6 +1882,8 @@ extern "C" int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* 
   }
   char* wb = (char*)work;
   const size_t a_bytes = align_up(apply_layout(n).total, 256);
+  int* aerr = (int*)(wb + apply_layout(n).off_err);
+  MPDOK_TRY(err_clear(aerr, s));
   PcCtx ctx{factors, n, fdtype, wb};
   Precond pc;
   pc.apply = pc_apply;
@@ -1840,8 +1903,8 @@ extern "C" int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* 
   // the mixed solve is guarded: on a singular or badly scaled system it returns
   // the best iterate with info->stagnated = 2 instead of diverging
   double* xbest = (double*)(wb + a_bytes + align_up((size_t)n * sizeof(float), 256) + align_up(ws.total, 256));
-  return gmres_ir_core(ws, stored_op32(&c), stored_res64(&c), b, x, tol, maxiter_outer, restart, inner_tol, &pc, info,
-                       s, xbest);
+  return err_finish(aerr, gmres_ir_core(ws, stored_op32(&c), stored_res64(&c), b, x, tol, maxiter_outer, restart,
+                                        inner_tol, &pc, info, s, xbest), s);
 }
 
 // --------------------------------------------------- LU-preconditioned CG-IR
@@ -1877,7 +1940,10 @@ static int lu_cg_ir_run(const Operator32& A, const Residual64& R, long long n, c
   Precond pc;
   pc.apply = pc_apply;
   pc.ctx = &ctx;
-  return cg_ir_core(w, A, R, B, ldb, X, ldx, tol, maxiter_outer, inner_tol, inner_maxiter, &pc, info, s);
+  int* aerr = (int*)(awork + apply_layout(n).off_err);
+  MPDOK_TRY(err_clear(aerr, s));
+  return err_finish(aerr, cg_ir_core(w, A, R, B, ldb, X, ldx, tol, maxiter_outer, inner_tol, inner_maxiter, &pc, info, s),
+                    s);
 }
 
 extern "C" int mpdok_lu_cg_ir(const double* A64, long long lda, long long n, int op_mode, void* opbuf, int op_ready,
@@ -1953,6 +2019,7 @@ extern "C" int mpdok_mf_lu_cg_ir(const double* coords, long long n, int dim, int
   c.w32_bytes = matfree_work_bytes(n, n, nrhs, MPDOK_F32);
   c.w64 = base + align_up(c.w32_bytes, 256);
   c.w64_bytes = matfree_work_bytes(n, n, nrhs, MPDOK_F64);
-  return lu_cg_ir_run(mf_op32(&c), mf_res64(&c), n, factors, fdtype, nrhs, B, ldb, X, ldx, tol, maxiter_outer,
-                      inner_tol, inner_maxiter, wb, w, info, s);
+  MPDOK_TRY(mf_timeout_clear(&c, s));
+  return mf_timeout_finish(&c, lu_cg_ir_run(mf_op32(&c), mf_res64(&c), n, factors, fdtype, nrhs, B, ldb, X, ldx, tol,
+                                            maxiter_outer, inner_tol, inner_maxiter, wb, w, info, s), s);
 }

@@ -211,12 +211,22 @@ k_matfree_f64(const double* __restrict__ rows, const double* __restrict__ cols, 
 
 // y = alpha * sum_s P + beta * y + reg * x_shift ; FP32 or FP64; optional
 // per-column sum of squares (residual mode: alpha = -1, y preloaded with b).
+// A timed-out evaluation (err[0] set by k_matfree_f32) leaves its partial
+// sums unwritten: the product is then NaN, not a silently wrong number, and
+// the sticky word err[1] tells the solve that owns this workspace why.
 template <typename T>
 __global__ void __launch_bounds__(MF_THREADS)
 k_mf_finalize(const T* __restrict__ P, int S, int K, long long nrows, T alpha, T beta, const T* bsrc, long long ldb,
-              T reg, const T* xs, long long ldx, T* y, long long ldy, const int* skip) {
+              T reg, const T* xs, long long ldx, T* y, long long ldy, const int* skip, int* err) {
   if (skip != nullptr && *skip) return;
   const long long total = nrows * K;
+  if (err != nullptr && *(volatile int*)err != 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(err + 1, 1);
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x)
+      y[idx % nrows + (idx / nrows) * ldy] = T(NAN);
+    return;
+  }
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * blockDim.x) {
     const long long i = idx % nrows;
@@ -289,10 +299,15 @@ static MfPlan mf_plan(long long nrows, long long ncols, int K, bool f64) {
   return p;
 }
 
+// Workspace: [0, 256) status words (err[0] of the last FP32 evaluation, err[1]
+// sticky for the solve), then the split partial sums, then (FP32) the packed
+// row and column centres.
+constexpr size_t MF_STATUS = 256;
+
 size_t matfree_work_bytes(long long nrows, long long ncols, int nrhs, int precision) {
   const bool f64 = precision == MPDOK_F64;
   const MfPlan p = mf_plan(nrows, ncols, nrhs, f64);
-  size_t b = p.part_bytes + 256;
+  size_t b = p.part_bytes + MF_STATUS;
   if (!f64) b += align_up((size_t)std::max(1LL, nrows) * 16, 256) + align_up((size_t)std::max(1LL, ncols) * 16, 256);
   return b;
 }
@@ -320,7 +335,8 @@ int matfree_apply(const MfOperand& op, int precision, const void* X, long long l
   MPDOK_ARG_CHECK(!has_reg || (op.diag_offset >= 0 && op.diag_offset + nr <= nc),
                   "nugget needs rows [0, n_rows) to map inside the columns");
   char* w = (char*)work;
-  void* P = w;
+  int* err = (int*)w;
+  void* P = w + MF_STATUS;
   MPDOK_ARG_CHECK(!f64 || skip == nullptr, "FP64 evaluation is not predicated");
   const int slot = prof_start(MPDOK_PROF_MATFREE, s);
   if (nc == 0) {
@@ -335,7 +351,7 @@ int matfree_apply(const MfOperand& op, int precision, const void* X, long long l
              op.gamma, (const double*)X, ldx, K, (double*)P);
   } else {
     MPDOK_ARG_CHECK(aligned16(X) && (ldx * 4) % 16 == 0, "FP32 X must be 16-byte aligned with ldx % 4 == 0");
-    float4* rp = (float4*)(w + p.part_bytes + 256);
+    float4* rp = (float4*)(w + MF_STATUS + p.part_bytes);
     float4* cp = (float4*)((char*)rp + align_up((size_t)nr * 16, 256));
     const float4* rows_p = op.rows_packed;
     const float4* cols_p = op.cols_packed;
@@ -351,7 +367,7 @@ int matfree_apply(const MfOperand& op, int precision, const void* X, long long l
     MPDOK_TRY(map2d_f32(&mc, cols_p, 4, nc, 16, 4, MF_BC));
     MPDOK_TRY(map2d_f32(&mx, X, nc, K, ldx * 4, MF_BC, K));
     const float g = (op.kernel == MPDOK_KERNEL_GAUSSIAN) ? (float)(-op.gamma * 1.4426950408889634) : (float)op.gamma;
-    int* err = (int*)(w + p.part_bytes);
+    MPDOK_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
 #define MF_CASE(KK)                                                                                           \
   case KK:                                                                                                    \
     if (op.kernel == MPDOK_KERNEL_GAUSSIAN)                                                                   \
@@ -370,11 +386,11 @@ int matfree_apply(const MfOperand& op, int precision, const void* X, long long l
   if (f64)
     launch(k_mf_finalize<double>, fb, MF_THREADS, 0, s, (const double*)P, p.S, K, nr, alpha, beta,
            (const double*)Bsrc, ldb, op.reg, has_reg ? (const double*)X + op.diag_offset : (const double*)nullptr, ldx,
-           (double*)Y, ldy, (const int*)nullptr);
+           (double*)Y, ldy, (const int*)nullptr, (int*)nullptr);
   else
     launch(k_mf_finalize<float>, fb, MF_THREADS, 0, s, (const float*)P, p.S, K, nr, (float)alpha, (float)beta,
            (const float*)Bsrc, ldb, (float)op.reg, has_reg ? (const float*)X + op.diag_offset : (const float*)nullptr,
-           ldx, (float*)Y, ldy, skip);
+           ldx, (float*)Y, ldy, skip, nc == 0 ? (int*)nullptr : err);
   MPDOK_LAUNCH_CHECK("matfree finalize");
   return MPDOK_OK;
 }
@@ -392,6 +408,23 @@ static int mf_residual64(const void* ctx, const double* b, const double* x, doub
   const MfCtx* c = (const MfCtx*)ctx;
   MPDOK_TRY(matfree_apply(c->op, MPDOK_F64, x, ld, nrhs, r, ld, -1.0, 1.0, b, ld, c->w64, c->w64_bytes, s, nullptr));
   return colnorms_f64(r, c->op.nrows, nrhs, ld, nrm2, s);
+}
+
+int mf_timeout_clear(const MfCtx* c, cudaStream_t s) {
+  MPDOK_CUDA_TRY(cudaMemsetAsync(c->w32, 0, 2 * sizeof(int), s));
+  return MPDOK_OK;
+}
+
+int mf_timeout_finish(const MfCtx* c, int status, cudaStream_t s) {
+  if (status == MPDOK_ERR_CUDA || status == MPDOK_ERR_ALLOC) return status;
+  int h = 0;
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(&h, (const int*)c->w32 + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h != 0) {
+    set_error("matrix-free product: a wait on a staged centre tile ran out (device wait limit)");
+    return MPDOK_ERR_TIMEOUT;
+  }
+  return status;
 }
 
 Operator32 mf_op32(const MfCtx* c) {
@@ -467,7 +500,7 @@ static int mf_setup(const double* coords, long long n, int dim, int kernel, doub
   c->w64_bytes = matfree_work_bytes(n, n, 8, MPDOK_F64);
   // pack the centres once for every FP32 apply of the solve
   const MfPlan p = mf_plan(n, n, 8, false);
-  float4* rp = (float4*)(w + p.part_bytes + 256);
+  float4* rp = (float4*)(w + MF_STATUS + p.part_bytes);
   launch(k_pack_coords, (unsigned)std::min<long long>((n + 255) / 256, 1024), 256, 0, s, coords, n, dim, rp);
   MPDOK_LAUNCH_CHECK("pack");
   c->op.rows_packed = rp;
@@ -487,7 +520,9 @@ extern "C" int mpdok_mf_gmres_ir(const double* coords, long long n, int dim, int
   KWs ws;
   MfCtx c;
   MPDOK_TRY(mf_setup(coords, n, dim, kernel, gamma, reg, restart, work, work_bytes, &ws, &c, s));
-  return gmres_ir_core(ws, mf_op32(&c), mf_res64(&c), b, x, tol, maxiter_outer, restart, inner_tol, nullptr, info, s);
+  MPDOK_TRY(mf_timeout_clear(&c, s));
+  return mf_timeout_finish(&c, gmres_ir_core(ws, mf_op32(&c), mf_res64(&c), b, x, tol, maxiter_outer, restart,
+                                             inner_tol, nullptr, info, s), s);
 }
 
 extern "C" int mpdok_mf_cg(const double* coords, long long n, int dim, int kernel, double gamma, double reg,
@@ -501,5 +536,6 @@ extern "C" int mpdok_mf_cg(const double* coords, long long n, int dim, int kerne
   KWs ws;
   MfCtx c;
   MPDOK_TRY(mf_setup(coords, n, dim, kernel, gamma, reg, 1, work, work_bytes, &ws, &c, s));
-  return cg_core(ws, mf_op32(&c), mf_res64(&c), b, x, tol, maxiter, check_every, info, s);
+  MPDOK_TRY(mf_timeout_clear(&c, s));
+  return mf_timeout_finish(&c, cg_core(ws, mf_op32(&c), mf_res64(&c), b, x, tol, maxiter, check_every, info, s), s);
 }

@@ -30,6 +30,11 @@ size_t matfree_work_bytes(long long nrows, long long ncols, int nrhs, int precis
 int matfree_apply(const MfOperand& op, int precision, const void* X, long long ldx, int K, void* Y, long long ldy,
                   double alpha, double beta, const void* Bsrc, long long ldb, void* work, size_t work_bytes,
                   cudaStream_t s, const int* skip);
+// The FP32 evaluation's bounded TMA waits report through a status word in
+// the FP32 workspace: a solve clears it at its start (mf_timeout_clear) and,
+// when it ends, turns a set word into MPDOK_ERR_TIMEOUT (mf_timeout_finish).
+int mf_timeout_clear(const MfCtx* c, cudaStream_t s);
+int mf_timeout_finish(const MfCtx* c, int status, cudaStream_t s);
 Operator32 mf_op32(const MfCtx* c);
 Residual64 mf_res64(const MfCtx* c);
 

@@ -341,12 +341,7 @@ constexpr int TC_STAGES = 2;
 static int launch_tc(const CUtensorMap& ma, const CUtensorMap& mb, float* C, long long ldc, int M, int N, int K,
                      int bf16, int* err, cudaStream_t s) {
   using S = tc::Smem<TC_STAGES>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    MPDOK_CUDA_TRY(cudaFuncSetAttribute(tc::tc_gemm_update<TC_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        S::ALLOC));
-    attr_set = true;
-  }
+  MPDOK_TRY(set_smem(tc::tc_gemm_update<TC_STAGES>, S::ALLOC));
   dim3 grid((M + tc::BM - 1) / tc::BM, (N + tc::BN - 1) / tc::BN);
   tc::tc_gemm_update<TC_STAGES><<<grid, tc::THREADS, S::ALLOC, s>>>(ma, mb, C, ldc, M, N, K, bf16, err);
   count_launch();

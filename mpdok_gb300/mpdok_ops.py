@@ -80,6 +80,18 @@ def _default_lib(lib_path):
     return N.load(lib_path)
 
 
+def _clear_error(lib):
+    fn = getattr(lib, "mpdok_clear_error", None)
+    if fn is not None:
+        fn()
+
+
+def _why(lib) -> str:
+    """' (library error: ...)' when the last py_* call failed rather than not converging."""
+    msg = N.call_error(lib)
+    return f" (library error: {msg})" if msg else ""
+
+
 def _oom_warning(A, N_):
     needed_gb = N_ * N_ * 12 / 1e9
     warnings.warn(
@@ -148,6 +160,7 @@ class MPDOKSolver:
             self._fp32_buf = fortran_empty(n, n, torch.float32)
         x_gpu = torch.zeros(n, dtype=torch.float64, device=b_gpu.device)
         converged = ctypes.c_int(0)
+        _clear_error(self._lib)
         self._lib.py_gmres_ir(
             ctypes.c_void_p(A_gpu.data_ptr()), ctypes.c_void_p(b_gpu.data_ptr()), ctypes.c_void_p(x_gpu.data_ptr()),
             ctypes.c_void_p(self._fp32_buf.data_ptr()), ctypes.c_int(n), ctypes.c_double(tol),
@@ -156,7 +169,7 @@ class MPDOKSolver:
         if not converged.value:
             warnings.warn(
                 f"GMRES-IR did not converge to tol={tol:.1e} within {maxiter_outer} outer iterations. "
-                f"Try increasing maxiter_outer or restart.",
+                f"Try increasing maxiter_outer or restart.{_why(self._lib)}",
                 RuntimeWarning, stacklevel=3)
         return x_gpu
 
@@ -212,6 +225,7 @@ class LUIRSolver:
         n = int(A_gpu.shape[0])
         x_gpu = torch.zeros(n, dtype=torch.float64, device=b_gpu.device)
         converged = ctypes.c_int(0)
+        _clear_error(self._lib)
         self._lib.py_lu_solve_factored(
             ctypes.c_void_p(A_gpu.data_ptr()), ctypes.c_void_p(b_gpu.data_ptr()), ctypes.c_void_p(x_gpu.data_ptr()),
             ctypes.c_int(n), ctypes.c_double(tol), ctypes.c_int(maxiter_outer), ctypes.byref(converged))
@@ -220,7 +234,7 @@ class LUIRSolver:
             raise RuntimeError("solve_factored: no factorization available — call factor(A) first.")
         if not converged.value:
             warnings.warn(f"LU-IR solve_factored did not converge to tol={tol:.1e} within {maxiter_outer} outer "
-                          f"iterations.", RuntimeWarning, stacklevel=2)
+                          f"iterations.{_why(self._lib)}", RuntimeWarning, stacklevel=2)
         return x_gpu
 
     def free_factored(self):
@@ -249,11 +263,12 @@ class LUIRSolver:
             raise ValueError(f"b must be (N,), got {tuple(b_gpu.shape)}")
         x_gpu = torch.zeros(n, dtype=torch.float64, device=b_gpu.device)
         converged = ctypes.c_int(0)
+        _clear_error(self._lib)
         self._lib.py_lu_ir(ctypes.c_void_p(A_gpu.data_ptr()), ctypes.c_void_p(b_gpu.data_ptr()),
                            ctypes.c_void_p(x_gpu.data_ptr()), ctypes.c_int(n), ctypes.c_double(tol),
                            ctypes.c_int(maxiter_outer), ctypes.byref(converged))
         torch.cuda.synchronize()
         if not converged.value:
-            warnings.warn(f"LU-IR did not converge to tol={tol:.1e} within {maxiter_outer} outer iterations.",
-                          RuntimeWarning, stacklevel=3)
+            warnings.warn(f"LU-IR did not converge to tol={tol:.1e} within {maxiter_outer} outer iterations."
+                          f"{_why(self._lib)}", RuntimeWarning, stacklevel=3)
         return x_gpu

@@ -107,4 +107,8 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MPDOK_REFERENCE")
+    if not ref:
+        sys.exit("usage: python tests/golden/make_golden.py <path to the MPDOK reference checkout> "
+                 "(or set MPDOK_REFERENCE)")
+    main(ref)
