@@ -111,7 +111,7 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sms)}
 
 
-def cpu_lu_sample(n_sample: int, repeats: int, config: str = "HEADLINE"):
+def cpu_lu_sample(n_sample: int, repeats: int, config: str = "HEADLINE", warmup_n: int = 0):
     """SciPy FP64 LU solve timed in a child process with all host threads."""
     try:
         threads = len(os.sched_getaffinity(0))
@@ -120,8 +120,8 @@ def cpu_lu_sample(n_sample: int, repeats: int, config: str = "HEADLINE"):
     env = dict(os.environ, OPENBLAS_NUM_THREADS=str(threads), OMP_NUM_THREADS=str(threads),
                MKL_NUM_THREADS=str(threads))
     out = subprocess.run([sys.executable, "-m", "oracle.cpu_baseline", "--n", str(n_sample), "--repeats",
-                          str(repeats), "--config", config], cwd=str(ROOT), env=env, capture_output=True, text=True,
-                         timeout=1800)
+                          str(repeats), "--config", config, "--warmup-n", str(warmup_n)], cwd=str(ROOT), env=env,
+                         capture_output=True, text=True, timeout=1800)
     if out.returncode != 0:
         raise RuntimeError(out.stderr[-2000:])
     d = json.loads(out.stdout.strip().splitlines()[-1])
@@ -194,7 +194,7 @@ def gemv_standalone(n: int, warmup: int, reps: int) -> dict:
 DF_FMA_OPS = 13  # FP32 instructions per double-float multiply-add in the trailing update
 
 
-def bench_batch(args) -> int:
+def bench_batch(args, emit: bool = True) -> dict:
     """C4: 256 Gaussian RBF systems, N ~ U{500..8000}, eps ~ U(2, 8), nugget 1e-8,
     8 RHS each.  One step = factor + solve + 2 FP64 refinement steps (one CUDA
     graph launch) + the adjoint of L = ||X - X*||^2 (one more solve on the
@@ -346,15 +346,15 @@ def bench_batch(args) -> int:
                    "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": sum(o.numel() * 8 for o in out),
                    "api": "BatchedRBFSolver.load + run_graph + solve + adjoint from pinned host coords/B"}
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
-    return 0
+    return line
 
 
-def bench_ooc(args) -> int:
+def bench_ooc(args, emit: bool = True) -> dict:
     """C5 layout: FP32 A in pinned host RAM in 16384-row tiles (or a raw file),
     streamed per product; reported against the pinned host->device copy rate
     measured in the same run, next to the matrix-free in-HBM product."""
@@ -442,11 +442,12 @@ def bench_ooc(args) -> int:
                          "peak_source": "pinned 1 GiB host->device copy measured in this run"},
             "matrix_free_in_hbm_ms": mf_ms, "streamed_over_matrix_free": ms / mf_ms, "ssd_store": ssd,
             "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": ck}
-    print(json.dumps(line))
-    return 0
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
-def bench_c2(args) -> int:
+def bench_c2(args, emit: bool = True) -> dict:
     """C2 as specified: N=20000 Gaussian, 3-D, eps=5, nugget 1e-6, 4 RHS.  Its
     kappa puts every FP32 Krylov body and 16/32-bit factorization out of reach
     (kappa * u > 1), so the solve is the double-float Cholesky + FP64
@@ -515,14 +516,15 @@ def bench_c2(args) -> int:
                          "frac": n ** 3 / 3.0 / per / 1e12 / df_peak, "traffic": None,
                          "note": "whole step (assembly, solves and refinement included) against the factor's flops"},
             "fp64_gpu_baseline": base, "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": ck}
-    print(json.dumps(line))
-    return 0
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 REF_OOC_SOLVE_32K_S = 45.0  # published: OOC-RAM GMRES-IR N=32768, build + solve, RTX 4060 (rbf_streaming_demo.ipynb)
 
 
-def bench_ooc_solve(args) -> int:
+def bench_ooc_solve(args, emit: bool = True) -> dict:
     """The reference's out-of-core demo at N=32768: 2-D points in [0,100]^2
     (seed 42), moving-front RHS, estimated gamma, nugget 1e-2, tol 1e-5,
     4096-row tiles in pinned host RAM, GMRES(50)-IR with up to 20 outer steps
@@ -581,14 +583,15 @@ def bench_ooc_solve(args) -> int:
                          "peak": None, "unit": "GB/s", "frac": None, "traffic": None,
                          "note": "bytes streamed over the solve time (compare with the --only ooc line's link rate)"},
             "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": ck}
-    print(json.dumps(line))
-    return 0
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 REF_FACTOR_ONCE_72_S = 0.791  # published: LU-IR factor once + 72 solves, N=8192, RTX 4060 (rbf_demo.ipynb:247)
 
 
-def bench_multi_rhs(args) -> int:
+def bench_multi_rhs(args, emit: bool = True) -> dict:
     """Factor once, solve 72 right-hand sides (3 fields x 24 steps), N=8192,
     nugget 1e-2, tol 1e-5, <= 3 refinement steps: the reference's time-series
     workload.  One step = FP32 LU of A + LU-IR of all 72 columns (8 per
@@ -673,34 +676,141 @@ def bench_multi_rhs(args) -> int:
         "dropin_per_rhs_seconds": t_dropin,
         "roofline": None, "cpu_baseline": cpu, "e2e": None, "gpu_launches": launches, "clocks": ck,
     }
-    print(json.dumps(line))
-    return 0
+    if emit:
+        print(json.dumps(line))
+    return line
+
+
+REF_FULL_STEPS = 2  # full-size SciPy solves the reference arm times (about 50 s each on 16 Arm cores)
+
+
+def headline_config(n: int, world: int) -> dict:
+    """The workload both arms measure (identical dicts, so the two lines compare like for like)."""
+    return {"workload": f"HEADLINE: Gaussian RBF N={n}, 2-D stratified jitter seed 2, eps=40 (gamma=1600), "
+                        f"nugget 1e-2, b~N(0,1); tol 1e-12; one step = one full solve from x = 0 "
+                        f"(A resident in memory, assembly excluded)",
+            "l2": "inputs larger than L2 (A64 8.6 GB, A32 4.3 GB)", "parallelism": f"replicas x{world}"}
 
 
 def run_reference(args):
-    """--impl reference: the reference's CPU path (SciPy FP64 LU) on rank 0."""
+    """--impl reference: the reference's CPU path for this workload (SciPy FP64
+    lu_factor / lu_solve + FP64 refinement, the path of rbf_demo.ipynb) on all
+    host threads, rank 0 only.  Every timed step is one full solve of the
+    N=32768 headline system itself: no sample, no scaling.  A full solve takes
+    about a minute on the host cores, so the arm times min(steps, 2) of them
+    after one small warm-up solve, and reports the count it timed."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    n_full = args.n
-    ns = args.cpu_sample_n
-    scale = (n_full / ns) ** 3
-    d = cpu_lu_sample(ns, args.warmup + args.steps)
-    secs = d["seconds"][args.warmup:] or d["seconds"]
-    per = sum(secs) / len(secs) * scale
+    n = args.n
+    k = max(1, min(args.steps, REF_FULL_STEPS))
+    d = cpu_lu_sample(n, k, warmup_n=2048)
+    secs = d["seconds"]
+    per = sum(secs) / len(secs)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     line = {
         "impl": "reference", "metric": HEADLINE_METRIC, "value": per, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded NumPy)",
-        "config": {"workload": f"HEADLINE Gaussian RBF N={n_full}, eps=40, nugget 1e-2, SciPy FP64 LU + refinement",
-                   "sample_n": ns},
+        "steps": len(secs), "steps_requested": args.steps, "warmup": 1, "ms_per_step": per * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded NumPy, HEADLINE system)",
+        "config": headline_config(n, world),
+        "timed_solves_seconds": secs, "relres": d["relres"], "host_assembly_seconds": d.get("assembly_seconds"),
         "cpu_baseline": {"value": per, "unit": UNIT, "cores": d["threads"], "kind": "port",
-                         "sample": f"scipy lu_factor/lu_solve FP64 at N={ns} (x{scale:.1f} O(N^3) scaling to "
-                                   f"N={n_full}); relres {d['relres']:.2e}"},
+                         "sample": f"the full N={n} headline system: scipy lu_factor/lu_solve FP64 + refinement, "
+                                   f"{len(secs)} timed solve(s) after one N=2048 warm-up solve; relres "
+                                   f"{d['relres']:.2e}"},
         "e2e": {"value": per, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def bench_hard(args, emit: bool = True) -> dict:
+    """The headline centres with C5's nugget (1e-6, kappa >= 1e6) and a smooth
+    right-hand side: each factor type (FP16, BF16, FP32) preconditioning the
+    three-precision GMRES-IR, against the plain FP64 GPU solve of the same
+    system.  Reports, per factor type, whether it reached relres 1e-12, its
+    outer / inner iterations and its time."""
+    import numpy as np
+    import torch
+    from mpdok_gb300 import configs
+    from mpdok_gb300.rbf_kernel import assemble
+    from mpdok_gb300.solvers import MixedSolver, fp64_gpu_solve
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    sysm = configs.hard_headline(n=args.n)
+    n = sysm.n
+    A = assemble(sysm.coords, gamma=sysm.gamma, reg=sysm.reg, kernel=sysm.kernel, dtype=torch.float64)
+    b = torch.from_numpy(np.asarray(sysm.b)).cuda()
+    fp64 = fp64_gpu_solve(A, b, tol=sysm.tol)
+    outcomes = {}
+    best = None
+    for fd in ("fp16", "bf16", "fp32"):
+        sv = MixedSolver(factor_dtype=fd, maxiter_outer=20)
+        import warnings
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            for _ in range(max(1, args.warmup)):
+                sv.solve(A, b, tol=sysm.tol)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                x, info = sv.solve(A, b, tol=sysm.tol)
+            e1.record()
+            torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3 / args.steps
+        err = float(torch.linalg.norm(x - fp64["x"]) / torch.linalg.norm(fp64["x"]))
+        outcomes[fd] = {"seconds": sec, "converged": bool(info["converged"]), "relres": info["relres"],
+                        "outer_iters": info["outer_iters"], "inner_iters": info["inner_iters"],
+                        "perturbed_pivots": info.get("perturbed_pivots"), "err_vs_fp64_lu": err,
+                        "factor_ms": info.get("factor_ms"), "refine_ms": info.get("refine_ms"),
+                        "speedup_vs_fp64_gpu": fp64["seconds"] / sec}
+        if info["converged"] and (best is None or sec < outcomes[best]["seconds"]):
+            best = fd
+        del sv
+        torch.cuda.empty_cache()
+    line = {"metric": "time to FP64 relres<=1e-12 on the hard family (N=32768 Gaussian, nugget 1e-6)",
+            "value": outcomes[best]["seconds"] if best else None, "unit": "s", "steps": args.steps,
+            "warmup": max(1, args.warmup), "higher_is_better": False, "dtype": "f32+f64 (mixed)",
+            "config": {"workload": f"HARD: the headline's N={n} stratified-jitter centres, Gaussian eps="
+                                   f"{configs.HARD_EPS:g}, nugget 1e-6, b = sin(2 pi x1) cos(2 pi x2); tol 1e-12; "
+                                   "one step = one full solve (factor + GMRES(30)-IR), A in HBM"},
+            "fastest_converged_factor": best, "by_factor": outcomes,
+            "fp64_gpu_baseline": {"seconds": fp64["seconds"], "relres": fp64["relres"], "method": fp64["method"]},
+            "speedup_vs_fp64_gpu": (fp64["seconds"] / outcomes[best]["seconds"]) if best else None}
+    del A
+    if emit:
+        print(json.dumps(line))
+    return line
+
+
+def run_extras(args) -> dict:
+    """Each secondary configuration once, with short step counts, as dicts for
+    the headline line: C2, C4 (batched + adjoint), the hard headline family,
+    out-of-core (streamed matvec at N=100000 and the reference's N=32768 OOC
+    solve) and factor-once / many-RHS.  A failure is recorded, not raised."""
+    import argparse as _ap
+    import torch
+    out = {}
+    plan = (("hard_headline", bench_hard, dict(steps=2, warmup=1)),
+            ("c2", bench_c2, dict(steps=2, warmup=1)),
+            ("c4_batch_adjoint", bench_batch, dict(steps=2, warmup=1, systems=256)),
+            ("ooc_matvec", bench_ooc, dict(steps=3, warmup=1, n=100000)),
+            ("ooc_solve", bench_ooc_solve, dict(steps=1, warmup=1)),
+            ("multi_rhs", bench_multi_rhs, dict(steps=3, warmup=1)))
+    for name, fn, over in plan:
+        a = _ap.Namespace(**dict(vars(args), **over))
+        t0 = time.perf_counter()
+        try:
+            line = fn(a, emit=False)
+            line = {k: v for k, v in line.items() if k not in ("n_gpus", "scaling", "data")}
+            line["wall_seconds"] = time.perf_counter() - t0
+            out[name] = line
+        except Exception as e:  # noqa: BLE001
+            out[name] = {"error": f"{type(e).__name__}: {e}"[:400], "wall_seconds": time.perf_counter() - t0}
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -710,12 +820,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
     ap.add_argument("--n", type=int, default=32768)
-    ap.add_argument("--cpu-sample-n", type=int, default=8192)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline only: skip the once-each lines of the other configurations")
     ap.add_argument("--no-fp64-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", default="headline",
-                    choices=["headline", "gemv", "batch", "ooc", "ooc_solve", "multi_rhs", "c2"],
+                    choices=["headline", "gemv", "batch", "ooc", "ooc_solve", "multi_rhs", "c2", "hard"],
                     help="gemv: only the standalone stored-matrix GEMV measurement (used for kernel profiles); "
                          "batch: the batched C4 solve + adjoint line; ooc: the out-of-core C5 streaming line")
     ap.add_argument("--systems", type=int, default=256, help="--only batch: number of C4 systems")
@@ -728,15 +839,23 @@ def main():
         print(json.dumps(gemv_standalone(args.n, max(3, args.warmup), max(5, args.steps))))
         return 0
     if args.only == "batch":
-        return bench_batch(args)
+        bench_batch(args)
+        return 0
     if args.only == "ooc":
-        return bench_ooc(args)
+        bench_ooc(args)
+        return 0
     if args.only == "multi_rhs":
-        return bench_multi_rhs(args)
+        bench_multi_rhs(args)
+        return 0
     if args.only == "c2":
-        return bench_c2(args)
+        bench_c2(args)
+        return 0
+    if args.only == "hard":
+        bench_hard(args)
+        return 0
     if args.only == "ooc_solve":
-        return bench_ooc_solve(args)
+        bench_ooc_solve(args)
+        return 0
 
     import numpy as np
     import torch
@@ -769,6 +888,7 @@ def main():
     t_asm = time.perf_counter() - t0
 
     solver = MixedSolver()
+    solver_desc = solver.describe()
     for _ in range(args.warmup):
         x, info = solver.solve(A, b, tol=sysm.tol)
     torch.cuda.synchronize()
@@ -871,36 +991,67 @@ def main():
             torch.cuda.synchronize()
             if i > 0:
                 times.append(time.perf_counter() - t0)
-        del A_host
+        # the upload alone (A straight into its device buffer with the FP32
+        # copy made per block), against a plain pinned 1 GiB host -> device copy
+        from mpdok_gb300._device import fortran_empty, upload_fortran
+        a32 = fortran_empty(n, n, torch.float32)
+        u0, u1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        u0.record()
+        Ad = upload_fortran(A_host, out32=a32)
+        u1.record()
+        torch.cuda.synchronize()
+        up_s = u0.elapsed_time(u1) / 1e3
+        del Ad, a32
+        hb = torch.empty(1 << 27, dtype=torch.float64).pin_memory()
+        db = torch.empty_like(hb, device="cuda")
+        db.copy_(hb, non_blocking=True)
+        torch.cuda.synchronize()
+        u0.record()
+        for _ in range(3):
+            db.copy_(hb, non_blocking=True)
+        u1.record()
+        torch.cuda.synchronize()
+        link = 3 * hb.numel() * 8 / (u0.elapsed_time(u1) / 1e3) / 1e9
+        del hb, db, A_host
         e2e = {"value": sum(times) / len(times), "unit": UNIT, "h2d_bytes_per_step": 8 * n * n + 8 * n,
-               "d2h_bytes_per_step": 8 * n, "api": "mpdok_gb300.solvers.MixedSolver.solve(host A, host b)"}
+               "d2h_bytes_per_step": 8 * n, "api": "mpdok_gb300.solvers.MixedSolver.solve(host A, host b)",
+               "upload_seconds": up_s, "upload_GBs": 8.0 * n * n / up_s / 1e9, "pinned_h2d_GBs": link,
+               "upload_frac_of_pinned_copy": 8.0 * n * n / up_s / 1e9 / link}
 
+    gemv_sa = gemv_standalone(n, 3, 10) if rank == 0 else None
+
+    # every other configuration once (not per step), so that the driver-run
+    # line carries them; each is a complete measurement of its own workload
+    extras = {}
+    if not args.no_extras and rank == 0 and world == 1:
+        del A
+        solver = None
+        torch.cuda.empty_cache()
+        extras = run_extras(args)
+
+    # the reference's CPU path on the full headline system, after all GPU work
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         try:
-            d = cpu_lu_sample(args.cpu_sample_n, 1)
-            scale = (n / args.cpu_sample_n) ** 3
-            cpu = {"value": d["seconds"][0] * scale, "unit": UNIT, "cores": d["threads"], "kind": "port",
-                   "sample": f"scipy lu_factor/lu_solve FP64 + refinement at N={args.cpu_sample_n}, "
-                             f"{d['seconds'][0]:.2f} s measured, x{scale:.1f} O(N^3) scaling to N={n}"}
+            d = cpu_lu_sample(n, 1, warmup_n=2048)
+            cpu = {"value": d["seconds"][0], "unit": UNIT, "cores": d["threads"], "kind": "port",
+                   "sample": f"the full N={n} headline system: scipy lu_factor/lu_solve FP64 + refinement, one "
+                             f"timed solve after an N=2048 warm-up solve; relres {d['relres']:.2e}",
+                   "relres": d["relres"]}
         except Exception as e:  # noqa: BLE001
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {e}"}
-
-    gemv_sa = gemv_standalone(n, 3, 10) if rank == 0 else None
 
     line = {
         "metric": HEADLINE_METRIC, "value": per_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_s * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded NumPy, HEADLINE system)",
-        "config": {"workload": f"HEADLINE: Gaussian RBF N={n}, 2-D stratified jitter seed 2, eps=40 (gamma=1600), "
-                               f"nugget 1e-2, b~N(0,1); tol 1e-12; one step = one full solve (A in HBM)",
-                   "l2": "inputs larger than L2 (A64 8.6 GB, A32 4.3 GB)", "parallelism": f"replicas x{world}",
-                   "solver": solver.describe(), "assembly_s": t_asm},
+        "config": headline_config(n, world), "solver": solver_desc, "assembly_s": t_asm,
         "relres": relres, "solve_info": infos[-1], "fp64_gpu_baseline": fp64,
         "roofline": roof, "gemv_roofline": rooflines.get("gemv_f32"), "gemv_standalone": gemv_sa,
         "rooflines": rooflines,
         "kernel_time_share": share, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": launches, "clocks": ck,
+        "gpu_launches": launches, "clocks": ck, "configs": extras,
     }
     if rank == 0:
         print(json.dumps(line))

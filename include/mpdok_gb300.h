@@ -225,19 +225,26 @@ MPDOK_API int mpdok_mf_cg_ir(const double* coords, long long n, int dim, int ker
                              mpdok_solve_info* info, cudaStream_t stream);
 
 /* ----------------------------------------------------------- LU (tensor cores)
- * Blocked right-looking LU of W = D A D (D = diag(1/sqrt|a_ii|), panel 128)
- * with FP32 panels and a trailing update W22 -= L21 U12 whose operands are
- * rounded to the factor type: BF16 / FP16 run on tcgen05 tensor cores
- * (FP32 accumulation in tensor memory), FP32 on CUDA cores (the reference's
- * Sgetrf precision, benchmark_mpdok.ipynb:982-993).
+ * Blocked right-looking LU with FP32 panels and a trailing update
+ * W22 -= L21 U12 whose operands are rounded to the factor type: BF16 / FP16
+ * run on tcgen05 tensor cores (FP32 accumulation in tensor memory), FP32 on
+ * CUDA cores (the reference's Sgetrf precision, benchmark_mpdok.ipynb:982-993).
+ *
+ * pivoting = 0: W = D A D (D = diag(1/sqrt|a_ii|), symmetric scaling), no row
+ *   exchanges (SPD / diagonally dominant systems, e.g. Gaussian RBF); pivots
+ *   below 1e-6 in magnitude are replaced by +-1e-6.  Return: 0 ok, > 0 the
+ *   number of pivots that had to be perturbed (still a usable preconditioner).
+ * pivoting = 1: W = Dr A Dc (power-of-two row and column equilibration),
+ *   P W = L U with partial pivoting by rows, as cusolverDnSgetrf / LAPACK
+ *   getrf (the reference's lu_ir.so, benchmark_mpdok.ipynb:989-990).  Return:
+ *   LAPACK's info, 0 ok or i > 0 when U(i, i) is exactly zero (1-based; the
+ *   factors are then singular).  n is limited by the panel factorization,
+ *   which keeps the panel's rows in the shared memory of co-resident CTAs
+ *   (about 65000 rows on a GB300): larger n returns MPDOK_ERR_UNSUPPORTED.
+ * Both: < 0 error.
  *
  * Factors live in a caller-owned device buffer of mpdok_lu_factor_size()
- * bytes; factorization scratch is mpdok_lu_work_size() bytes.  pivoting must
- * be 0: the LU is unpivoted (SPD / diagonally dominant systems, e.g. Gaussian
- * RBF), with pivots below 1e-6 in magnitude replaced by +-1e-6; partial
- * pivoting is not implemented (MPDOK_ERR_INVALID_ARG).  Return: 0 ok, > 0
- * number of pivots that had to be perturbed away from zero (still a usable
- * preconditioner), < 0 error. */
+ * bytes; factorization scratch is mpdok_lu_work_size() bytes. */
 enum { MPDOK_ENGINE_TENSOR = 0, MPDOK_ENGINE_SIMT = 1 };
 
 MPDOK_API int mpdok_gemm_update(float* C, long long ldc, const void* A, const void* B, int M, int N, int K,
@@ -257,7 +264,14 @@ MPDOK_API int mpdok_lu_factor(const double* A, long long lda, long long n, int f
  * max_steps steps (out may be NULL); returns the number of steps or a
  * negative status. */
 MPDOK_API long long mpdok_lu_schedule(long long n, int fdtype, long long* out, long long max_steps);
-/* z = (D U^-1 L^-1 P D) v: one application of the factorization (FP32 vectors). */
+/* The factors in plain form (device outputs, each may be NULL): L\U as an
+ * n x n column-major FP32 matrix (unit L below the diagonal), the 0-based
+ * pivot rows (LAPACK's ipiv; the identity for unpivoted factors), the row
+ * permutation as a gather ((P x)_i = x_perm[i]) and the scalings Dr, Dc,
+ * with P (Dr A Dc) = L U. */
+MPDOK_API int mpdok_lu_export(const void* factors, long long n, int fdtype, float* lu, long long ldo, int* ipiv,
+                              int* perm, float* dr, float* dc, cudaStream_t stream);
+/* z = (Dc U^-1 L^-1 P Dr) v: one application of the factorization (FP32 vectors). */
 MPDOK_API size_t mpdok_lu_apply_work_size(long long n);
 MPDOK_API int mpdok_lu_apply(const void* factors, long long n, int fdtype, const float* v, float* z, void* work,
                              size_t work_bytes, cudaStream_t stream);

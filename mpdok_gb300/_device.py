@@ -48,6 +48,8 @@ def as_fortran(A, dtype=torch.float64) -> torch.Tensor:
             raise ValueError(f"A must be 2-D, got shape {tuple(A.shape)}")
         if A.is_cuda and A.dtype == dtype and is_fortran(A):
             return A
+        if not A.is_cuda and A.dtype == torch.float64 and dtype == torch.float64:
+            return upload_fortran(A)
         out = fortran_empty(A.shape[0], A.shape[1], dtype, dev)
         out.copy_(A.to(device=dev, dtype=dtype))
         return out
@@ -58,6 +60,49 @@ def as_fortran(A, dtype=torch.float64) -> torch.Tensor:
     host = torch.from_numpy(arr)
     out = fortran_empty(arr.shape[0], arr.shape[1], dtype, dev)
     out.copy_(host.to(dtype))
+    return out
+
+
+def upload_fortran(A_host: torch.Tensor, out: torch.Tensor | None = None, out32: torch.Tensor | None = None,
+                   chunk_bytes: int = 256 << 20) -> torch.Tensor:
+    """Host (N, M) FP64 matrix in column-major order -> CUDA column-major FP64 tensor.
+
+    The host columns are copied straight into the device buffer (no device
+    temporary), in blocks of whole columns on a side stream; when ``out32`` is
+    given, each block is converted to FP32 on the current stream while the
+    next block is still on the host link, so the FP32 copy of A costs no extra
+    pass once the upload ends.  A pinned host tensor gives the full host-link
+    rate; a pageable one is copied synchronously.  The current stream owns the
+    result (it waits for every block)."""
+    from . import _native as N
+    if A_host.dim() != 2 or A_host.dtype != torch.float64 or A_host.is_cuda:
+        raise ValueError("upload_fortran expects a host FP64 2-D tensor")
+    n, m = A_host.shape
+    if not is_fortran(A_host):
+        A_host = A_host.t().contiguous().t()
+    dev = require_cuda()
+    if out is None:
+        out = fortran_empty(n, m, torch.float64, dev)
+    flat_h = A_host.t().reshape(-1)   # column-major storage as one contiguous run
+    flat_d = out.t().reshape(-1)
+    flat_32 = out32.t().reshape(-1) if out32 is not None else None
+    cols = max(1, chunk_bytes // max(1, 8 * n))
+    cur = torch.cuda.current_stream(dev)
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(cur)
+    lib = N.load() if out32 is not None else None
+    for c0 in range(0, m, cols):
+        c1 = min(m, c0 + cols)
+        lo, hi = c0 * n, c1 * n
+        with torch.cuda.stream(side):
+            flat_d[lo:hi].copy_(flat_h[lo:hi], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(side)
+        cur.wait_event(ev)
+        if out32 is not None:
+            N.check(lib.mpdok_convert(ptr(flat_d[lo:hi]), N.F64, ptr(flat_32[lo:hi]), N.F32, hi - lo,
+                                      ctypes.c_void_p(cur.cuda_stream)), "convert")
+    flat_d.record_stream(side)
     return out
 
 

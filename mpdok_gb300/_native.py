@@ -102,6 +102,8 @@ _SIGS = {
     "mpdok_lu_work_size": (c_size_t, [c_ll, c_int]),
     "mpdok_lu_factor": (c_int, [c_void_p, c_ll, c_ll, c_int, c_int, c_void_p, c_size_t, c_void_p, c_size_t,
                                 c_void_p]),
+    "mpdok_lu_export": (c_int, [c_void_p, c_ll, c_int, c_void_p, c_ll, c_void_p, c_void_p, c_void_p, c_void_p,
+                                c_void_p]),
     "mpdok_lu_apply_work_size": (c_size_t, [c_ll]),
     "mpdok_lu_apply": (c_int, [c_void_p, c_ll, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "mpdok_lu_ir_work_size": (c_size_t, [c_ll]),

@@ -80,6 +80,21 @@ def headline(n: int = 32768) -> RBFSystem:
     return RBFSystem("HEADLINE", X, "gaussian", 1600.0, 1e-2, b, tol=1e-12, extra={"restart": 30})
 
 
+HARD_EPS = 40.0
+
+
+def hard_headline(n: int = 32768, eps: float = HARD_EPS) -> RBFSystem:
+    """The headline centres with C5's nugget (1e-6): kappa ~ lambda_max / 1e-6.
+
+    With a white-noise right-hand side the solution's components along the
+    eigenvectors at the nugget grow by 1e6 and the FP64 LU floor itself sits
+    near u * kappa; the right-hand side is therefore the smooth field of C1 /
+    C3, sin(2 pi x1) cos(2 pi x2), for which the FP64 solve reaches 1e-12."""
+    X = stratified_jitter(n, 2)
+    b = np.sin(2 * np.pi * X[:, 0]) * np.cos(2 * np.pi * X[:, 1])
+    return RBFSystem("HARD", X, "gaussian", eps * eps, 1e-6, b, tol=1e-12, extra={"restart": 30})
+
+
 def c4(n_systems: int = 256, nrhs: int = 8, n_lo: int = 500, n_hi: int = 8000) -> list[RBFSystem]:
     rng = np.random.default_rng(3)
     sizes = rng.integers(n_lo, n_hi + 1, size=n_systems)

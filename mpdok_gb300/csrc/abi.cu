@@ -122,8 +122,10 @@ extern "C" void py_free_managed(void) {
 // ------------------------------------------------- lu_ir.so symbols
 // mpdok_ops.py:101-141.  One process-wide saved factorization, as in the
 // reference (py_lu_factor keeps it until py_lu_free_factored).  Factors are
-// FP32 (the reference's Sgetrf precision) so that two or three refinement
-// steps reach FP64 accuracy on the systems it is documented for.
+// FP32 with partial pivoting by rows (the reference's Sgetrf: L, U and P,
+// benchmark_mpdok.ipynb:989-990), so that two or three refinement steps reach
+// FP64 accuracy on general non-singular matrices, and info has LAPACK's
+// meaning: > 0 is the first exactly zero pivot (1-based).
 
 namespace mpdok {
 
@@ -166,8 +168,8 @@ static int lu_factor_global(double* A, int N) {
   MPDOK_TRY(ensure(&st.factors, &st.factor_bytes, fb));
   MPDOK_TRY(ensure(&st.work, &st.work_bytes, wb));
   st.n = -1;
-  const int s = mpdok_lu_factor(A, N, N, MPDOK_F32, 0, st.factors, st.factor_bytes, st.work, st.work_bytes, 0);
-  if (s >= 0) st.n = N;
+  const int s = mpdok_lu_factor(A, N, N, MPDOK_F32, 1, st.factors, st.factor_bytes, st.work, st.work_bytes, 0);
+  if (s == 0) st.n = N;  // a singular factorization (info > 0) is not kept for solves, as LAPACK getrs would divide by 0
   return s;
 }
 
@@ -177,7 +179,7 @@ extern "C" void py_lu_factor(double* A, int N, int* info_out) {
   std::lock_guard<std::mutex> lk(abi_state().mu);
   int s = (N <= 0) ? 0 : lu_factor_global(A, N);
   if (N <= 0) lu_state().n = 0;
-  if (info_out) *info_out = s;  // > 0: pivots perturbed (numerically singular), < 0: error
+  if (info_out) *info_out = s;  // > 0: U(s, s) is exactly zero (LAPACK's info), < 0: error
 }
 
 extern "C" void py_lu_solve_factored(double* A, double* b, double* x, int N, double tol, int maxiter,
@@ -201,7 +203,8 @@ extern "C" void py_lu_solve_factored(double* A, double* b, double* x, int N, dou
 extern "C" void py_lu_ir(double* A, double* b, double* x, int N, double tol, int maxiter, int* converged_out) {
   int info = 0;
   py_lu_factor(A, N, &info);
-  if (info < 0) {
+  if (info != 0) {
+    if (info > 0) set_error("LU-IR: U(%d, %d) is exactly zero; the matrix is singular", info, info);
     if (converged_out) *converged_out = 0;
     return;
   }

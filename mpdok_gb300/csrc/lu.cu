@@ -46,7 +46,8 @@ static int fsize(int fdtype) { return fdtype == MPDOK_F32 ? 4 : 2; }
 struct LULayout {
   long long n = 0, ldf = 0;
   int nblk = 0, fdtype = MPDOK_BF16;
-  size_t off_lu = 0, off_linv = 0, off_uinv = 0, off_ml = 0, off_mu = 0, off_d = 0, off_meta = 0, total = 0;
+  size_t off_lu = 0, off_linv = 0, off_uinv = 0, off_ml = 0, off_mu = 0, off_d = 0, off_dr = 0, off_perm = 0,
+         off_ipiv = 0, off_meta = 0, total = 0;
 };
 
 struct LUMeta {
@@ -71,15 +72,26 @@ static LULayout lu_layout(long long n, int fdtype) {
   // chain tiles of the triangular solves: Ml_t = Linv_t L(t, t-1), Mu_t = Uinv_t U(t, t+1)
   L.off_ml = take((size_t)L.nblk * LNB * LNB * sizeof(float));
   L.off_mu = take((size_t)L.nblk * LNB * LNB * sizeof(float));
+  // W = Dr A Dc with P W = L U, so A^-1 = Dc U^-1 L^-1 P Dr: d holds Dc, dr
+  // holds Dr, perm the row permutation ((P x)_i = x_perm[i]) and ipiv the
+  // LAPACK-style pivot rows.  Unpivoted factors have Dr = Dc and perm = 1.
   L.off_d = take((size_t)std::max(1LL, n) * sizeof(float));
+  L.off_dr = take((size_t)std::max(1LL, n) * sizeof(float));
+  L.off_perm = take((size_t)std::max(1LL, n) * sizeof(int));
+  L.off_ipiv = take((size_t)std::max(1LL, n) * sizeof(int));
   L.off_meta = take(sizeof(LUMeta));
   L.total = off;
   return L;
 }
 
+// Partial pivoting: the panel factorization runs on up to PIV_MAX_CTAS
+// co-resident CTAs that meet at one grid barrier per column.
+constexpr int PIV_MAX_CTAS = 256;
+
 struct LUWork {
   long long ldw = 0;
-  size_t off_W = 0, off_Lp = 0, off_Up = 0, off_err = 0, total = 0;
+  size_t off_W = 0, off_Lp = 0, off_Up = 0, off_err = 0, off_cand = 0, off_crow = 0, off_top = 0, off_bar = 0,
+         off_plan = 0, off_scale = 0, total = 0;
 };
 
 static LUWork lu_work_layout(long long n, int fdtype) {
@@ -93,15 +105,29 @@ static LUWork lu_work_layout(long long n, int fdtype) {
   w.off_Lp = take(2 * (size_t)std::max(1LL, n) * super_panel_width(fdtype) * fsize(fdtype));
   w.off_Up = take(2 * (size_t)std::max(1LL, n) * super_panel_width(fdtype) * fsize(fdtype));
   w.off_err = take(64);
+  // pivoting: candidate (|value|, row) per CTA and the candidate rows, double
+  // buffered by column parity; the row at the panel's current position; the
+  // barrier counter; the panel's row moves (dst, src pairs); row / column
+  // maxima of the equilibration
+  w.off_cand = take(2 * PIV_MAX_CTAS * 8);
+  w.off_crow = take(2 * (size_t)PIV_MAX_CTAS * LNB * sizeof(float));
+  w.off_top = take(2 * LNB * sizeof(float));
+  w.off_bar = take(64);
+  w.off_plan = take((1 + 4 * LNB) * sizeof(int));
+  w.off_scale = take(2 * (size_t)std::max(1LL, n) * sizeof(double));
   w.total = off;
   return w;
 }
 
 // ----------------------------------------------------------------- scaling
-__global__ void k_diag_scale(const double* __restrict__ A, long long lda, long long n, float* __restrict__ d) {
+__global__ void k_diag_scale(const double* __restrict__ A, long long lda, long long n, float* __restrict__ d,
+                             float* __restrict__ dr, int* __restrict__ perm) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double a = fabs(A[i + i * lda]);
-    d[i] = (a > 0.0 && isfinite(a)) ? (float)(1.0 / sqrt(a)) : 1.f;
+    const float v = (a > 0.0 && isfinite(a)) ? (float)(1.0 / sqrt(a)) : 1.f;
+    d[i] = v;
+    dr[i] = v;
+    perm[i] = (int)i;
   }
 }
 
@@ -716,8 +742,8 @@ __device__ __forceinline__ bool wait_value(const float* p, float& v) {
 template <typename F, bool LOWER>
 __global__ void __launch_bounds__(256)
 k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, const float* __restrict__ Mt,
-       long long n, int nblk, const float* __restrict__ rhs, const float* __restrict__ dsc, float* out, int* ticket,
-       int* err, const int* skip) {
+       long long n, int nblk, const float* __restrict__ rhs, const float* __restrict__ dsc,
+       const int* __restrict__ perm, float* out, int* ticket, int* err, const int* skip) {
   extern __shared__ float sDi[];      // 128 x 128 diagonal-block inverse (column-major)
   __shared__ int s_t;
   __shared__ int s_abort;
@@ -750,7 +776,19 @@ k_trsv(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, 
   for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) sDi[idx] = __ldg(Di + idx);
   // the block's right-hand side, staged now so that its latency stays off the
   // path from x_{t-2} to y_t
-  if (tid < LNB) s_rhs[tid] = tid < rows ? (LOWER ? rhs[r0 + tid] * dsc[r0 + tid] : rhs[r0 + tid]) : 0.f;
+  // (the lower solve takes P Dr v: row i of its right-hand side is row perm[i] of v)
+  if (tid < LNB) {
+    float r = 0.f;
+    if (tid < rows) {
+      if (LOWER) {
+        const int pi = __ldg(perm + r0 + tid);
+        r = rhs[pi] * __ldg(dsc + pi);
+      } else {
+        r = rhs[r0 + tid];
+      }
+    }
+    s_rhs[tid] = r;
+  }
   const int rg = tid % 16, cg = tid / 16;
   const long long rbase = r0 + rg * 8;
   float acc[8];
@@ -889,7 +927,7 @@ template <typename F, bool LOWER, int K>
 __global__ void __launch_bounds__(256)
 k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ Dinv, const float* __restrict__ Mt,
              long long n, int nblk, const float* __restrict__ rhs, long long ld, const float* __restrict__ dsc,
-             float* out, int* ticket, int* err) {
+             const int* __restrict__ perm, float* out, int* ticket, int* err) {
   extern __shared__ float sDi[];      // 128 x 128 diagonal-block inverse (column-major)
   __shared__ int s_t;
   __shared__ int s_abort;
@@ -917,8 +955,12 @@ k_trsv_multi(const F* __restrict__ LU, long long ldf, const float* __restrict__ 
     const int row = e % LNB, k = e / LNB;
     float r = 0.f;
     if (row < rows) {
-      const float b = rhs[(long long)k * ld + r0 + row];
-      r = LOWER ? b * dsc[r0 + row] : b;
+      if (LOWER) {
+        const int pi = __ldg(perm + r0 + row);
+        r = rhs[(long long)k * ld + pi] * __ldg(dsc + pi);
+      } else {
+        r = rhs[(long long)k * ld + r0 + row];
+      }
     }
     s_a[k][row] = r;
   }
@@ -1029,6 +1071,390 @@ __global__ void k_scale_out_multi(const float* __restrict__ z, const float* __re
   }
 }
 
+// ------------------------------------------------------- partial pivoting
+// The LU with row pivoting behind the reference's lu_ir.so (cusolverDnSgetrf +
+// Sgetrs with L, U, P: benchmark_mpdok.ipynb:989-990; py_lu_factor's info is
+// LAPACK's, mpdok_ops.py:195-202).  The matrix is first equilibrated with
+// power-of-two row and column scales (W = Dr A Dc, exact, |W| <= 1 in every
+// row and column, which keeps 16-bit operands in range), then factored
+// right-looking in 128-column panels:
+//   1. k_getf2: the tall panel W[jp:n, jp:jp+128] with partial pivoting on G
+//      co-resident CTAs, each holding a slice of its rows in shared memory;
+//      one grid barrier per column (pivot search, row exchange, rank-1 update);
+//   2. k_laswp: the panel's row exchanges applied to every other column of W;
+//   3. k_piv_diag: the 128 x 128 diagonal block's unit-lower / upper inverses;
+//   4. U12 = L11^-1 W12 (the panel solve of the unpivoted path), L21 to the
+//      K-major operand, and W22 -= L21 U12 (tensor cores or CUDA cores);
+// and at the end the strictly lower part of W is rounded into the factor.
+
+// |a_ij| maxima per row over a column chunk (non-negative doubles compare as
+// their bit patterns).
+__global__ void k_row_absmax(const double* __restrict__ A, long long lda, long long n, long long cchunk,
+                             unsigned long long* __restrict__ rmax) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const long long c0 = (long long)blockIdx.y * cchunk, c1 = min(n, c0 + cchunk);
+  double m = 0.0;
+  for (long long c = c0; c < c1; ++c) m = fmax(m, fabs(A[i + c * lda]));
+  atomicMax(rmax + i, (unsigned long long)__double_as_longlong(m));
+}
+
+// 2^-e with max * 2^-e in [0.5, 1): an exact scale; 1 for a zero or non-finite max.
+__device__ __forceinline__ float pow2_inv_scale(double m) {
+  if (!(m > 0.0) || !isfinite(m)) return 1.f;
+  int e = 0;
+  frexp(m, &e);
+  e = max(-120, min(120, e));
+  return ldexpf(1.f, -e);
+}
+
+__global__ void k_row_scale(const unsigned long long* __restrict__ rmax, long long n, float* __restrict__ dr,
+                            int* __restrict__ perm) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    dr[i] = pow2_inv_scale(__longlong_as_double((long long)rmax[i]));
+    perm[i] = (int)i;
+  }
+}
+
+// Column scales of the row-scaled matrix (one CTA per column) and W = Dr A Dc
+// rounded once to FP32.
+__global__ void __launch_bounds__(256)
+k_col_scale_copy(const double* __restrict__ A, long long lda, long long n, const float* __restrict__ dr,
+                 float* __restrict__ dc, float* __restrict__ W, long long ldw) {
+  __shared__ double red[32];
+  const long long j = blockIdx.x;
+  double m = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(A[i + j * lda]) * (double)dr[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
+    if (threadIdx.x == 0) red[0] = t;
+  }
+  __syncthreads();
+  const float c = pow2_inv_scale(red[0]);
+  if (threadIdx.x == 0) dc[j] = c;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x)
+    W[i + j * ldw] = (float)(A[i + j * lda] * (double)dr[i] * (double)c);
+}
+
+struct PivCand {
+  float val;  // |candidate|, -1 when the CTA has no eligible row
+  int row;    // global row, -1 when none
+};
+
+// (v2, i2) beats (v1, i1): larger magnitude, ties to the smaller row (LAPACK's
+// isamax takes the first maximum).
+__device__ __forceinline__ bool piv_better(float v2, int i2, float v1, int i1) {
+  return v2 > v1 || (v2 == v1 && i2 >= 0 && (i1 < 0 || i2 < i1));
+}
+
+__device__ __forceinline__ void warp_argmax(float& v, int& i) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+    const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+    if (piv_better(v2, i2, v, i)) { v = v2; i = i2; }
+  }
+}
+
+// Block-wide argmax; the result is valid in every thread.
+__device__ __forceinline__ void block_argmax(float& v, int& i, float* sv, int* si) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  warp_argmax(v, i);
+  if (lane == 0) { sv[wid] = v; si[wid] = i; }
+  __syncthreads();
+  if (wid == 0) {
+    float a = lane < nw ? sv[lane] : -1.f;
+    int b = lane < nw ? si[lane] : -1;
+    warp_argmax(a, b);
+    if (lane == 0) { sv[0] = a; si[0] = b; }
+  }
+  __syncthreads();
+  v = sv[0];
+  i = si[0];
+  __syncthreads();
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+constexpr int GETF2_THREADS = 512;
+constexpr long long GRID_WAIT_LIMIT = 1LL << 22;
+
+// Partial-pivoting LU of the panel W[jp:n, jp:jp+nb] (nb <= 128) on G CTAs
+// (gridDim.x, all co-resident: cooperative launch).  CTA g holds rows
+// [jp + g R, jp + (g + 1) R) column-major in shared memory.  Per column j:
+//   a. each CTA finds its largest |w| among rows >= jp + j and publishes the
+//      value, the row and that row's nb values (buffer j & 1); the owner of
+//      row jp + j publishes that row too;
+//   b. grid barrier (counter reaches (j + 1) G; bounded wait);
+//   c. every CTA picks the same winner from the G candidates (largest, ties
+//      to the smaller row), exchanges rows jp + j and the winner's from the
+//      published copies, scales the column below the pivot by the pivot's
+//      reciprocal and applies the rank-1 update to the rest of its rows.
+// A zero pivot (LAPACK's info > 0) leaves the column as it is and records the
+// first such column in *info (1-based).  The winner rows go to ipiv; CTA 0
+// finally turns the panel's exchanges into a list of row moves (dst <- src)
+// that k_laswp applies to the other columns.
+__global__ void __launch_bounds__(GETF2_THREADS, 1)
+k_getf2(float* __restrict__ W, long long ldw, long long n, long long jp, int nb, int R, int* __restrict__ ipiv,
+        int* info, PivCand* cand, float* crow, float* top, unsigned* bar, int* plan, int* err) {
+  extern __shared__ float P[];  // [nb][R]
+  __shared__ float s_u[LNB];
+  __shared__ float s_rv[32];
+  __shared__ int s_ri[32];
+  __shared__ int s_abort;
+  __shared__ int s_piv[LNB];
+  const int tid = threadIdx.x, G = gridDim.x, g = blockIdx.x;
+  const long long rbeg = jp + (long long)g * R;
+  const int rows = (int)max(0LL, min((long long)R, n - rbeg));
+  for (int e = tid; e < nb * R; e += blockDim.x) {
+    const int c = e / R, r = e % R;
+    P[e] = r < rows ? W[(rbeg + r) + (jp + c) * ldw] : 0.f;
+  }
+  if (tid == 0) s_abort = 0;
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    const int q = j & 1;
+    const long long trow = jp + j;  // the position this column's pivot moves to
+    float best = -1.f;
+    int bi = -1;
+    for (int r = tid; r < rows; r += blockDim.x) {
+      if (rbeg + r < trow) continue;
+      const float v = fabsf(P[j * R + r]);
+      if (piv_better(v, (int)(rbeg + r), best, bi)) { best = v; bi = (int)(rbeg + r); }
+    }
+    block_argmax(best, bi, s_rv, s_ri);
+    if (tid == 0) {
+      const long long raw = ((long long)bi << 32) | (long long)(unsigned)__float_as_int(best);
+      reinterpret_cast<long long*>(cand)[q * G + g] = raw;
+    }
+    if (bi >= 0 && tid < nb) crow[((size_t)q * G + g) * LNB + tid] = P[tid * R + (int)(bi - rbeg)];
+    if (trow >= rbeg && trow < rbeg + rows && tid < nb) top[q * LNB + tid] = P[tid * R + (int)(trow - rbeg)];
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      atomicAdd(bar, 1u);
+      const unsigned target = (unsigned)(j + 1) * (unsigned)G;
+      bool ok = false;
+      for (long long it = 0; it < GRID_WAIT_LIMIT; ++it) {
+        if (ld_acquire_u32(bar) >= target) { ok = true; break; }
+        if (it > 64) __nanosleep(64);
+      }
+      if (!ok) {
+        s_abort = 1;
+        atomicExch(err, 3);
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (s_abort) return;
+    // the winner among the G candidates
+    float v = -1.f;
+    int wr = -1, wc = -1;
+    if (tid < G) {
+      // one 8-byte load of (|value|, row), past L1 (written by other CTAs)
+      const long long raw = __ldcg(reinterpret_cast<const long long*>(cand) + q * G + tid);
+      v = __int_as_float((int)(raw & 0xffffffffLL));
+      wr = (int)(raw >> 32);
+    }
+    // the winner's CTA follows from its row
+    block_argmax(v, wr, s_rv, s_ri);
+    if (wr >= 0) wc = (int)((wr - jp) / R);
+    if (tid < nb) s_u[tid] = wr >= 0 ? __ldcg(crow + ((size_t)q * G + wc) * LNB + tid) : 0.f;
+    __syncthreads();
+    const float pv = wr >= 0 ? s_u[j] : 0.f;
+    if (wr < 0 || pv == 0.f) {
+      // zero pivot: LAPACK records the first one and leaves the column
+      if (g == 0 && tid == 0) {
+        ipiv[trow] = (int)trow;
+        s_piv[j] = (int)trow;
+        atomicCAS(info, 0, (int)(trow + 1));
+      }
+      __syncthreads();
+      continue;
+    }
+    if (g == 0 && tid == 0) {
+      ipiv[trow] = wr;
+      s_piv[j] = wr;
+    }
+    if ((long long)wr != trow) {
+      if (trow >= rbeg && trow < rbeg + rows && tid < nb) P[tid * R + (int)(trow - rbeg)] = s_u[tid];
+      if (wr >= rbeg && wr < rbeg + rows && tid < nb) P[tid * R + (int)(wr - rbeg)] = __ldcg(top + q * LNB + tid);
+    }
+    __syncthreads();
+    const float pinv = __frcp_rn(pv);
+    for (int r = tid; r < rows; r += blockDim.x)
+      if (rbeg + r > trow) P[j * R + r] *= pinv;
+    __syncthreads();
+    const int ncol = nb - 1 - j;
+    for (int e = tid; e < ncol * rows; e += blockDim.x) {
+      const int c = j + 1 + e / rows, r = e % rows;
+      if (rbeg + r > trow) P[c * R + r] = fmaf(-P[j * R + r], s_u[c], P[c * R + r]);
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < nb * R; e += blockDim.x) {
+    const int c = e / R, r = e % R;
+    if (r < rows) W[(rbeg + r) + (jp + c) * ldw] = P[e];
+  }
+  // the panel's exchanges as row moves: position jp + k receives the content
+  // that the exchanges leave there (warp 0 of CTA 0 replays them)
+  if (g == 0 && tid < 32) {
+    int* cnt = plan;
+    int* dst = plan + 1;
+    int* src = plan + 1 + 2 * LNB;
+    __shared__ int s_in[LNB];        // content of positions jp .. jp + nb - 1
+    __shared__ int s_key[LNB], s_val[LNB];
+    __shared__ int s_nout;
+    for (int k = tid; k < nb; k += 32) s_in[k] = (int)(jp + k);
+    if (tid == 0) s_nout = 0;
+    __syncwarp();
+    for (int k = 0; k < nb; ++k) {
+      const int p = s_piv[k];
+      if (p == (int)(jp + k)) continue;
+      if (p < jp + nb) {
+        if (tid == 0) {
+          const int t = s_in[k];
+          s_in[k] = s_in[p - jp];
+          s_in[p - jp] = t;
+        }
+      } else {
+        // find p among the rows outside the panel moved so far
+        int found = -1;
+        const int nout = s_nout;
+        for (int b = 0; b < nout; b += 32) {
+          const unsigned m = __ballot_sync(0xffffffffu, b + tid < nout && s_key[b + tid] == p);
+          if (m) { found = b + __ffs(m) - 1; break; }
+        }
+        if (tid == 0) {
+          if (found >= 0) {
+            const int t = s_in[k];
+            s_in[k] = s_val[found];
+            s_val[found] = t;
+          } else {
+            s_key[nout] = p;
+            s_val[nout] = s_in[k];
+            s_in[k] = p;
+            s_nout = nout + 1;
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (tid == 0) {
+      int c = 0;
+      for (int k = 0; k < nb; ++k)
+        if (s_in[k] != (int)(jp + k)) { dst[c] = (int)(jp + k); src[c] = s_in[k]; ++c; }
+      for (int t = 0; t < s_nout; ++t)
+        if (s_val[t] != s_key[t]) { dst[c] = s_key[t]; src[c] = s_val[t]; ++c; }
+      *cnt = c;
+    }
+  }
+}
+
+// The panel's row moves (dst <- src, all reads before all writes) applied to
+// columns [c0, c0 + ncols) and [c1, c1 + ncols1) of W, 32 columns per CTA.
+constexpr int LASWP_COLS = 32;
+__global__ void __launch_bounds__(256)
+k_laswp(float* __restrict__ W, long long ldw, const int* __restrict__ plan, long long c0, long long ncols0,
+        long long c1, long long ncols1) {
+  __shared__ float tile[2 * LNB * LASWP_COLS];
+  __shared__ int s_dst[2 * LNB], s_src[2 * LNB];
+  const int cnt = plan[0];
+  if (cnt == 0) return;
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    s_dst[t] = plan[1 + t];
+    s_src[t] = plan[1 + 2 * LNB + t];
+  }
+  const long long t0 = (long long)blockIdx.x * LASWP_COLS;
+  __syncthreads();
+  const int total = cnt * LASWP_COLS;
+  auto col_of = [&](int cc) -> long long {
+    const long long t = t0 + cc;
+    if (t < ncols0) return c0 + t;
+    if (t - ncols0 < ncols1) return c1 + (t - ncols0);
+    return -1;
+  };
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    const int i = e % cnt, cc = e / cnt;
+    const long long c = col_of(cc);
+    tile[e] = c >= 0 ? W[(long long)s_src[i] + c * ldw] : 0.f;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    const int i = e % cnt, cc = e / cnt;
+    const long long c = col_of(cc);
+    if (c >= 0) W[(long long)s_dst[i] + c * ldw] = tile[e];
+  }
+}
+
+// Inverses of the factored diagonal block (unit-lower and upper triangles)
+// and the block itself rounded into the factor.
+template <typename F>
+__global__ void __launch_bounds__(DIAG_THREADS, 1)
+k_piv_diag(const float* __restrict__ W, long long ldw, long long j0, int nbk, F* __restrict__ LU, long long ldf,
+           float* __restrict__ Linv, float* __restrict__ Uinv) {
+  extern __shared__ float sm[];
+  float* T = sm;
+  float* XL = sm + LNB * DP;
+  float* XU = sm + 2 * LNB * DP;
+  float* Tmp = sm + 3 * LNB * DP;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < LNB * LNB; idx += DIAG_THREADS) {
+    const int r = idx % LNB, c = idx / LNB;
+    T[r * DP + c] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
+  }
+  __syncthreads();
+  for (int idx = tid; idx < nbk * nbk; idx += blockDim.x) {
+    const int r = idx % nbk, c = idx / nbk;
+    LU[(j0 + r) + (j0 + c) * ldf] = from_f32<F>(T[r * DP + c]);
+  }
+  tri_inverses(T, XL, XU, Tmp);
+  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
+    const int r = idx % LNB, c = idx / LNB;
+    Linv[c * LNB + r] = XL[r * DP + c];
+    Uinv[c * LNB + r] = XU[r * DP + c];
+  }
+}
+
+// L21 (rows [r0, n) of the panel's columns in W) into the K-major operand
+// Lp[(r - r0) * pitch + k], rounded to the factor type; 32 rows per CTA.
+template <typename F>
+__global__ void __launch_bounds__(256)
+k_make_lop(const float* __restrict__ W, long long ldw, long long jp, int nb, long long r0, long long n,
+           F* __restrict__ Lp, long long pitch) {
+  __shared__ float t[LNB][33];
+  const long long rb = r0 + (long long)blockIdx.x * 32;
+  for (int e = threadIdx.x; e < 32 * LNB; e += blockDim.x) {
+    const int i = e % 32, k = e / 32;
+    t[k][i] = (k < nb && rb + i < n) ? W[(rb + i) + (jp + k) * ldw] : 0.f;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < 32 * LNB; e += blockDim.x) {
+    const int k = e % LNB, i = e / LNB;
+    if (rb + i < n && k < nb) Lp[(rb + i - r0) * pitch + k] = from_f32<F>(t[k][i]);
+  }
+}
+
+// The strictly lower part below the diagonal blocks, W -> factor (rounded).
+template <typename F>
+__global__ void k_store_lower(const float* __restrict__ W, long long ldw, long long n, F* __restrict__ LU,
+                              long long ldf) {
+  for (long long c = blockIdx.y; c < n; c += gridDim.y) {
+    const long long rs = (c / LNB + 1) * LNB;
+    for (long long r = rs + (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+         r += (long long)gridDim.x * blockDim.x)
+      LU[r + c * ldf] = from_f32<F>(W[r + c * ldw]);
+  }
+}
+
 // ---------------------------------------------------------------- host side
 
 // First ticket of the next triangular solves; 0 except under a test hook
@@ -1112,9 +1538,11 @@ static int lu_apply_t(const void* fbuf, long long n, int fdtype, const float* v,
   const size_t smem = (size_t)LNB * LNB * sizeof(float);
   MPDOK_TRY(set_smem(k_trsv<F, true>, smem));
   MPDOK_TRY(set_smem(k_trsv<F, false>, smem));
-  launch(k_trsv<F, true>, L.nblk, 256, smem, s, LU, L.ldf, Linv, Ml, n, L.nblk, v, d, y, tk, err, skip);
-  launch(k_trsv<F, false>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, Mu, n, L.nblk, (const float*)y, d, zz, tk + 1,
-         err, skip);
+  const float* dr = (const float*)(fb + L.off_dr);
+  const int* perm = (const int*)(fb + L.off_perm);
+  launch(k_trsv<F, true>, L.nblk, 256, smem, s, LU, L.ldf, Linv, Ml, n, L.nblk, v, dr, perm, y, tk, err, skip);
+  launch(k_trsv<F, false>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, Mu, n, L.nblk, (const float*)y, d, perm, zz,
+         tk + 1, err, skip);
   launch(k_scale_out, grid_for(n), 256, 0, s, (const float*)zz, d, z, n, skip);
   prof_stop(slot, s, (double)n * (double)n * sizeof(F), skip);
   MPDOK_LAUNCH_CHECK("lu apply");
@@ -1313,7 +1741,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   int* errw = (int*)(wb + w.off_err);
   MPDOK_CUDA_TRY(cudaMemsetAsync(errw, 0, 64, s));
   MPDOK_CUDA_TRY(cudaMemsetAsync(meta, 0, sizeof(LUMeta), s));
-  launch(k_diag_scale, grid_for(n), 256, 0, s, A, lda, n, d);
+  launch(k_diag_scale, grid_for(n), 256, 0, s, A, lda, n, d, (float*)(fb + L.off_dr), (int*)(fb + L.off_perm));
   dim3 g2((unsigned)std::min<long long>((n + 255) / 256, 16), (unsigned)std::min<long long>(n, 65535));
   launch(k_scaled_copy, g2, 256, 0, s, A, lda, n, (const float*)d, W, w.ldw);
   MPDOK_LAUNCH_CHECK("lu scale");
@@ -1462,6 +1890,161 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   return MPDOK_OK;
 }
 
+// Rows per CTA of the pivoted panel factorization for m panel rows, or -1
+// when the slices would not fit in shared memory.
+static int piv_rows_per_cta(long long m, int nb, int* grid) {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return -1;
+  const int g0 = std::min(PIV_MAX_CTAS, num_sms());
+  long long R = (m + g0 - 1) / g0;
+  R = std::max(32LL, (R + 31) / 32 * 32);
+  const long long budget = (long long)optin - 8 * 1024;  // the kernel's static shared memory and slack
+  if (R * nb * (long long)sizeof(float) > budget) return -1;
+  *grid = (int)((m + R - 1) / R);
+  return (int)R;
+}
+
+template <typename F>
+static int lu_factor_piv(const double* A, long long lda, long long n, int fdtype, void* fbuf, void* work,
+                         cudaStream_t s, int* info_host) {
+  const LULayout L = lu_layout(n, fdtype);
+  const LUWork w = lu_work_layout(n, fdtype);
+  char* fb = (char*)fbuf;
+  char* wb = (char*)work;
+  F* LU = (F*)(fb + L.off_lu);
+  float* Linv = (float*)(fb + L.off_linv);
+  float* Uinv = (float*)(fb + L.off_uinv);
+  float* dc = (float*)(fb + L.off_d);
+  float* dr = (float*)(fb + L.off_dr);
+  int* perm = (int*)(fb + L.off_perm);
+  int* ipiv = (int*)(fb + L.off_ipiv);
+  LUMeta* meta = (LUMeta*)(fb + L.off_meta);
+  float* W = (float*)(wb + w.off_W);
+  F* Lp = (F*)(wb + w.off_Lp);
+  F* Up = (F*)(wb + w.off_Up);
+  const long long pitch = super_panel_width(fdtype);
+  int* errw = (int*)(wb + w.off_err);  // [0] tensor-core wait, [2] first zero pivot, [3] panel barrier wait
+  PivCand* cand = (PivCand*)(wb + w.off_cand);
+  float* crow = (float*)(wb + w.off_crow);
+  float* top = (float*)(wb + w.off_top);
+  unsigned* bar = (unsigned*)(wb + w.off_bar);
+  int* plan = (int*)(wb + w.off_plan);
+  unsigned long long* rmax = (unsigned long long*)(wb + w.off_scale);
+  MPDOK_CUDA_TRY(cudaMemsetAsync(errw, 0, 64, s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(meta, 0, sizeof(LUMeta), s));
+  // equilibration W = Dr A Dc (powers of two)
+  MPDOK_CUDA_TRY(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long) * n, s));
+  const long long cchunk = 256;
+  dim3 gr((unsigned)((n + 255) / 256), (unsigned)std::min<long long>((n + cchunk - 1) / cchunk, 65535));
+  launch(k_row_absmax, gr, 256, 0, s, A, lda, n, (n + gr.y - 1) / gr.y, rmax);
+  launch(k_row_scale, grid_for(n), 256, 0, s, (const unsigned long long*)rmax, n, dr, perm);
+  launch(k_col_scale_copy, (unsigned)n, 256, 0, s, A, lda, n, (const float*)dr, dc, W, w.ldw);
+  MPDOK_LAUNCH_CHECK("lu equilibration");
+  constexpr size_t smem_tp = trsm_pair_smem(64);
+  MPDOK_TRY(set_smem(k_piv_diag<F>, DIAG_SMEM));
+  MPDOK_TRY(set_smem(k_trsm_pair<F, 64>, smem_tp));
+  for (long long jp = 0; jp < n; jp += LNB) {
+    const int nb = (int)std::min<long long>(LNB, n - jp);
+    const long long m = n - jp;
+    int G = 0;
+    const int R = piv_rows_per_cta(m, nb, &G);
+    if (R < 0) {
+      set_error("pivoted LU: a %lld-row panel does not fit the co-resident CTAs' shared memory (n too large for "
+                "pivoting = 1 on this device)", m);
+      return MPDOK_ERR_UNSUPPORTED;
+    }
+    const size_t smem = (size_t)nb * R * sizeof(float);
+    MPDOK_TRY(set_smem(k_getf2, smem));
+    MPDOK_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(unsigned), s));
+    {
+      float* aW = W;
+      long long aldw = w.ldw, an = n, ajp = jp;
+      int anb = nb, aR = R;
+      int* aipiv = ipiv;
+      int* ainfo = errw + 2;
+      int* aerr = errw + 3;
+      void* args[] = {&aW, &aldw, &an, &ajp, &anb, &aR, &aipiv, &ainfo, &cand, &crow, &top, &bar, &plan, &aerr};
+      MPDOK_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_getf2, dim3(G), dim3(GETF2_THREADS), args, smem, s));
+      count_launch();
+    }
+    const long long rest = n - jp - nb;
+    if (jp + rest > 0) {
+      const unsigned gl = (unsigned)((jp + rest + LASWP_COLS - 1) / LASWP_COLS);
+      launch(k_laswp, gl, 256, 0, s, W, w.ldw, (const int*)plan, 0LL, jp, jp + nb, rest);
+    }
+    const int k = (int)(jp / LNB);
+    launch(k_piv_diag<F>, 1, DIAG_THREADS, DIAG_SMEM, s, (const float*)W, w.ldw, jp, nb, LU, L.ldf,
+           Linv + (size_t)k * LNB * LNB, Uinv + (size_t)k * LNB * LNB);
+    MPDOK_LAUNCH_CHECK("pivoted panel");
+    if (rest <= 0) continue;
+    const long long r1 = jp + nb;
+    // U12 = L11^-1 W12 (rows jp .. jp + 128, every column to the right)
+    launch(k_trsm_pair<F, 64>, (unsigned)((rest + 63) / 64), TRSM_THREADS, smem_tp, s, (const float*)W, w.ldw, jp,
+           r1, n, (const float*)(Uinv + (size_t)k * LNB * LNB), (const float*)(Linv + (size_t)k * LNB * LNB), Lp, Up,
+           pitch, r1, 0, LU, L.ldf, 0);
+    launch(k_make_lop<F>, (unsigned)((rest + 31) / 32), 256, 0, s, (const float*)W, w.ldw, jp, nb, r1, n, Lp, pitch);
+    MPDOK_LAUNCH_CHECK("pivoted panel solve");
+    float* C = W + r1 + r1 * w.ldw;
+    if (fdtype == MPDOK_F32) {
+      const int gs = prof_start(MPDOK_PROF_LU_GEMM, s);
+      dim3 gg((unsigned)((rest + 127) / 128), (unsigned)((rest + 127) / 128));
+      launch(k_gemm_update_f32, gg, 256, 0, s, C, w.ldw, (const float*)Lp, (const float*)Up, pitch, (int)rest,
+             (int)rest, nb);
+      prof_stop(gs, s, 2.0 * (double)rest * (double)rest * nb);
+      prof_stop_bytes(gs, 8.0 * (double)rest * (double)rest + 4.0 * nb * 2.0 * (double)rest);
+      MPDOK_LAUNCH_CHECK("pivoted update f32");
+    } else {
+      MPDOK_TRY(gemm_update(C, w.ldw, Lp, Up, pitch, (int)rest, (int)rest, nb, fdtype, MPDOK_ENGINE_TENSOR, errw, s));
+    }
+  }
+  {
+    dim3 g2((unsigned)std::min<long long>((n + 255) / 256, 16), (unsigned)std::min<long long>(n, 65535));
+    launch(k_store_lower<F>, g2, 256, 0, s, (const float*)W, w.ldw, n, LU, L.ldf);
+    const size_t smem_ct = 2 * (size_t)LNB * LNB * sizeof(float);
+    MPDOK_TRY(set_smem(k_trsv_chain_tiles<F>, smem_ct));
+    launch(k_trsv_chain_tiles<F>, dim3(L.nblk, 2), 256, smem_ct, s, (const F*)LU, L.ldf, (const float*)Linv,
+           (const float*)Uinv, (float*)(fb + L.off_ml), (float*)(fb + L.off_mu), n, L.nblk);
+    MPDOK_LAUNCH_CHECK("pivoted factor store");
+  }
+  int herr[4] = {0, 0, 0, 0};
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(herr, errw, sizeof(herr), cudaMemcpyDeviceToHost, s));
+  std::vector<int> hp((size_t)n), hperm((size_t)n);
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(hp.data(), ipiv, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  if (herr[0] != 0) {
+    set_error("tensor-core update timed out waiting on an mbarrier");
+    return MPDOK_ERR_TIMEOUT;
+  }
+  if (herr[3] != 0) {
+    set_error("pivoted panel factorization: the grid barrier wait ran out");
+    return MPDOK_ERR_TIMEOUT;
+  }
+  // P as a gather: (P x)_i = x_perm[i], the row exchanges of ipiv applied in order
+  for (long long i = 0; i < n; ++i) hperm[(size_t)i] = (int)i;
+  for (long long i = 0; i < n; ++i) {
+    const int p = hp[(size_t)i];
+    if (p < 0 || p >= n) {
+      set_error("pivoted LU: invalid pivot row %d at step %lld", p, i);
+      return MPDOK_ERR_CUDA;
+    }
+    std::swap(hperm[(size_t)i], hperm[(size_t)p]);
+  }
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(perm, hperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  LUMeta hm;
+  hm.n_lo = (int)(n & 0x7fffffff);
+  hm.n_hi = (int)(n >> 31);
+  hm.fdtype = fdtype;
+  hm.pivoting = 1;
+  hm.nperturbed = 0;
+  hm.valid = 1;
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(meta, &hm, sizeof(hm), cudaMemcpyHostToDevice, s));
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  if (info_host) *info_host = herr[2];
+  return MPDOK_OK;
+}
+
 static int read_meta(const void* fbuf, long long n, int fdtype, LUMeta* hm, cudaStream_t s) {
   const LULayout L = lu_layout(n, fdtype);
   MPDOK_CUDA_TRY(cudaMemcpyAsync(hm, (const char*)fbuf + L.off_meta, sizeof(LUMeta), cudaMemcpyDeviceToHost, s));
@@ -1549,7 +2132,7 @@ extern "C" int mpdok_lu_factor(const double* A, long long lda, long long n, int 
                                size_t factor_bytes, void* work, size_t work_bytes, cudaStream_t s) {
   MPDOK_ARG_CHECK(n >= 0, "negative n");
   MPDOK_ARG_CHECK(fdtype == MPDOK_BF16 || fdtype == MPDOK_F16 || fdtype == MPDOK_F32, "factor dtype");
-  MPDOK_ARG_CHECK(pivoting == 0, "partial pivoting is not implemented; use pivoting = 0");
+  MPDOK_ARG_CHECK(pivoting == 0 || pivoting == 1, "pivoting must be 0 (none) or 1 (partial, by rows)");
   if (n == 0) return MPDOK_OK;
   MPDOK_ARG_CHECK(A && factors && work, "null pointer");
   MPDOK_ARG_CHECK(lda >= n, "lda < n");
@@ -1558,6 +2141,15 @@ extern "C" int mpdok_lu_factor(const double* A, long long lda, long long n, int 
   MPDOK_ARG_CHECK(n < (1LL << 31), "n too large");
   int np = 0;
   int st;
+  if (pivoting == 1) {
+    switch (fdtype) {
+      case MPDOK_BF16: st = lu_factor_piv<__nv_bfloat16>(A, lda, n, fdtype, factors, work, s, &np); break;
+      case MPDOK_F16: st = lu_factor_piv<__half>(A, lda, n, fdtype, factors, work, s, &np); break;
+      default: st = lu_factor_piv<float>(A, lda, n, fdtype, factors, work, s, &np); break;
+    }
+    if (st < 0) return st;
+    return np;  // LAPACK's info: 0, or the first column whose pivot is exactly zero (1-based)
+  }
   switch (fdtype) {
     case MPDOK_BF16: st = lu_factor_t<__nv_bfloat16>(A, lda, n, fdtype, pivoting, factors, work, s, &np); break;
     case MPDOK_F16: st = lu_factor_t<__half>(A, lda, n, fdtype, pivoting, factors, work, s, &np); break;
@@ -1565,6 +2157,54 @@ extern "C" int mpdok_lu_factor(const double* A, long long lda, long long n, int 
   }
   if (st < 0) return st;
   return np;
+}
+
+template <typename F>
+__global__ void k_export_lu(const F* __restrict__ LU, long long ldf, long long n, float* __restrict__ out,
+                            long long ldo) {
+  for (long long c = blockIdx.y; c < n; c += gridDim.y)
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x)
+      out[r + c * ldo] = to_f32<F>(LU[r + c * ldf]);
+}
+
+// The factors in plain form: L\U (unit L below the diagonal, U on and above)
+// as an n x n column-major FP32 matrix, LAPACK's 0-based pivot rows, the row
+// permutation as a gather ((P x)_i = x_perm[i]) and the two scalings, so that
+// P (Dr A Dc) = L U.  Any output may be NULL.
+extern "C" int mpdok_lu_export(const void* factors, long long n, int fdtype, float* lu, long long ldo, int* ipiv,
+                               int* perm, float* dr, float* dc, cudaStream_t s) {
+  MPDOK_ARG_CHECK(n >= 0 && factors, "n >= 0 and a factor buffer");
+  MPDOK_ARG_CHECK(fdtype == MPDOK_BF16 || fdtype == MPDOK_F16 || fdtype == MPDOK_F32, "factor dtype");
+  if (n == 0) return MPDOK_OK;
+  LUMeta hm;
+  MPDOK_TRY(read_meta(factors, n, fdtype, &hm, s));
+  if (!hm.valid || hm.fdtype != fdtype || hm.n_lo != (int)(n & 0x7fffffff)) {
+    set_error("no factorization of this size / type in the factor buffer");
+    return MPDOK_ERR_NOT_FACTORED;
+  }
+  const LULayout L = lu_layout(n, fdtype);
+  const char* fb = (const char*)factors;
+  if (lu) {
+    MPDOK_ARG_CHECK(ldo >= n, "ldo < n");
+    dim3 g((unsigned)std::min<long long>((n + 255) / 256, 16), (unsigned)std::min<long long>(n, 65535));
+    switch (fdtype) {
+      case MPDOK_BF16: launch(k_export_lu<__nv_bfloat16>, g, 256, 0, s, (const __nv_bfloat16*)(fb + L.off_lu), L.ldf, n, lu, ldo); break;
+      case MPDOK_F16: launch(k_export_lu<__half>, g, 256, 0, s, (const __half*)(fb + L.off_lu), L.ldf, n, lu, ldo); break;
+      default: launch(k_export_lu<float>, g, 256, 0, s, (const float*)(fb + L.off_lu), L.ldf, n, lu, ldo); break;
+    }
+    MPDOK_LAUNCH_CHECK("lu export");
+  }
+  if (ipiv) {
+    if (hm.pivoting) {
+      MPDOK_CUDA_TRY(cudaMemcpyAsync(ipiv, fb + L.off_ipiv, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+    } else {
+      MPDOK_CUDA_TRY(cudaMemcpyAsync(ipiv, fb + L.off_perm, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  if (perm) MPDOK_CUDA_TRY(cudaMemcpyAsync(perm, fb + L.off_perm, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+  if (dr) MPDOK_CUDA_TRY(cudaMemcpyAsync(dr, fb + L.off_dr, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+  if (dc) MPDOK_CUDA_TRY(cudaMemcpyAsync(dc, fb + L.off_d, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+  return MPDOK_OK;
 }
 
 extern "C" int mpdok_lu_apply(const void* factors, long long n, int fdtype, const float* v, float* z, void* work,
@@ -1717,9 +2357,11 @@ static int lu_apply_multi_t(const void* fbuf, long long n, int fdtype, const flo
   MPDOK_TRY(set_smem(k_trsv_multi<F, true, K>, smem));
   MPDOK_TRY(set_smem(k_trsv_multi<F, false, K>, smem));
   const int slot = prof_start(MPDOK_PROF_TRSV, s);
-  launch(k_trsv_multi<F, true, K>, L.nblk, 256, smem, s, LU, L.ldf, Linv, Ml, n, L.nblk, v, n, d, y, tk, err);
-  launch(k_trsv_multi<F, false, K>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, Mu, n, L.nblk, (const float*)y, n, d, zz,
-         tk + 1, err);
+  const float* dr = (const float*)(fb + L.off_dr);
+  const int* perm = (const int*)(fb + L.off_perm);
+  launch(k_trsv_multi<F, true, K>, L.nblk, 256, smem, s, LU, L.ldf, Linv, Ml, n, L.nblk, v, n, dr, perm, y, tk, err);
+  launch(k_trsv_multi<F, false, K>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, Mu, n, L.nblk, (const float*)y, n, d,
+         perm, zz, tk + 1, err);
   launch(k_scale_out_multi, grid_for(n * K), 256, 0, s, (const float*)zz, d, z, n, n, K);
   prof_stop(slot, s, (double)n * (double)n * sizeof(F));
   MPDOK_LAUNCH_CHECK("lu apply multi");

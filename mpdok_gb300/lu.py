@@ -4,6 +4,8 @@
 128-wide FP32 panels and a tcgen05 trailing update whose operands are rounded
 to BF16 or FP16 (FP32 accumulation).  ``dtype='fp32'`` keeps FP32 operands and
 runs the update on CUDA cores (the reference's Sgetrf precision).
+``pivoting=True`` equilibrates rows and columns by powers of two and pivots by
+rows (P Dr A Dc = L U), the reference's cusolverDnSgetrf semantics.
 
 The factorization is then used as
 * a direct refinement solver: ``solve_ir`` (LU-IR, benchmark_mpdok.ipynb:982-993),
@@ -34,9 +36,13 @@ class LUFactorization:
     """Factors of one dense matrix, owned in a device buffer."""
 
     def __init__(self, A, dtype: str = "fp16", pivoting: bool = False, work: Workspace | None = None):
-        if pivoting:
-            raise NotImplementedError("partial pivoting is not implemented: the LU is unpivoted with pivot perturbation")
+        """pivoting=False: W = D A D with D = diag(1/sqrt|a_ii|), no row exchanges
+        (SPD / diagonally dominant systems; tiny pivots perturbed, counted in
+        ``n_perturbed``).  pivoting=True: power-of-two row / column
+        equilibration and partial pivoting by rows, P (Dr A Dc) = L U as
+        LAPACK getrf; ``info`` is LAPACK's (first exactly zero pivot, 1-based)."""
         self.fdtype = DTYPES[dtype]
+        self.pivoting = bool(pivoting)
         self.dtype = dtype
         A64 = as_fortran(A, torch.float64)
         self.n = n = int(A64.shape[0])
@@ -45,11 +51,27 @@ class LUFactorization:
                                    device=A64.device)
         ws = work or Workspace()
         w = ws.get(lib.mpdok_lu_work_size(n, self.fdtype))
-        st = lib.mpdok_lu_factor(ptr(A64), n, n, self.fdtype, 0, ptr(self.factors), self.factors.numel(), ptr(w),
-                                 w.numel(), stream_handle())
+        st = lib.mpdok_lu_factor(ptr(A64), n, n, self.fdtype, 1 if self.pivoting else 0, ptr(self.factors),
+                                 self.factors.numel(), ptr(w), w.numel(), stream_handle())
         N.check(st, "lu_factor")
-        self.n_perturbed = int(st)
+        self.n_perturbed = 0 if self.pivoting else int(st)
+        self.info = int(st) if self.pivoting else 0
         self._ws = Workspace()
+
+    def export(self):
+        """(LU, ipiv, perm, dr, dc) as CUDA tensors: L\\U column-major FP32 (unit L
+        below the diagonal), LAPACK's 0-based pivot rows, the gather
+        permutation ((P x)_i = x[perm[i]]) and the scalings, P (Dr A Dc) = L U."""
+        n = self.n
+        dev = self.factors.device
+        LU = fortran_empty(n, n, torch.float32, dev)
+        ipiv = torch.empty(n, dtype=torch.int32, device=dev)
+        perm = torch.empty(n, dtype=torch.int32, device=dev)
+        dr = torch.empty(n, dtype=torch.float32, device=dev)
+        dc = torch.empty(n, dtype=torch.float32, device=dev)
+        N.check(N.load().mpdok_lu_export(ptr(self.factors), n, self.fdtype, ptr(LU), n, ptr(ipiv), ptr(perm),
+                                         ptr(dr), ptr(dc), stream_handle()), "lu_export")
+        return LU, ipiv, perm, dr, dc
 
     def apply(self, v) -> torch.Tensor:
         """z = A^-1 v through the factors (FP32 vectors)."""

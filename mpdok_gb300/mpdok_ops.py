@@ -178,9 +178,11 @@ class LUIRSolver:
     """LU with FP64 iterative refinement over the lu_ir.so symbols (mpdok_ops.py:69-320).
 
     ``factor(A)`` keeps one process-wide FP32 factorization in the library
-    (blocked LU on sm_103a, panels in FP32); ``solve_factored(b)`` refines with
-    FP64 residuals; ``solve(A, b)`` does both.  For BF16 / FP16 tensor-core
-    factors use ``mpdok_gb300.lu.LUFactorization`` instead.
+    (blocked LU on sm_103a with partial pivoting by rows, as Sgetrf);
+    ``solve_factored(b)`` refines with FP64 residuals; ``solve(A, b)`` does
+    both.  ``factor`` raises when LAPACK's info is not 0 (an exactly zero
+    pivot).  For BF16 / FP16 tensor-core factors use
+    ``mpdok_gb300.lu.LUFactorization`` instead.
     """
 
     def __init__(self, lib_path=None):

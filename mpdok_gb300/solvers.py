@@ -16,7 +16,7 @@ import warnings
 import torch
 
 from . import _native as N
-from ._device import Workspace, as_fortran, as_vector, fortran_empty, ptr, stream_handle
+from ._device import Workspace, as_fortran, as_vector, fortran_empty, ptr, stream_handle, upload_fortran
 
 
 def _info_dict(info: N.SolveInfo) -> dict:
@@ -56,11 +56,20 @@ class MixedSolver:
                 f"{self.inner_tol:g}); FP64 residual/update")
 
     def solve(self, A, b, tol: float = 1e-12):
-        A64 = as_fortran(A, torch.float64)
+        """x, info for A x = b.  A may live on the host: then it is uploaded
+        straight into its device buffer, and for the LU method its FP32 copy
+        is made block by block while the rest of A is still in flight."""
         b64 = as_vector(b, torch.float64)
-        n = A64.shape[0]
+        n = int(A.shape[0])
         if self._a32 is None or self._a32.shape[0] != n:
             self._a32 = fortran_empty(n, n, torch.float32)
+        a32_ready = False
+        if isinstance(A, torch.Tensor) and not A.is_cuda and A.dtype == torch.float64 and A.dim() == 2 \
+                and self.method != "gmres-ir":
+            A64 = upload_fortran(A, out32=self._a32)
+            a32_ready = True
+        else:
+            A64 = as_fortran(A, torch.float64)
         x = torch.zeros(n, dtype=torch.float64, device=b64.device)
         lib = N.load()
         info = N.SolveInfo()
@@ -73,7 +82,8 @@ class MixedSolver:
         from .lu import LUFactorization
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         ev[0].record()
-        N.check(lib.mpdok_convert(ptr(A64), N.F64, ptr(self._a32), N.F32, n * n, stream_handle()), "convert")
+        if not a32_ready:
+            N.check(lib.mpdok_convert(ptr(A64), N.F64, ptr(self._a32), N.F32, n * n, stream_handle()), "convert")
         lu = LUFactorization(A64, dtype=self.factor_dtype, work=self._fws)
         ev[1].record()
         x, d = lu.gmres_ir(A64, b64, A32=self._a32, tol=tol, maxiter_outer=self.maxiter_outer,

@@ -6,8 +6,11 @@ can be set before NumPy loads.  It times scipy.linalg.lu_factor + lu_solve
 (FP64, partial pivoting) plus FP64 refinement steps until the relative
 residual meets the tolerance, on the same seeded RBF family as the GPU run.
 
-    python -m oracle.cpu_baseline --n 8192 --repeats 1 --config HEADLINE
-prints one JSON line: {"seconds": [...], "n": ..., "threads": ..., "relres": ...}
+    python -m oracle.cpu_baseline --n 32768 --repeats 2 --warmup-n 2048 --config HEADLINE
+prints one JSON line: {"seconds": [...], "n": ..., "threads": ..., "relres": ..., "assembly_seconds": ...}.
+Each repeat is one full solve of the N-point system (no sampling, no
+scaling); --warmup-n runs one untimed solve of a small system of the same
+family first, so that the BLAS threads are up before the timed solves.
 
     python -m oracle.cpu_baseline --config C4 --systems 0,37,101
 times SciPy FP64 cho_factor + cho_solve (8 RHS) on the listed C4 systems and
@@ -29,6 +32,7 @@ def main(argv=None):
     ap.add_argument("--config", default="HEADLINE")
     ap.add_argument("--tol", type=float, default=1e-12)
     ap.add_argument("--systems", default="")
+    ap.add_argument("--warmup-n", type=int, default=0)
     args = ap.parse_args(argv)
 
     import numpy as np
@@ -55,25 +59,41 @@ def main(argv=None):
                           "threads": int(os.environ.get("OPENBLAS_NUM_THREADS", "0")), "config": "C4"}))
         return
 
-    gen = {"HEADLINE": configs.headline, "C3": configs.c3}[args.config.upper()]
-    sysm = gen(n=args.n)
-    A = np.asfortranarray(rbf_matrix(sysm.coords, gamma=sysm.gamma, reg=sysm.reg, kernel=sysm.kernel))
-    b = np.asarray(sysm.b, dtype=np.float64)
-    bn = float(np.linalg.norm(b))
-    times, rel = [], float("nan")
-    for _ in range(args.repeats):
-        t0 = time.perf_counter()
+    gen = {"HEADLINE": configs.headline, "HARD": configs.hard_headline, "C3": configs.c3}[args.config.upper()]
+
+    def system(n):
+        sysm = gen(n=n)
+        # the kernel matrix is symmetric, so the transposed view of the C-order
+        # result is the column-major A of the reference ABI without a copy
+        A = rbf_matrix(sysm.coords, gamma=sysm.gamma, reg=sysm.reg, kernel=sysm.kernel).T
+        return A, np.asarray(sysm.b, dtype=np.float64)
+
+    def solve(A, b):
+        bn = float(np.linalg.norm(b))
         lu = sla.lu_factor(A, check_finite=False)
         x = sla.lu_solve(lu, b, check_finite=False)
+        rel = float("nan")
         for _ in range(3):
             r = b - A @ x
             rel = float(np.linalg.norm(r)) / bn
             if rel <= args.tol:
                 break
             x = x + sla.lu_solve(lu, r, check_finite=False)
+        return rel
+
+    if args.warmup_n > 0:
+        solve(*system(args.warmup_n))
+    t0 = time.perf_counter()
+    A, b = system(args.n)
+    t_asm = time.perf_counter() - t0
+    times, rel = [], float("nan")
+    for _ in range(args.repeats):
+        t0 = time.perf_counter()
+        rel = solve(A, b)
         times.append(time.perf_counter() - t0)
     print(json.dumps({"seconds": times, "n": args.n, "threads": int(os.environ.get("OPENBLAS_NUM_THREADS", "0")),
-                      "relres": rel, "config": args.config}))
+                      "relres": rel, "config": args.config, "assembly_seconds": t_asm,
+                      "warmup_n": args.warmup_n}))
 
 
 if __name__ == "__main__":

@@ -175,8 +175,13 @@ def test_bounded_wait_reports_timeout_and_device_recovers(native_lib):
         N.debug_set(N.DEBUG_TRSV_FIRST_TICKET, 0)
         N.debug_set(N.DEBUG_WAIT_LIMIT, 0)
     torch.cuda.synchronize()
-    # the context is intact: the same solve now converges
+    # the context is intact: the same solve now converges (from x = 0: the
+    # timed-out solve left NaN in x, which the solver rejects as a start)
     bt = torch.tensor(b, device="cuda")
+    st = lib.mpdok_lu_gmres_ir(_ptr(A64), n, _ptr(_fortran(A, torch.float32)), n, n, _ptr(fac), N.F16, _ptr(bt),
+                               _ptr(x), 1e-12, 10, 30, 1e-6, _ptr(work), work.numel(), ctypes.byref(info), None)
+    assert st == N.ERR_NONFINITE and "initial guess" in N.last_error()
+    x.zero_()
     st = lib.mpdok_lu_gmres_ir(_ptr(A64), n, _ptr(_fortran(A, torch.float32)), n, n, _ptr(fac), N.F16, _ptr(bt),
                                _ptr(x), 1e-12, 10, 30, 1e-6, _ptr(work), work.numel(), ctypes.byref(info), None)
     assert st == 0 and info.converged == 1
