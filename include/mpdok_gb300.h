@@ -224,6 +224,24 @@ MPDOK_API int mpdok_mf_cg_ir(const double* coords, long long n, int dim, int ker
                              int maxiter_outer, double inner_tol, int inner_maxiter, void* work, size_t work_bytes,
                              mpdok_solve_info* info, cudaStream_t stream);
 
+/* CG-IR whose inner CG is preconditioned by an FP64-accurate Cholesky factor:
+ * a batch plan (below) of one system of size n with nrhs equal to this
+ * solve's nrhs, loaded and factored (mpdok_batch_factor).  For SPD systems
+ * too ill-conditioned for any FP32 CG body (kappa * 6e-8 > 1, the C2
+ * family), the preconditioned FP32 CG converges in a few steps and the FP64
+ * refinement reaches the FP64 floor.  mode 0: FP32 copy of A64 in opbuf
+ * (mpdok_cg_ir_operator_size(n, 0)) + native FP64 residual; 1: split A64
+ * (mpdok_cg_ir_operator_size(n, 1)) for the FP32 products and the residual;
+ * 2: matrix-free from coords (dim, kernel, gamma, reg; A64 / opbuf unused).
+ * The reference's cg (dense_krylov.py:119-205) with its FP64 residual check,
+ * made convergent on this family by the preconditioner. */
+MPDOK_API size_t mpdok_chol_cg_ir_workspace_size(long long n, int nrhs, int mode);
+MPDOK_API int mpdok_chol_cg_ir(void* plan, const double* A64, long long lda, const double* coords, int dim,
+                               int kernel, double gamma, double reg, long long n, int mode, void* opbuf, int op_ready,
+                               int nrhs, const double* B, long long ldb, double* X, long long ldx, double tol,
+                               int maxiter_outer, double inner_tol, int inner_maxiter, void* work, size_t work_bytes,
+                               mpdok_solve_info* info, cudaStream_t stream);
+
 /* ----------------------------------------------------------- LU (tensor cores)
  * Blocked right-looking LU with FP32 panels and a trailing update
  * W22 -= L21 U12 whose operands are rounded to the factor type: BF16 / FP16

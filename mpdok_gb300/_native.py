@@ -134,6 +134,10 @@ _SIGS = {
     "mpdok_mf_cg_ir": (c_int, [c_void_p, c_ll, c_int, c_int, c_double, c_double, c_int, c_void_p, c_ll, c_void_p,
                                c_ll, c_double, c_int, c_double, c_int, c_void_p, c_size_t, ctypes.POINTER(SolveInfo),
                                c_void_p]),
+    "mpdok_chol_cg_ir_workspace_size": (c_size_t, [c_ll, c_int, c_int]),
+    "mpdok_chol_cg_ir": (c_int, [c_void_p, c_void_p, c_ll, c_void_p, c_int, c_int, c_double, c_double, c_ll, c_int,
+                                 c_void_p, c_int, c_int, c_void_p, c_ll, c_void_p, c_ll, c_double, c_int, c_double,
+                                 c_int, c_void_p, c_size_t, ctypes.POINTER(SolveInfo), c_void_p]),
     "mpdok_lu_cg_ir_workspace_size": (c_size_t, [c_ll, c_int, c_int]),
     "mpdok_lu_cg_ir": (c_int, [c_void_p, c_ll, c_ll, c_int, c_void_p, c_int, c_void_p, c_int, c_int, c_void_p, c_ll,
                                c_void_p, c_ll, c_double, c_int, c_double, c_int, c_void_p, c_size_t,

@@ -302,6 +302,31 @@ class BatchedRBFSolver:
 
 # ---------------------------------------------------------------------------- autograd
 
+class CholeskyPreconditioner:
+    """FP64-accurate Cholesky factor of one RBF system, for ``cg_ir(..., precond=)``.
+
+    A batch plan of one system (double-float trailing update, FP64 diagonal
+    blocks and solves) factored once; the CG-IR's inner CG applies
+    z = (L L^T)^-1 r to all ``nrhs`` columns at once.  This makes the FP32 CG
+    body converge on systems whose kappa * 6e-8 > 1 (the C2 family), where
+    the unpreconditioned CG of the reference (dense_krylov.py:119-205) stalls.
+    """
+
+    def __init__(self, coords, eps: float, reg: float, nrhs: int = 1, kernel: str = "gaussian",
+                 arith: str = "df32", grid_mult: int = 2):
+        c = coords if isinstance(coords, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(coords))
+        c = c.detach().to(device=require_cuda(), dtype=torch.float64).contiguous()
+        self.n, self.dim = int(c.shape[0]), int(c.shape[1])
+        self.nrhs = int(nrhs)
+        self.solver = BatchedRBFSolver([self.n], dim=self.dim, nrhs=self.nrhs, kernel=kernel, arith=arith,
+                                       grid_mult=grid_mult)
+        self.solver.load(c, float(eps), float(reg)).factor()
+
+    @property
+    def plan(self):
+        return self.solver._plan
+
+
 class _BatchSolveFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, coords, eps, reg, B, solver, refine):

@@ -80,7 +80,7 @@ def headline(n: int = 32768) -> RBFSystem:
     return RBFSystem("HEADLINE", X, "gaussian", 1600.0, 1e-2, b, tol=1e-12, extra={"restart": 30})
 
 
-HARD_EPS = 40.0
+HARD_EPS = 100.0
 
 
 def hard_headline(n: int = 32768, eps: float = HARD_EPS) -> RBFSystem:

@@ -33,7 +33,7 @@
 //    diagonal phi(0) + reg.
 //  * The adjoint contraction recomputes phi and its derivatives from the
 //    coordinates (nothing of size N^2 is stored for the gradient).
-#include "common.cuh"
+#include "krylov.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -800,6 +800,46 @@ static int batch_solve(BatchPlan* p, const double* B, double* X, int refine, cud
     launch(k_badd, dim3(g), 256, 0, s, X, (const double*)p->V, nx);
   }
   MPDOK_LAUNCH_CHECK("batch refine");
+  return MPDOK_OK;
+}
+
+// FP32 columns (leading dimension ld) <-> the plan's FP64 packing (n x K, ld n).
+__global__ void k_cols_f32_to_f64(const float* __restrict__ v, long long ld, double* __restrict__ t, long long n,
+                                  int K) {
+  const long long total = n * K;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x)
+    t[e] = (double)v[(e / n) * ld + e % n];
+}
+__global__ void k_cols_f64_to_f32(const double* __restrict__ t, float* __restrict__ z, long long ld, long long n,
+                                  int K) {
+  const long long total = n * K;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x)
+    z[(e / n) * ld + e % n] = (float)t[e];
+}
+
+static int bpc_apply_cols(void* ctx, const float* v, float* z, int K, long long ld, cudaStream_t s) {
+  BatchPcCtx* c = (BatchPcCtx*)ctx;
+  BatchPlan* p = (BatchPlan*)c->plan;
+  const long long total = c->n * K;
+  const unsigned g = (unsigned)std::max(1LL, std::min<long long>((total + 255) / 256, (long long)num_sms() * 8));
+  launch(k_cols_f32_to_f64, g, 256, 0, s, v, ld, c->tmp, c->n, K);
+  MPDOK_TRY(batch_solve_inplace(p, c->tmp, s));
+  launch(k_cols_f64_to_f32, g, 256, 0, s, (const double*)c->tmp, z, ld, c->n, K);
+  MPDOK_LAUNCH_CHECK("batch preconditioner");
+  return MPDOK_OK;
+}
+
+int batch_precond(void* plan, long long n, int K, double* tmp, BatchPcCtx* ctx, Precond* pc) {
+  MPDOK_ARG_CHECK(plan && tmp && ctx && pc, "null pointer");
+  BatchPlan* p = (BatchPlan*)plan;
+  MPDOK_ARG_CHECK(p->nsys == 1 && p->sys[0].n == n, "the preconditioner plan must hold one system of size n");
+  MPDOK_ARG_CHECK(p->nrhs == K, "the preconditioner plan's nrhs must equal the solve's nrhs");
+  ctx->plan = plan;
+  ctx->tmp = tmp;
+  ctx->n = n;
+  pc->apply = nullptr;
+  pc->apply_cols = bpc_apply_cols;
+  pc->ctx = ctx;
   return MPDOK_OK;
 }
 

@@ -1076,7 +1076,12 @@ int cg_ir_core(const CgIrWs& w, const Operator32& A, const Residual64& R, const 
     launch(k_mcg_init, grid, KT, 0, s, (const double*)w.R64, ld, n, w.E, w.r, w.p, w.parts, w.ticket, cols, g);
     if (pc) {
       // z = M^-1 r, p = z, rz = r . z
-      for (int c = 0; c < K; ++c) MPDOK_TRY(pc->apply(pc->ctx, w.r + (long long)c * ld, w.z + (long long)c * ld, s, nullptr));
+      if (pc->apply_cols) {
+        MPDOK_TRY(pc->apply_cols(pc->ctx, w.r, w.z, K, ld, s));
+      } else {
+        for (int c = 0; c < K; ++c)
+          MPDOK_TRY(pc->apply(pc->ctx, w.r + (long long)c * ld, w.z + (long long)c * ld, s, nullptr));
+      }
       launch(k_mcg_rz, grid, KT, 0, s, (const float*)w.r, (const float*)w.z, ld, n, w.parts, w.ticket + 3, cols,
              (const MCGGlobal*)g, 1);
       MPDOK_CUDA_TRY(cudaMemcpyAsync(w.p, w.z, sizeof(float) * ld * K, cudaMemcpyDeviceToDevice, s));
@@ -1092,8 +1097,12 @@ int cg_ir_core(const CgIrWs& w, const Operator32& A, const Residual64& R, const 
         launch(k_mcg_xr, grid, KT, 0, s, w.E, w.r, (const float*)w.p, (const float*)w.q, ld, n, w.parts,
                w.ticket + 2, cols, g, inner_tol, pc ? 1 : 0);
         if (pc) {
-          for (int c = 0; c < K; ++c)
-            MPDOK_TRY(pc->apply(pc->ctx, w.r + (long long)c * ld, w.z + (long long)c * ld, s, &g->done));
+          if (pc->apply_cols) {
+            MPDOK_TRY(pc->apply_cols(pc->ctx, w.r, w.z, K, ld, s));
+          } else {
+            for (int c = 0; c < K; ++c)
+              MPDOK_TRY(pc->apply(pc->ctx, w.r + (long long)c * ld, w.z + (long long)c * ld, s, &g->done));
+          }
           launch(k_mcg_rz, grid, KT, 0, s, (const float*)w.r, (const float*)w.z, ld, n, w.parts, w.ticket + 3, cols,
                  (const MCGGlobal*)g, 0);
         }

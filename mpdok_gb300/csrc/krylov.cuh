@@ -85,7 +85,20 @@ struct Precond {
   int (*apply)(void* ctx, const float* v, float* z, cudaStream_t s, const int* skip) = nullptr;
   void* ctx = nullptr;
   float* z = nullptr;  // n floats of scratch for M^{-1} v
+  // optional: all K columns (leading dimension ld) in one call; CG-IR uses it
+  // when set (a factorization applied to K right-hand sides at once)
+  int (*apply_cols)(void* ctx, const float* v, float* z, int K, long long ld, cudaStream_t s) = nullptr;
 };
+
+// Preconditioner z = A^-1 v from the Cholesky factor held in a batch plan of
+// one system of size n with nrhs == K (double-float trailing update, FP64
+// diagonal blocks and solves); tmp holds n * K doubles.  Defined in batch.cu.
+struct BatchPcCtx {
+  void* plan = nullptr;
+  double* tmp = nullptr;
+  long long n = 0;
+};
+int batch_precond(void* plan, long long n, int K, double* tmp, BatchPcCtx* ctx, Precond* pc);
 
 // One Arnoldi cycle (up to m steps) on the FP32 operator A32 with the
 // unnormalised start vector already in V[:,0] and ws.sc->nrm2 = ||V[:,0]||^2

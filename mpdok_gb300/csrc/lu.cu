@@ -265,24 +265,39 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
   for (int idx = tid; idx < LNB * DP; idx += blockDim.x) { XL[idx] = 0.f; XU[idx] = 0.f; }
   __syncthreads();
   {
+    // Each 32 x 32 diagonal block is inverted by one warp with its column j in
+    // lane j's registers (fully unrolled substitution; the block's rows are
+    // shared-memory broadcasts).  The terms outside a column's triangle are
+    // exact zeros, so every entry gets the same operations in the same order
+    // as a column-by-column substitution.
     const int b = warp & 3;
-    const int col = b * 32 + lane;
+    const int o = b * 32;
+    const float* Tb = T + o * DP + o;
     if (warp >= 8) {
       // idle during the 32 x 32 substitutions
     } else if (warp < 4) {
-      XL[col * DP + col] = 1.f;
-      for (int i = col + 1; i < b * 32 + 32; ++i) {
-        float sacc = 0.f;
-        for (int k = col; k < i; ++k) sacc = fmaf(T[i * DP + k], XL[k * DP + col], sacc);
-        XL[i * DP + col] = -sacc;
+      float x[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        float acc = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+        for (int k = 0; k < i; ++k) acc = fmaf(-Tb[i * DP + k], x[k], acc);
+        x[i] = (i < lane) ? 0.f : acc;
       }
+#pragma unroll
+      for (int i = 0; i < 32; ++i) XL[(o + i) * DP + o + lane] = x[i];
     } else {
-      XU[col * DP + col] = 1.f / T[col * DP + col];
-      for (int i = col - 1; i >= b * 32; --i) {
-        float sacc = 0.f;
-        for (int k = i + 1; k <= col; ++k) sacc = fmaf(T[i * DP + k], XU[k * DP + col], sacc);
-        XU[i * DP + col] = -sacc / T[i * DP + i];
+      float x[32];
+#pragma unroll
+      for (int i = 31; i >= 0; --i) {
+        float acc = 0.f;
+#pragma unroll
+        for (int k = i + 1; k < 32; ++k) acc = fmaf(Tb[i * DP + k], x[k], acc);
+        const float d = Tb[i * DP + i];
+        x[i] = (i > lane) ? 0.f : (i == lane ? 1.f / d : -acc / d);
       }
+#pragma unroll
+      for (int i = 0; i < 32; ++i) XU[(o + i) * DP + o + lane] = x[i];
     }
   }
   __syncthreads();

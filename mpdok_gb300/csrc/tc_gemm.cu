@@ -129,6 +129,19 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 // Shared memory: STAGES x ([A 128x64][B 256x64]) ring, then barriers and the
 // tensor-memory address slot.
 template <int STAGES>
@@ -277,6 +290,254 @@ tc_gemm_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   }
 }
 
+// ------------------------------------------------------------------------
+// Warp-specialised form for deep updates (K >= 256): one CTA per SM walks a
+// strip of T tiles (128 x 256) that share their A rows, with
+//   * a 4-stage TMA ring (48 KB per stage: the A and B blocks of one 64-deep
+//     K step), so four loads are in flight while the tensor cores work;
+//   * two TMEM accumulators (2 x 256 columns, all 512), so the MMAs of tile
+//     t + 1 run while the epilogue drains tile t;
+//   * warp 0 the TMA producer, warp 1 the MMA issuer, warps 2..9 the epilogue
+//     (warp w reads TMEM lane quarter w % 4, column half (w - 2) / 4, and
+//     applies C -= acc as coalesced column-major read-modify-writes with two
+//     32-column chunks of C in flight).
+// Barriers: full[s] / empty[s] for the ring, acc_full[a] (MMA -> epilogue,
+// one commit) and acc_empty[a] (epilogue -> MMA, 8 warp arrivals).  Every
+// wait is bounded and also gives up as soon as another role has failed; a
+// failed CTA waits (bounded) for its own loads in flight before it releases
+// its tensor memory and returns.
+namespace ws {
+
+constexpr int STAGES = 4;
+constexpr int EPI_WARPS = 8;
+constexpr int THREADS = 32 * (2 + EPI_WARPS);
+constexpr int TMEM_COLS = 512;
+constexpr int A_SUB = BM * BK * 2;   // 16 KB
+constexpr int B_SUB = BN * BK * 2;   // 32 KB
+constexpr int STAGE = A_SUB + B_SUB;
+// epilogue staging: per epilogue warp two 16-column x 32-row FP32 buffers
+// ([column][row], 2 KB each), drained into C by TMA reduce-add
+constexpr int EPI_COLS = 16;
+constexpr int EPI_BUF = 32 * EPI_COLS * 4;
+constexpr int STAGING_OFF = STAGES * STAGE;
+constexpr int BAR_OFF = STAGING_OFF + EPI_WARPS * 2 * EPI_BUF;
+constexpr int NBAR = 2 * STAGES + 5;
+constexpr int TOTAL = BAR_OFF + 8 * NBAR + 16;
+constexpr int ALLOC = TOTAL + 1024;
+static_assert(ALLOC <= 232448, "shared memory of one CTA");
+
+__device__ __forceinline__ bool wait_or_fail(uint32_t bar, uint32_t parity, volatile int* fail) {
+  for (long long i = 0; i < WAIT_LIMIT; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63) == 63) {
+      if (*fail) return false;
+      __nanosleep(32);
+    }
+  }
+  return false;
+}
+
+// C += (staged tile) by TMA: the L2 performs the read-modify-write, so the
+// epilogue holds no C values and issues no C loads.  Coordinates: x = row
+// (a multiple of 32 FP32 elements, 128 bytes), y = column.
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, uint32_t src, int x, int y) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%2, %3}], [%1];"
+      ::"l"(reinterpret_cast<uint64_t>(map)), "r"(src), "r"(x), "r"(y)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// at most N bulk groups of this thread still reading shared memory
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory"); }
+template <int N>
+__device__ __forceinline__ void bulk_wait() { asm volatile("cp.async.bulk.wait_group %0;" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+tc_gemm_update_ws(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  const __grid_constant__ CUtensorMap tmC, int M, int N, int K, int T, int bf16, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t* gbase = smem_raw + (base - raw);
+  const uint32_t bar_full = base + BAR_OFF;
+  const uint32_t bar_empty = bar_full + 8 * STAGES;
+  const uint32_t bar_accf = bar_empty + 8 * STAGES;
+  const uint32_t bar_acce = bar_accf + 16;
+  const uint32_t bar_drain = bar_acce + 16;  // the MMA issuer's last commit: all its MMAs are done
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + BAR_OFF + 8 * NBAR);
+  __shared__ int s_fail;
+  volatile int* fail = &s_fail;
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM;
+  const int tile0 = blockIdx.y * T;
+  const int ntiles_n = (N + BN - 1) / BN;
+  const int nt = max(0, min(T, ntiles_n - tile0));
+  const int KB = K / BK;
+
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    for (int st = 0; st < STAGES; ++st) {
+      mbar_init(bar_full + 8 * st, 1);
+      mbar_init(bar_empty + 8 * st, 1);
+    }
+    mbar_init(bar_accf, 1);
+    mbar_init(bar_accf + 8, 1);
+    mbar_init(bar_acce, EPI_WARPS);
+    mbar_init(bar_acce + 8, EPI_WARPS);
+    mbar_init(bar_drain, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // TMA producer over every (tile, K block) of the strip
+      int g = 0;
+      bool ok = true;
+      for (int t = 0; t < nt && ok; ++t) {
+        const int n0 = (tile0 + t) * BN;
+        for (int kb = 0; kb < KB; ++kb, ++g) {
+          const int st = g % STAGES, round = g / STAGES;
+          if (round > 0 && !wait_or_fail(bar_empty + 8 * st, (round - 1) & 1, fail)) {
+            atomicExch(&s_fail, 1);
+            ok = false;
+            break;
+          }
+          const uint32_t sa = base + st * STAGE;
+          mbar_expect_tx(bar_full + 8 * st, (uint32_t)STAGE);
+          tma_load_2d(sa, &tmA, bar_full + 8 * st, kb * BK, m0);
+          tma_load_2d(sa + A_SUB, &tmB, bar_full + 8 * st, kb * BK, n0);
+        }
+      }
+      if (!ok || *fail) {
+        // loads still in flight land in this CTA's shared memory: wait for
+        // each stage's last issued load (bounded) before the CTA may exit
+        for (int st = 0; st < STAGES && st < g; ++st) {
+          const int last = g - 1 - ((g - 1 - st) % STAGES);
+          const int round = last / STAGES;
+          for (long long i = 0; i < WAIT_LIMIT && !mbar_try_wait(bar_full + 8 * st, round & 1); ++i) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_f16(bf16 != 0, BM, BN);
+      int g = 0;
+      bool ok = true;
+      for (int t = 0; t < nt && ok; ++t) {
+        const int a = t & 1, use = t >> 1;
+        if (use > 0 && !wait_or_fail(bar_acce + 8 * a, (use - 1) & 1, fail)) {
+          atomicExch(&s_fail, 2);
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t dacc = tmem + (uint32_t)(a * BN);
+        for (int kb = 0; kb < KB; ++kb, ++g) {
+          const int st = g % STAGES, round = g / STAGES;
+          if (!wait_or_fail(bar_full + 8 * st, round & 1, fail)) {
+            atomicExch(&s_fail, 3);
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sa = base + st * STAGE;
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k) {
+            const uint64_t ad = smem_desc_sw128(sa + k * 32);
+            const uint64_t bd = smem_desc_sw128(sa + A_SUB + k * 32);
+            mma_f16(dacc, ad, bd, idesc, (kb | k) ? 1u : 0u);
+          }
+          mma_commit(bar_empty + 8 * st);
+        }
+        if (ok) mma_commit(bar_accf + 8 * a);
+      }
+      // before the tensor memory may be released, every MMA issued here must
+      // have completed (also after a failure, when no epilogue waited for them)
+      mma_commit(bar_drain);
+      for (long long i = 0; i < WAIT_LIMIT && !mbar_try_wait(bar_drain, 0); ++i) {
+        if (i > 64) __nanosleep(32);
+      }
+    }
+  } else {
+    // epilogue: TMEM lane quarter q = warp % 4 (rows m0 + 32 q + lane), column
+    // half h.  Per 16-column chunk: tcgen05.ld, -acc into a staging buffer
+    // ([column][row], conflict-free), then lane 0 adds it into C with one TMA
+    // reduce; two buffers per warp alternate, so the next chunk is staged
+    // while the last one drains.
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    const int ew = warp - 2;
+    float* stg = reinterpret_cast<float*>(gbase + STAGING_OFF + ew * 2 * EPI_BUF);
+    const uint32_t stg_s = base + STAGING_OFF + ew * 2 * EPI_BUF;
+    constexpr int HALF = BN / 2;
+    constexpr int NCH = HALF / EPI_COLS;
+    int nbuf = 0;
+    for (int t = 0; t < nt; ++t) {
+      const int a = t & 1, use = t >> 1;
+      const int nbase = (tile0 + t) * BN + h * HALF;
+      if (!wait_or_fail(bar_accf + 8 * a, use & 1, fail)) {
+        atomicExch(&s_fail, 4);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t tacc = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BN + h * HALF);
+#pragma unroll 1
+      for (int i = 0; i < NCH; ++i) {
+        // chunks past N hold nothing to add; skipping them keeps the two
+        // staging buffers strictly alternating between issued reduces (a
+        // skipped chunk must not overwrite a buffer whose reduce is pending)
+        if (nbase + i * EPI_COLS >= N || m0 + q * 32 >= M) break;
+        float v[EPI_COLS];
+        tmem_ld16(tacc + (uint32_t)(i * EPI_COLS), v);
+        const int b = nbuf & 1;
+        ++nbuf;
+        if (lane == 0) bulk_wait_read<1>();  // the buffer's previous reduce has read it
+        __syncwarp();
+        float* buf = stg + b * (EPI_BUF / 4);
+#pragma unroll
+        for (int c = 0; c < EPI_COLS; ++c) buf[c * 32 + lane] = -v[c];
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) {
+          tma_reduce_add_2d(&tmC, stg_s + b * EPI_BUF, m0 + q * 32, nbase + i * EPI_COLS);
+          bulk_commit();
+        }
+      }
+      // this warp has read its part of accumulator a: hand it back to the MMA
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bar_acce + 8 * a);
+    }
+    if (lane == 0) bulk_wait<0>();  // every reduce of this warp has completed
+    __syncwarp();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (threadIdx.x == 0 && s_fail != 0 && err) atomicExch(err, 1);
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+}  // namespace ws
+
 // CUDA-core comparator with the same operand rounding (test use).
 __global__ void simt_gemm_update(const void* A, const void* B, long long ldk, int bf16, float* C, long long ldc,
                                  int M, int N, int K) {
@@ -336,10 +597,48 @@ static int make_map(CUtensorMap* map, const void* ptr, int rows, int K, long lon
   return MPDOK_OK;
 }
 
+// 2-D tensor map over the FP32 C (rows x columns, column-major, ldc), box 32
+// rows x 16 columns: the target of the epilogue's TMA reduce-adds.
+static int make_map_c(CUtensorMap* map, float* C, int M, int N, long long ldc) {
+  auto enc = get_encode();
+  if (!enc) {
+    set_error("cuTensorMapEncodeTiled unavailable from the driver");
+    return MPDOK_ERR_UNSUPPORTED;
+  }
+  cuuint64_t gdim[2] = {(cuuint64_t)M, (cuuint64_t)N};
+  cuuint64_t gstride[1] = {(cuuint64_t)ldc * 4};
+  cuuint32_t box[2] = {32, (cuuint32_t)tc::ws::EPI_COLS};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, gdim, gstride, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled (C) failed (%d)", (int)r);
+    return MPDOK_ERR_CUDA;
+  }
+  return MPDOK_OK;
+}
+
 constexpr int TC_STAGES = 2;
+
+// Tiles per CTA of the warp-specialised kernel along N (the strip shares A).
+constexpr int WS_TILES = 4;
+// K from which the warp-specialised kernel is used; shallower updates keep the
+// two-CTA-per-SM kernel, whose set-up is cheaper for two or three K blocks.
+constexpr int WS_MIN_K = 256;
 
 static int launch_tc(const CUtensorMap& ma, const CUtensorMap& mb, float* C, long long ldc, int M, int N, int K,
                      int bf16, int* err, cudaStream_t s) {
+  if (K >= WS_MIN_K && aligned16(C) && ldc % 4 == 0) {
+    CUtensorMap mc;
+    MPDOK_TRY(make_map_c(&mc, C, M, N, ldc));
+    MPDOK_TRY(set_smem(tc::ws::tc_gemm_update_ws, tc::ws::ALLOC));
+    const int ntn = (N + tc::BN - 1) / tc::BN;
+    dim3 grid((M + tc::BM - 1) / tc::BM, (ntn + WS_TILES - 1) / WS_TILES);
+    tc::ws::tc_gemm_update_ws<<<grid, tc::ws::THREADS, tc::ws::ALLOC, s>>>(ma, mb, mc, M, N, K, WS_TILES, bf16, err);
+    count_launch();
+    MPDOK_LAUNCH_CHECK("tc_gemm_update_ws");
+    return MPDOK_OK;
+  }
   using S = tc::Smem<TC_STAGES>;
   MPDOK_TRY(set_smem(tc::tc_gemm_update<TC_STAGES>, S::ALLOC));
   dim3 grid((M + tc::BM - 1) / tc::BM, (N + tc::BN - 1) / tc::BN);

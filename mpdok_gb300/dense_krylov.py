@@ -192,9 +192,12 @@ def cg_ir(op, B, tol: float = 1e-12, maxiter_outer: int = 10, inner_tol: float =
 
     B: (N,) or (N, k<=8).  ``split=True`` stores A as two FP32 slices and forms
     every product with error-free FP32 arithmetic (FP64-level accuracy on the
-    FP32 pipe) for both the inner operator and the residual.  ``precond`` (an
-    ``mpdok_gb300.lu.LUFactorization``) preconditions the inner CG, which an
-    FP32 CG body needs once kappa(A) * 6e-8 >= 1.
+    FP32 pipe) for both the inner operator and the residual.  ``precond``
+    preconditions the inner CG, which an FP32 CG body needs once
+    kappa(A) * 6e-8 >= 1: an ``mpdok_gb300.lu.LUFactorization`` (16/32-bit
+    factors, for kappa up to about 1e7) or an
+    ``mpdok_gb300.batch.CholeskyPreconditioner`` (FP64-accurate Cholesky, for
+    the C2 family at kappa ~ 1e8).
     Returns ``(X_fp64, history, converged)``; history holds the worst column.
     """
     if getattr(op, "_matrix_free", False):
@@ -223,7 +226,17 @@ def cg_ir(op, B, tol: float = 1e-12, maxiter_outer: int = 10, inner_tol: float =
             buf, ready = cache[1], 1
         opbuf = buf
     info = N.SolveInfo()
-    if precond is None:
+    if precond is not None and hasattr(precond, "plan"):
+        # FP64-accurate Cholesky (batch plan of one system) as the inner PCG's preconditioner
+        if precond.n != n or precond.nrhs != k:
+            raise ValueError(f"the Cholesky preconditioner holds n={precond.n}, nrhs={precond.nrhs}; "
+                             f"this solve has n={n}, nrhs={k}")
+        w = op._ws.get(lib.mpdok_chol_cg_ir_workspace_size(n, k, mode))
+        N.check(lib.mpdok_chol_cg_ir(precond.plan, ptr(op.A_fp64), n, None, 0, 0, 0.0, 0.0, n, mode, ptr(opbuf), ready,
+                                     k, ptr(Bc), n, ptr(X), n, float(tol), int(maxiter_outer), float(inner_tol),
+                                     int(inner_maxiter), ptr(w), w.numel(), ctypes.byref(info), stream_handle()),
+                "chol_cg_ir")
+    elif precond is None:
         w = op._ws.get(lib.mpdok_cg_ir_workspace_size(n, k, mode))
         N.check(lib.mpdok_cg_ir(ptr(op.A_fp64), n, n, mode, ptr(opbuf), ready, k, ptr(Bc), n, ptr(X), n,
                                 float(tol), int(maxiter_outer), float(inner_tol), int(inner_maxiter), ptr(w),

@@ -102,7 +102,8 @@ class MatrixFreeOperator:
         return x, info.history_list(), bool(info.converged)
 
     def cg_ir(self, B, tol=1e-12, maxiter_outer=10, inner_tol=1e-6, inner_maxiter=500, precond=None):
-        """Multi-RHS CG-IR on the matrix-free operator (optionally LU-preconditioned)."""
+        """Multi-RHS CG-IR on the matrix-free operator, optionally preconditioned by LU
+        factors or by a ``CholeskyPreconditioner`` (see ``dense_krylov.cg_ir``)."""
         Bc = as_columns(B, torch.float64)
         k = Bc.shape[1]
         if k > 8:
@@ -110,7 +111,16 @@ class MatrixFreeOperator:
         X = fortran_empty(self.N, k, torch.float64)
         lib = N.load()
         info = N.SolveInfo()
-        if precond is None:
+        if precond is not None and hasattr(precond, "plan"):
+            if precond.n != self.N or precond.nrhs != k:
+                raise ValueError(f"the Cholesky preconditioner holds n={precond.n}, nrhs={precond.nrhs}; "
+                                 f"this solve has n={self.N}, nrhs={k}")
+            w = self._ws.get(lib.mpdok_chol_cg_ir_workspace_size(self.N, k, 2))
+            N.check(lib.mpdok_chol_cg_ir(precond.plan, None, 0, ptr(self.coords), self.dim, self.kcode, self.gamma,
+                                         self.reg, self.N, 2, None, 0, k, ptr(Bc), self.N, ptr(X), self.N,
+                                         float(tol), int(maxiter_outer), float(inner_tol), int(inner_maxiter),
+                                         ptr(w), w.numel(), ctypes.byref(info), stream_handle()), "mf_chol_cg_ir")
+        elif precond is None:
             w = self._ws.get(lib.mpdok_mf_cg_ir_workspace_size(self.N, k))
             N.check(lib.mpdok_mf_cg_ir(ptr(self.coords), self.N, self.dim, self.kcode, self.gamma, self.reg, k,
                                        ptr(Bc), self.N, ptr(X), self.N, float(tol), int(maxiter_outer),

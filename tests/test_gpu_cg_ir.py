@@ -111,3 +111,33 @@ def test_cg_ir_c2_family_reports_infeasibility():
     assert not conv
     assert len(hist) == 4 and hist[0] == (0, pytest.approx(1.0))
     assert np.all(np.isfinite(Xs.cpu().numpy()))
+
+
+@pytest.mark.parametrize("variant", ["stored", "split", "matfree"])
+def test_c2_family_through_cholesky_preconditioned_cg_ir(variant):
+    """C2's family (3-D Gaussian eps=5, nugget 1e-6, 4 RHS; kappa ~ 1e8 at this
+    N): every FP32 CG body stalls here (kappa * 6e-8 > 1).  With the inner CG
+    preconditioned by the FP64-accurate Cholesky factor, CG-IR reaches the
+    FP64 LU oracle's own floor on every column (relres <= 10x the oracle's)."""
+    from mpdok_gb300.batch import CholeskyPreconditioner
+    from mpdok_gb300.dense_krylov import DenseLinearOperator, cg_ir
+    from mpdok_gb300.matfree import MatrixFreeOperator
+    n = 5000
+    X, A, B = _spd(n, 25.0, 1e-6, seed=1)
+    pc = CholeskyPreconditioner(X, eps=5.0, reg=1e-6, nrhs=4)
+    if variant == "matfree":
+        op = MatrixFreeOperator(X, gamma=25.0, reg=1e-6)
+        Xs, hist, conv = op.cg_ir(B, tol=1e-12, maxiter_outer=8, inner_tol=1e-6, inner_maxiter=6, precond=pc)
+    else:
+        op = DenseLinearOperator(A, verbose=False)
+        Xs, hist, conv = cg_ir(op, B, tol=1e-12, maxiter_outer=8, inner_tol=1e-6, inner_maxiter=6,
+                               split=(variant == "split"), precond=pc)
+    Xs = Xs.cpu().numpy()
+    for j in range(B.shape[1]):
+        x_lu = O.fp64_solve(A, B[:, j])
+        floor = O.relres(A, x_lu, B[:, j])
+        rel = O.relres(A, Xs[:, j], B[:, j])
+        assert rel <= max(1e-12, 10 * floor), (variant, j, rel, floor, hist)
+        assert np.linalg.norm(Xs[:, j] - x_lu) / np.linalg.norm(x_lu) < 1e3 * max(floor, 1e-13) * 1e4
+    # a handful of preconditioned steps per refinement, not hundreds
+    assert hist[-1][0] <= 8

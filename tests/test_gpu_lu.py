@@ -12,7 +12,10 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("dt", [torch.bfloat16, torch.float16])
 @pytest.mark.parametrize("M,Nn,K", [(128, 256, 128), (300, 520, 128), (1000, 777, 64), (257, 1029, 256),
-                                    (129, 100, 192)])
+                                    (129, 100, 192),
+                                    # K >= 256 with ldc % 4 == 0: the warp-specialised kernel (strips of
+                                    # four tiles, two TMEM accumulators, TMA reduce-add epilogue)
+                                    (1000, 777, 256), (512, 1100, 512), (4096, 4100, 1024), (132, 2048, 320)])
 def test_tensor_core_update_matches_cuda_cores(dt, M, Nn, K):
     from mpdok_gb300.lu import gemm_update
     g = torch.Generator(device="cuda").manual_seed(M + Nn + K)
