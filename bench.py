@@ -242,18 +242,30 @@ def bench_batch(args, emit: bool = True) -> dict:
     torch.cuda.synchronize()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
+    from mpdok_gb300 import _native as NV
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()
+    l0 = NV.launch_count()
     e0.record()
     for _ in range(args.steps):
         grads = step()
     e1.record()
     torch.cuda.synchronize()
+    launches = NV.launch_count() - l0
     barrier()
     ck = clocks.stop()
+    if solver.schedule == "dag":
+        solver.dag_status()
     per = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, device="cuda")
-    # factor alone, for the roofline of the trailing update
+    # the graph step alone (assembly + factor + solve + 2 refinements), and the
+    # level-scheduled factor alone for the roofline of the trailing update
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record()
+    solver.run_graph()
+    g1.record()
+    torch.cuda.synchronize()
+    t_graph = g0.elapsed_time(g1) / 1e3
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record()
     solver.factor()
@@ -312,18 +324,18 @@ def bench_batch(args, emit: bool = True) -> dict:
                                "2-D uniform centres, eps~U(2,8), nugget 1e-8, 8 RHS; step = graph(factor + solve + "
                                "2 FP64 IR) + adjoint (solve + contraction)",
                    "l2": "inputs larger than L2 (A: %.1f GB FP64)" % (sum(n * n for n in sizes) * 8 / 1e9),
-                   "grid_mult": solver.grid_mult, "autotune": tune,
+                   "schedule": solver.config, "autotune": tune, "graph_nodes": solver.graph_nodes,
                    "parallelism": f"{world} rank(s), systems sharded by N^3 (LPT), imbalance "
                                   f"{shard_imbalance([q.n for q in all_systems], parts):.3f}"},
         "relres_max": float(relres.max()), "relres_median": float(np.median(relres)),
-        "factor_seconds": t_factor,
+        "factor_seconds": t_factor, "graph_step_seconds": t_graph,
         "roofline": {"bound": "fp32 pipe (double-float trailing update)", "achieved": ach,
                      "peak": df_peak, "unit": "TFLOP/s (FP64-equivalent)", "frac": ach / df_peak, "traffic": None,
                      "kernel": "batched Cholesky factor (k_bsyrk dominant)",
                      "peak_source": f"nominal FP32 FMA rate {fp32_peak:.1f} TFLOP/s / {DF_FMA_OPS} instructions "
                                     "per double-float multiply-add"},
         "fp64_gpu_baseline": base, "cpu_baseline": cpu,
-        "e2e": None, "gpu_launches": solver.graph_nodes * args.steps, "clocks": ck,
+        "e2e": None, "gpu_launches": launches, "clocks": ck,
         "gradient_norms": {"coords": float(grads[0].norm()), "eps": float(grads[1].norm()),
                            "reg": float(grads[2].norm())},
     }
@@ -982,7 +994,7 @@ def main():
         A_host = torch.empty_strided((n, n), (1, n), dtype=torch.float64, pin_memory=True)
         A_host.copy_(A.cpu())
         b_host = torch.from_numpy(np.asarray(sysm.b)).pin_memory()
-        times = []
+        times, parts = [], []
         for i in range(max(1, min(args.steps, 3)) + 1):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -991,6 +1003,7 @@ def main():
             torch.cuda.synchronize()
             if i > 0:
                 times.append(time.perf_counter() - t0)
+                parts.append(dict(solver.last_timing))
         # the upload alone (A straight into its device buffer with the FP32
         # copy made per block), against a plain pinned 1 GiB host -> device copy
         from mpdok_gb300._device import fortran_empty, upload_fortran
@@ -1016,6 +1029,7 @@ def main():
         del hb, db, A_host
         e2e = {"value": sum(times) / len(times), "unit": UNIT, "h2d_bytes_per_step": 8 * n * n + 8 * n,
                "d2h_bytes_per_step": 8 * n, "api": "mpdok_gb300.solvers.MixedSolver.solve(host A, host b)",
+               "breakdown_ms": parts[-1] if parts else None,
                "upload_seconds": up_s, "upload_GBs": 8.0 * n * n / up_s / 1e9, "pinned_h2d_GBs": link,
                "upload_frac_of_pinned_copy": 8.0 * n * n / up_s / 1e9 / link}
 

@@ -386,6 +386,18 @@ MPDOK_API int mpdok_batch_relres(void* plan, const double* B, const double* X, d
  * coords, grad_eps and grad_reg (nsys, device).  phi recomputed in FP64. */
 MPDOK_API int mpdok_batch_adjoint(void* plan, const double* X, const double* Lam, double* grad_coords,
                                   double* grad_eps, double* grad_reg, cudaStream_t stream);
+/* The gradient contraction of ONE system (the in-core solvers' adjoint):
+ * with A = phi_eps(||c_i - c_j||) + reg I (gamma = eps^2), X the solution and
+ * Lam = A^-1 dL/dX (n x nrhs column-major, ld n, nrhs <= 8):
+ *   grad_coords (n x dim row-major) = dL/dc,  *grad_eps = dL/deps,
+ *   *grad_reg = dL/dreg  (= -sum Lam .* X),
+ * phi and its derivatives recomputed in FP64 from the coordinates (dA is
+ * never stored).  Workspace: mpdok_rbf_adjoint_workspace_size(n) bytes.
+ * Synchronises the stream. */
+MPDOK_API size_t mpdok_rbf_adjoint_workspace_size(long long n);
+MPDOK_API int mpdok_rbf_adjoint(const double* coords, long long n, int dim, int kernel, double eps, int nrhs,
+                                const double* X, const double* Lam, double* grad_coords, double* grad_eps,
+                                double* grad_reg, void* work, size_t work_bytes, cudaStream_t stream);
 /* Pivots perturbed by the last factorization (synchronises the stream). */
 MPDOK_API int mpdok_batch_perturbed(void* plan, cudaStream_t stream);
 /* Capture factor + solve (+ refine) on fixed B / X into one CUDA graph, then
@@ -393,6 +405,20 @@ MPDOK_API int mpdok_batch_perturbed(void* plan, cudaStream_t stream);
 MPDOK_API int mpdok_batch_graph_build(void* plan, const double* B, double* X, int refine);
 MPDOK_API int mpdok_batch_graph_launch(void* plan, cudaStream_t stream);
 MPDOK_API long long mpdok_batch_graph_nodes(void* plan);
+/* Schedule of mpdok_batch_step and of the captured graph.  0: level
+ * synchronous, three launches per 64-column block level (diagonal factor,
+ * panel solve, trailing update over every active system) plus the level
+ * scheduled solves.  1: the whole step as ONE persistent launch of
+ * ctas_per_sm (1..3) CTAs per SM that take tile tasks (assembly, Cholesky,
+ * solve, FP64 refinement) from a queue in a topological order and start each
+ * one as soon as its inputs are final; results are bit-identical to 0. */
+MPDOK_API int mpdok_batch_schedule(void* plan, int schedule, int ctas_per_sm);
+/* One step on B / X: assembly + factor + solve + `refine` refinement steps
+ * under the plan's schedule (no host synchronisation). */
+MPDOK_API int mpdok_batch_step(void* plan, const double* B, double* X, int refine, cudaStream_t stream);
+/* MPDOK_ERR_TIMEOUT when a task of the last task-graph step gave up waiting
+ * on its inputs (synchronises the stream), else 0. */
+MPDOK_API int mpdok_batch_dag_status(void* plan, cudaStream_t stream);
 
 /* --------------------------------------------------------- instrumentation
  * mpdok_launch_count: kernels launched by this library since load.

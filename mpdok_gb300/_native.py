@@ -175,6 +175,12 @@ _SIGS = {
     "mpdok_batch_graph_build": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
     "mpdok_batch_graph_launch": (c_int, [c_void_p, c_void_p]),
     "mpdok_batch_graph_nodes": (c_ll, [c_void_p]),
+    "mpdok_batch_schedule": (c_int, [c_void_p, c_int, c_int]),
+    "mpdok_rbf_adjoint_workspace_size": (c_size_t, [c_ll]),
+    "mpdok_rbf_adjoint": (c_int, [c_void_p, c_ll, c_int, c_int, c_double, c_int, c_void_p, c_void_p, c_void_p,
+                                  c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "mpdok_batch_step": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "mpdok_batch_dag_status": (c_int, [c_void_p, c_void_p]),
     "mpdok_launch_count": (c_ll, []),
     "mpdok_profile_enable": (c_int, [c_int]),
     "mpdok_profile_query": (c_int, [c_int, ctypes.POINTER(c_double), ctypes.POINTER(c_ll), ctypes.POINTER(c_double)]),

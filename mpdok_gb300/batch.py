@@ -1,13 +1,18 @@
 """Batched RBF solves with gradients: many systems of uneven N, several RHS each.
 
 ``BatchedRBFSolver(sizes, dim, nrhs)`` owns one plan of ``libmpdok_gb300``:
-FP64 storage for every A_s = phi(eps_s ||c_i - c_j||) + reg_s I, a level-
-scheduled batched Cholesky (systems sorted by N, one launch per block level
-over every active system, a persistent trailing-update grid over the
-(system, tile) task list), FP64 triangular solves and FP64 refinement.  The
-factor + solve sequence can be captured into one CUDA graph and replayed with
-a single launch.  The grid size of the trailing update is chosen by
-``autotune`` (timed on the real batch, cached as JSON per device and batch).
+FP64 storage for every A_s = phi(eps_s ||c_i - c_j||) + reg_s I, a batched
+Cholesky on 64 x 64 tiles (double-float trailing update), FP64 triangular
+solves and FP64 refinement.  Two schedules run the same tile arithmetic:
+``levels`` (three launches per block level over every active system, a
+persistent trailing-update grid over the level's (system, tile) tasks, then
+level-scheduled solves) and ``dag`` (the whole step, assembly to the last
+refinement, as ONE persistent launch whose CTAs take tile tasks from a queue
+in topological order and start each one when its inputs are final).  The
+step is captured into a CUDA graph and replayed with a single launch.
+``autotune`` times the schedules and their grid sizes on the real batch and
+caches the choice as JSON per device and batch (the tile is 64: two 64 x 65
+double-float tiles fill 66.5 KB of shared memory, three CTAs per SM).
 
 ``rbf_batch_solve(coords, eps, reg, B, solver)`` is a ``torch.autograd``
 function: its backward runs one more solve with A^T = A on the stored factors
@@ -113,6 +118,16 @@ def cache_put(key: str, value) -> None:
     tmp.replace(p)
 
 
+def _config_of(rec):
+    """('levels', grid_mult) or ('dag', ctas_per_sm) from a cache record."""
+    if "config" in rec:
+        kind, v = str(rec["config"]).split(":")
+        if kind not in ("levels", "dag"):
+            raise ValueError(f"unknown schedule {kind!r}")
+        return kind, int(v)
+    return "levels", int(rec["grid_mult"])
+
+
 def choose(candidates, measure, reps: int = 2):
     """Smallest median time over `reps` runs of measure(candidate); returns (best, {cand: seconds})."""
     times = {}
@@ -145,13 +160,19 @@ class BatchedRBFSolver:
         self.device_name = torch.cuda.get_device_name(dev)
         self.key = tune_key(self.device_name, self.sizes, self.dim, self.nrhs, kernel, arith)
         self.tuned = None
+        self.schedule, self.dag_ctas = "levels", 3
+        cfg = None
         if grid_mult is None:
             hit = cache_get(self.key)
-            grid_mult = int(hit["grid_mult"]) if hit else 2
+            cfg = _config_of(hit) if hit else None
             self.tuned = hit
         self._plan = None
-        self._create(int(grid_mult))
         self._loaded = None
+        if cfg and cfg[0] == "dag":
+            self._create(2)
+            self._set_schedule("dag", cfg[1])
+        else:
+            self._create(int(cfg[1]) if cfg else int(grid_mult or 2))
 
     def _create(self, grid_mult: int):
         self.free()
@@ -162,6 +183,29 @@ class BatchedRBFSolver:
                                        ARITH[self.arith], grid_mult, ctypes.byref(h)), "batch_create")
         self._plan = h
         self.grid_mult = grid_mult
+        self.schedule = "levels"
+
+    def _set_schedule(self, schedule: str, ctas_per_sm: int = 3):
+        N.check(N.load().mpdok_batch_schedule(self._plan, 1 if schedule == "dag" else 0, int(ctas_per_sm)),
+                "batch_schedule")
+        self.schedule, self.dag_ctas = schedule, int(ctas_per_sm)
+
+    def configure(self, config: str):
+        """Apply a schedule: 'levels:<grid_mult>' or 'dag:<ctas per SM>'."""
+        kind, v = _config_of({"config": config})
+        if kind == "dag":
+            self._set_schedule("dag", v)
+        else:
+            if v != self.grid_mult:
+                self._create(v)
+                if self._loaded is not None:
+                    self.load(*self._loaded)
+            self._set_schedule("levels")
+        return self
+
+    @property
+    def config(self) -> str:
+        return f"dag:{self.dag_ctas}" if self.schedule == "dag" else f"levels:{self.grid_mult}"
 
     @property
     def device_bytes(self) -> int:
@@ -209,6 +253,18 @@ class BatchedRBFSolver:
         N.check(N.load().mpdok_batch_solve(self._plan, ptr(b), ptr(X), int(refine), stream_handle()), "batch_solve")
         return X
 
+    def step(self, B, refine: int = 2) -> torch.Tensor:
+        """Assembly + factor + solve + `refine` FP64 refinements under the plan's schedule."""
+        self._need_loaded()
+        b = self._rhs(B)
+        X = torch.empty_like(b)
+        N.check(N.load().mpdok_batch_step(self._plan, ptr(b), ptr(X), int(refine), stream_handle()), "batch_step")
+        return X
+
+    def dag_status(self):
+        """Raise when a task of the last task-graph step gave up waiting on its inputs."""
+        N.check(N.load().mpdok_batch_dag_status(self._plan, stream_handle()), "batch_dag_status")
+
     def relres(self, B, X) -> torch.Tensor:
         b = self._rhs(B)
         x = self._rhs(X)
@@ -248,39 +304,40 @@ class BatchedRBFSolver:
         return int(N.load().mpdok_batch_graph_nodes(self._plan))
 
     # -- tuning ---------------------------------------------------------------
-    def autotune(self, candidates=None, reps: int = 2, force: bool = False):
-        """Time the factorization for each trailing-update grid multiplier on the
-        loaded batch, keep the fastest, and cache it per device and batch."""
+    CANDIDATES = ("levels:2", "levels:4", "dag:2", "dag:3")
+
+    def autotune(self, candidates=None, reps: int = 1, force: bool = False):
+        """Time one full step (assembly, factor, solve, two refinements) per
+        schedule candidate on the loaded batch, keep the fastest and cache it
+        per device and batch.  Candidates: 'levels:<trailing-update grid
+        multiplier>' and 'dag:<CTAs per SM of the persistent task graph>'."""
         self._need_loaded()
         if not force:
             hit = cache_get(self.key)
-            if hit:
-                if int(hit["grid_mult"]) != self.grid_mult:
-                    self._create(int(hit["grid_mult"]))
-                    self.load(*self._loaded)
+            if hit and "config" in hit:
+                self.configure(hit["config"])
                 self.tuned = hit
                 return hit
-        loaded = self._loaded
-        cands = tuple(candidates or self.GRID_CANDIDATES)
+        cands = tuple(candidates or self.CANDIDATES)
+        Bt = torch.ones(self.total_x, dtype=torch.float64, device=require_cuda())
 
-        def measure(g):
-            if g != self.grid_mult:
-                self._create(g)
-                self.load(*loaded)
+        def measure(cfg):
+            self.configure(cfg)
+            self.step(Bt, refine=2)  # warm: allocation of the task-graph tables, first-touch
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            self.factor()
+            self.step(Bt, refine=2)
             e1.record()
             torch.cuda.synchronize()
+            if self.schedule == "dag":
+                self.dag_status()
             return e0.elapsed_time(e1) / 1e3
 
         best, times = choose(cands, measure, reps)
-        rec = {"grid_mult": best, "seconds": {str(k): v for k, v in times.items()}, "when": time.time()}
+        rec = {"config": best, "seconds": dict(times), "tile": 64, "when": time.time()}
         cache_put(self.key, rec)
-        if best != self.grid_mult:
-            self._create(best)
-            self.load(*loaded)
+        self.configure(best)
         self.tuned = rec
         return rec
 

@@ -77,6 +77,15 @@ struct BatchPlan {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   size_t graph_nodes = 0;
+  // schedule of the captured step: 0 level-synchronous launches, 1 one
+  // persistent task-graph launch (dag_ctas_per_sm CTAs per SM)
+  int schedule = 0, dag_ctas_per_sm = 3;
+  int dag_refine = -1, dag_nsec = 0;
+  long long dag_total = 0, dag_st_off = 0, dag_v_off = 0, dag_v_total = 0;
+  size_t dag_n_neg = 0, dag_n_zero = 0, dag_head_idx = 0;
+  long long* d_dagpre = nullptr;
+  void* d_secs = nullptr;
+  int* d_dagstate = nullptr;
 };
 
 // ------------------------------------------------------------------ helpers
@@ -705,6 +714,539 @@ __global__ void __launch_bounds__(BT) k_badj_reduce(const BSys* __restrict__ sys
   }
 }
 
+// ------------------------------------------------------------------ persistent task-graph step
+// The whole step (assembly, Cholesky, solve and FP64 refinement of every
+// system) as ONE persistent launch.  The work is a list of tile tasks in a
+// topological order:
+//   COPY(s, r)             X_r := B_r
+//   ASM(s, i, j)           tile (i, j) of A_s
+//   per level k: POTRF(s, k), TRSM(s, k, i), SYRK(s, k, i, j)
+//   per phase f = 0 .. refine (f = 0 solves into X, f >= 1 refines):
+//     RES(f, s, r)         V_r := B_r - (A X)_r                (f >= 1)
+//     forward, level k:    DIAG_F(f, s, k), UPD_F(f, s, k, r)   (r > k)
+//     backward, level k:   DIAG_B(f, s, k), UPD_B(f, s, k, r)   (r < k), k descending
+//     ADD(f, s, r)         X_r += V_r                            (f >= 1)
+// CTAs take tasks in list order from one atomic counter and wait (bounded,
+// one thread, acquire loads) until the task's inputs are final; every
+// dependency points to an earlier task, so a running CTA only ever waits on
+// tasks that running CTAs hold or have finished, and the launch needs no
+// co-residency.  Completion is published with a release after a fence:
+//   st[s](i, j)     lower tile: -1 unassembled, 0..j updates applied, j + 1 final
+//   fw[f][s][r]     block r of the phase's vector: -1 not ready, 0..r updates, r + 1 solved
+//   bw[f][s][r]     backward updates applied (from blocks > r), nblk - r once solved
+//   done[f][s]      blocks of X final after phase f;  asm_done[s]  tiles assembled
+// Reads of data other tasks wrote bypass L1 (ld.global.cg); the arithmetic of
+// every task is that of the level-scheduled kernels.
+enum BTaskKind : int { BT_COPY = 0, BT_ASM, BT_POTRF, BT_TRSM, BT_SYRK, BT_RES, BT_DIAGF, BT_UPDF, BT_DIAGB, BT_UPDB,
+                       BT_ADD };
+
+struct DagSec {         // one contiguous run of tasks of one kind
+  long long begin;      // first global task index
+  int kind, k, phase, pad;
+  long long pre_off;    // offset of its per-system prefix (cnt + 1 entries) in d_pre
+  int cnt, pad2;        // systems covered (a prefix of the sorted systems)
+};
+
+struct DagState {
+  int* st;        // Σ nblk (nblk + 1) / 2
+  int* fw;        // (refine + 1) x Σ nblk
+  int* bw;        // (refine + 1) x Σ nblk
+  int* done;      // (refine + 1) x nsys
+  int* asm_done;  // nsys
+  unsigned long long* head;
+  int* err;
+};
+
+__device__ __forceinline__ int ld_acq(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_rel(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+constexpr long long DAG_WAIT = 1LL << 25;
+
+// thread 0: spin until *p == want; false when the limit ran out or another
+// CTA has already given up (then every CTA stops within one poll)
+__device__ __forceinline__ bool dag_wait(const int* p, int want, const int* err) {
+  for (long long it = 0; it < DAG_WAIT; ++it) {
+    if (ld_acq(p) == want) return true;
+    if (it > 32) {
+      if ((it & 255) == 0 && *(volatile const int*)err) return false;
+      __nanosleep(it > 4096 ? 256 : 32);
+    }
+  }
+  return false;
+}
+
+__device__ __forceinline__ DF ld_df_cg(const double* p) {
+  const float2 f = __ldcg(reinterpret_cast<const float2*>(p));
+  DF r;
+  r.h = f.x;
+  r.l = f.y;
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ void stage_block_cg(T* sT, const double* __restrict__ src, long long ld, int nr, int nc) {
+  for (int e = threadIdx.x; e < BNB * BNB; e += BT) {
+    const int r = e & 63, kk = e >> 6;
+    DF v;
+    v.h = 0.f;
+    v.l = 0.f;
+    if (r < nr && kk < nc) v = ld_df_cg(src + (long long)r + (long long)kk * ld);
+    if constexpr (std::is_same<T, double>::value) sT[kk * BPAD + r] = df_to_f64(v);
+    else sT[kk * BPAD + r] = v;
+  }
+}
+
+__device__ __forceinline__ int tri_idx(int i, int j) { return i * (i + 1) / 2 + j; }
+
+template <int KIND, int D, int ARITH>
+__global__ void __launch_bounds__(BT) k_bstep_dag(const BSys* __restrict__ sys, const long long* __restrict__ pre,
+                                                  const DagSec* __restrict__ secs, int nsec, long long total,
+                                                  const long long* __restrict__ st_off, const long long* __restrict__ v_off,
+                                                  long long v_total, int nsys, int nrhs,
+                                                  const double* __restrict__ coords, double* __restrict__ A,
+                                                  double* __restrict__ Linv, const double* __restrict__ B,
+                                                  double* __restrict__ X, double* __restrict__ V, int* pert,
+                                                  DagState S) {
+  extern __shared__ double smem[];
+  __shared__ long long s_t;
+  __shared__ int s_ok;
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  for (;;) {
+    if (tid == 0) s_t = *(volatile const int*)S.err ? total : (long long)atomicAdd(S.head, 1ULL);
+    __syncthreads();
+    const long long t = s_t;
+    if (t >= total) return;
+    // section of t
+    int lo = 0, hi = nsec - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (secs[mid].begin <= t) lo = mid; else hi = mid - 1;
+    }
+    const DagSec sec = secs[lo];
+    const long long u0 = t - sec.begin;
+    const long long* sp = pre + sec.pre_off;
+    const int s = task_system(sp, sec.cnt + 1, u0);
+    const BSys q = sys[s];
+    const long long u = u0 - sp[s];
+    const int k = sec.k, f = sec.phase;
+    int* st = S.st + st_off[s];
+    int* fw = S.fw + (long long)f * v_total + v_off[s];
+    int* bw = S.bw + (long long)f * v_total + v_off[s];
+    double* Ab = A + q.offA;
+    const long long lda = q.n;
+    const int nblk = q.nblk;
+    // ---- decode the task's tiles, wait for its inputs
+    int ti = 0, tj = 0;
+    if (tid == 0) {
+      bool ok = true;
+      switch (sec.kind) {
+        case BT_COPY: case BT_ASM: break;
+        case BT_POTRF: ok = dag_wait(st + tri_idx(k, k), k, S.err); break;
+        case BT_TRSM:
+          ti = k + 1 + (int)u;
+          ok = dag_wait(st + tri_idx(k, k), k + 1, S.err) && dag_wait(st + tri_idx(ti, k), k, S.err);
+          break;
+        case BT_SYRK: {
+          int a = (int)((sqrt(8.0 * (double)u + 1.0) - 1.0) * 0.5);
+          while ((long long)(a + 1) * (a + 2) / 2 <= u) ++a;
+          while ((long long)a * (a + 1) / 2 > u) --a;
+          ti = k + 1 + a;
+          tj = k + 1 + (int)(u - (long long)a * (a + 1) / 2);
+          ok = dag_wait(st + tri_idx(ti, k), k + 1, S.err) && dag_wait(st + tri_idx(tj, k), k + 1, S.err) &&
+               dag_wait(st + tri_idx(ti, tj), k, S.err);
+          break;
+        }
+        case BT_RES:
+          ok = dag_wait(S.done + (long long)(f - 1) * nsys + s, nblk, S.err) &&
+               dag_wait(S.asm_done + s, nblk * nblk, S.err);
+          break;
+        case BT_DIAGF: ok = dag_wait(st + tri_idx(k, k), k + 1, S.err) && dag_wait(fw + k, k, S.err); break;
+        case BT_UPDF:
+          ti = k + 1 + (int)u;
+          ok = dag_wait(st + tri_idx(ti, k), k + 1, S.err) && dag_wait(fw + k, k + 1, S.err) &&
+               dag_wait(fw + ti, k, S.err);
+          break;
+        case BT_DIAGB: ok = dag_wait(fw + k, k + 1, S.err) && dag_wait(bw + k, nblk - 1 - k, S.err); break;
+        case BT_UPDB:
+          ti = (int)u;  // r < k
+          ok = dag_wait(bw + k, nblk - k, S.err) && dag_wait(bw + ti, nblk - 1 - k, S.err) &&
+               dag_wait(fw + ti, ti + 1, S.err);
+          break;
+        case BT_ADD: ti = (int)u; ok = dag_wait(bw + ti, nblk - ti, S.err); break;
+      }
+      s_ok = ok ? 1 : 0;
+      if (!ok) atomicExch(S.err, 1);
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    if (sec.kind == BT_TRSM || sec.kind == BT_UPDF || sec.kind == BT_UPDB || sec.kind == BT_ADD) {
+      ti = (sec.kind == BT_TRSM || sec.kind == BT_UPDF) ? k + 1 + (int)u : (int)u;
+    } else if (sec.kind == BT_SYRK) {
+      int a = (int)((sqrt(8.0 * (double)u + 1.0) - 1.0) * 0.5);
+      while ((long long)(a + 1) * (a + 2) / 2 <= u) ++a;
+      while ((long long)a * (a + 1) / 2 > u) --a;
+      ti = k + 1 + a;
+      tj = k + 1 + (int)(u - (long long)a * (a + 1) / 2);
+    }
+    // ---- the task
+    int* pub = nullptr;  // state word set to pub_val when the task is done
+    int pub_val = 0;
+    int* cnt_add = nullptr;  // counter incremented when the task is done
+    switch (sec.kind) {
+      case BT_COPY: {
+        const int r = (int)u, r0 = r * BNB, nr = min(BNB, q.n - r0);
+        for (int e = tid; e < BNB * nrhs; e += BT) {
+          const int i = e % BNB, c = e / BNB;
+          if (i < nr) {
+            const long long o = q.offX + (long long)(r0 + i) + (long long)c * q.n;
+            X[o] = B[o];
+          }
+        }
+        pub = S.fw + v_off[s] + r;  // phase 0
+        pub_val = 0;
+        break;
+      }
+      case BT_ASM: {
+        ti = (int)(u % nblk);
+        tj = (int)(u / nblk);
+        double* sR = smem;
+        double* sC = smem + BNB * D;
+        const int r0 = ti * BNB, c0 = tj * BNB;
+        const double* Xc = coords + q.offC;
+        for (int e = tid; e < BNB * D; e += BT) {
+          const int i = e / D, d = e % D;
+          sR[e] = (r0 + i < q.n) ? Xc[(long long)(r0 + i) * D + d] : 0.0;
+          sC[e] = (c0 + i < q.n) ? Xc[(long long)(c0 + i) * D + d] : 0.0;
+        }
+        __syncthreads();
+        const int row = tid & 63;
+        for (int col = tid >> 6; col < BNB; col += BT / BNB) {
+          const int i = r0 + row, j = c0 + col;
+          if (i >= q.n || j >= q.n) continue;
+          double r2 = 0.0;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            const double df = sR[row * D + d] - sC[col * D + d];
+            r2 = fma(df, df, r2);
+          }
+          double v = phi_only<KIND>(r2, q.gamma);
+          if (i == j) v += q.reg;
+          double* slot = Ab + (long long)i + (long long)j * q.n;
+          if (i >= j) st_df(slot, to_df(v));
+          else *slot = v;
+        }
+        if (ti >= tj) {
+          pub = st + tri_idx(ti, tj);
+          pub_val = 0;
+        }
+        cnt_add = S.asm_done + s;
+        break;
+      }
+      case BT_POTRF: {
+        double* sL = smem;
+        double* sI = smem + BNB * BPAD;
+        double* s_inv = smem + 2 * BNB * BPAD;
+        const int kb = k * BNB;
+        const int nb = min(BNB, q.n - kb);
+        for (int e = tid; e < BNB * BNB; e += BT) {
+          const int i = e & 63, j = e >> 6;
+          double v = 0.0;
+          if (i < nb && j < nb && i >= j) v = df_to_f64(ld_df_cg(Ab + (long long)(kb + i) + (long long)(kb + j) * lda));
+          sL[i * BPAD + j] = v;
+          sI[i * BPAD + j] = 0.0;
+        }
+        __syncthreads();
+        const double dref = 1.0 + q.reg;
+        for (int j = 0; j < nb; ++j) {
+          if (tid == 0) {
+            double d = sL[j * BPAD + j];
+            if (!(d > 1e-15 * dref)) {
+              d = 1e-15 * dref;
+              atomicAdd(pert, 1);
+            }
+            const double p = sqrt(d);
+            sL[j * BPAD + j] = p;
+            *s_inv = 1.0 / p;
+          }
+          __syncthreads();
+          const double ip = *s_inv;
+          for (int i = j + 1 + tid; i < nb; i += BT) sL[i * BPAD + j] *= ip;
+          __syncthreads();
+          const int m = nb - j - 1;
+          for (int e = tid; e < m * m; e += BT) {
+            const int i = j + 1 + e / m, l = j + 1 + e % m;
+            if (l <= i) sL[i * BPAD + l] -= sL[i * BPAD + j] * sL[l * BPAD + j];
+          }
+          __syncthreads();
+        }
+        for (int i = 0; i < nb; ++i) {
+          const int c = tid;
+          if (c <= i && c < BNB) {
+            double acc = (c == i) ? 1.0 : 0.0;
+            for (int l = c; l < i; ++l) acc -= sL[i * BPAD + l] * sI[l * BPAD + c];
+            sI[i * BPAD + c] = acc / sL[i * BPAD + i];
+          }
+          __syncthreads();
+        }
+        for (int e = tid; e < BNB * BNB; e += BT) {
+          const int i = e & 63, j = e >> 6;
+          if (i < nb && j < nb && i >= j)
+            st_df(Ab + (long long)(kb + i) + (long long)(kb + j) * lda, to_df(sL[i * BPAD + j]));
+          Linv[q.offL + (long long)k * BNB * BNB + i + (long long)j * BNB] = sI[i * BPAD + j];
+        }
+        pub = st + tri_idx(k, k);
+        pub_val = k + 1;
+        break;
+      }
+      case BT_TRSM: {
+        double* sA = smem;
+        double* sB = smem + BNB * BPAD;
+        const int kb = k * BNB, r0 = ti * BNB;
+        const int nb = min(BNB, q.n - kb), nr = min(BNB, q.n - r0);
+        stage_block_cg(sA, Ab + r0 + (long long)kb * lda, lda, nr, nb);
+        const double* Li = Linv + q.offL + (long long)k * BNB * BNB;
+        for (int e = tid; e < BNB * BNB; e += BT) {
+          const int col = e & 63, kk = e >> 6;
+          sB[kk * BPAD + col] = __ldcg(Li + col + kk * BNB);
+        }
+        __syncthreads();
+        double acc[4][4] = {};
+        tile_fma_f64(sA, sB, acc, ty, tx);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int row = ty * 4 + i, col = tx * 4 + j;
+            if (row < nr && col < nb)
+              st_df(Ab + (long long)(r0 + row) + (long long)(kb + col) * lda, to_df(acc[i][j]));
+          }
+        pub = st + tri_idx(ti, k);
+        pub_val = k + 1;
+        break;
+      }
+      case BT_SYRK: {
+        using STT = typename std::conditional<ARITH == 0, double, DF>::type;
+        STT* sA = reinterpret_cast<STT*>(smem);
+        STT* sB = sA + BNB * BPAD;
+        const int kb = k * BNB, r0 = ti * BNB, c0 = tj * BNB;
+        const int nb = min(BNB, q.n - kb), nr = min(BNB, q.n - r0), nc = min(BNB, q.n - c0);
+        stage_block_cg(sA, Ab + r0 + (long long)kb * lda, lda, nr, nb);
+        stage_block_cg(sB, Ab + c0 + (long long)kb * lda, lda, nc, nb);
+        __syncthreads();
+        if (ARITH == 0) {
+          double acc[4][4] = {};
+          tile_fma_f64(reinterpret_cast<const double*>(sA), reinterpret_cast<const double*>(sB), acc, ty, tx);
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const int row = ty * 4 + i, col = tx * 4 + j;
+              if (row < nr && col < nc && (ti != tj || row >= col)) {
+                double* p = Ab + (long long)(r0 + row) + (long long)(c0 + col) * lda;
+                st_df(p, to_df(df_to_f64(ld_df_cg(p)) - acc[i][j]));
+              }
+            }
+        } else {
+          float sh[4][4] = {}, sl[4][4] = {};
+          tile_fma_df(reinterpret_cast<const DF*>(sA), reinterpret_cast<const DF*>(sB), sh, sl, ty, tx);
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const int row = ty * 4 + i, col = tx * 4 + j;
+              if (row < nr && col < nc && (ti != tj || row >= col)) {
+                double* p = Ab + (long long)(r0 + row) + (long long)(c0 + col) * lda;
+                const float h = sh[i][j] + sl[i][j];
+                const float l = sl[i][j] - (h - sh[i][j]);
+                st_df(p, df_sub(ld_df_cg(p), h, l));
+              }
+            }
+        }
+        pub = st + tri_idx(ti, tj);
+        pub_val = k + 1;
+        break;
+      }
+      case BT_RES: {
+        const int r = (int)u, r0 = r * BNB, nr = min(BNB, q.n - r0);
+        double* sT = smem;
+        double* sX = smem + BNB * BPAD;
+        const double dia = 1.0 + q.reg;
+        const int row = tid & 63, g = tid >> 6;
+        double acc[2] = {0.0, 0.0};
+        for (int c = 0; c < nblk; ++c) {
+          const int c0 = c * BNB, nc = min(BNB, q.n - c0);
+          __syncthreads();
+          for (int e = tid; e < BNB * BNB; e += BT) {
+            const int i = e & 63, j = e >> 6;
+            double v = 0.0;
+            if (r < c) {
+              if (i < nr && j < nc) v = __ldcg(Ab + (long long)(r0 + i) + (long long)(c0 + j) * lda);
+              sT[j * BPAD + i] = v;
+            } else if (r > c) {
+              if (i < nc && j < nr) v = __ldcg(Ab + (long long)(c0 + i) + (long long)(r0 + j) * lda);
+              sT[i * BPAD + j] = v;
+            } else {
+              if (i < nr && j < nr) {
+                if (i < j) v = __ldcg(Ab + (long long)(r0 + i) + (long long)(r0 + j) * lda);
+                else if (i > j) v = __ldcg(Ab + (long long)(r0 + j) + (long long)(r0 + i) * lda);
+                else v = dia;
+              }
+              sT[j * BPAD + i] = v;
+            }
+          }
+          for (int e = tid; e < BNB * nrhs; e += BT) {
+            const int i = e % BNB, rr = e / BNB;
+            sX[e] = (i < nc) ? __ldcg(X + q.offX + (long long)(c0 + i) + (long long)rr * q.n) : 0.0;
+          }
+          __syncthreads();
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int rr = g + 4 * h;
+            if (rr < nrhs) {
+              double a = acc[h];
+#pragma unroll 8
+              for (int j = 0; j < BNB; ++j) a = fma(sT[j * BPAD + row], sX[rr * BNB + j], a);
+              acc[h] = a;
+            }
+          }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int rr = g + 4 * h;
+          if (rr < nrhs && row < nr) {
+            const long long o = q.offX + (long long)(r0 + row) + (long long)rr * q.n;
+            V[o] = B[o] - acc[h];
+          }
+        }
+        pub = fw + r;
+        pub_val = 0;
+        break;
+      }
+      case BT_DIAGF:
+      case BT_DIAGB: {
+        const bool trans = sec.kind == BT_DIAGB;
+        double* Vec = f == 0 ? X : V;
+        double* sX = smem;
+        double* sLi = smem + BNB * BMAX_RHS;
+        const int kb = k * BNB, nb = min(BNB, q.n - kb);
+        double* Vb = Vec + q.offX;
+        const double* Li = Linv + q.offL + (long long)k * BNB * BNB;
+        for (int e = tid; e < BNB * nrhs; e += BT) {
+          const int i = e % BNB, r = e / BNB;
+          sX[e] = (i < nb) ? __ldcg(Vb + (long long)(kb + i) + (long long)r * q.n) : 0.0;
+        }
+        for (int e = tid; e < BNB * BNB; e += BT) {
+          const int i = e & 63, j = e >> 6;
+          sLi[i * BPAD + j] = __ldcg(Li + i + j * BNB);
+        }
+        __syncthreads();
+        for (int e = tid; e < BNB * nrhs; e += BT) {
+          const int i = e % BNB, r = e / BNB;
+          if (i >= nb) continue;
+          double acc = 0.0;
+          if (!trans) {
+            for (int c = 0; c <= i; ++c) acc = fma(sLi[i * BPAD + c], sX[r * BNB + c], acc);
+          } else {
+            for (int c = i; c < nb; ++c) acc = fma(sLi[c * BPAD + i], sX[r * BNB + c], acc);
+          }
+          Vb[(long long)(kb + i) + (long long)r * q.n] = acc;
+        }
+        if (!trans) {
+          pub = fw + k;
+          pub_val = k + 1;
+        } else {
+          pub = bw + k;
+          pub_val = nblk - k;
+          if (f == 0) cnt_add = S.done + s;  // phase 0 solves straight into X
+        }
+        break;
+      }
+      case BT_UPDF:
+      case BT_UPDB: {
+        const bool trans = sec.kind == BT_UPDB;
+        double* Vec = f == 0 ? X : V;
+        DF* sT = reinterpret_cast<DF*>(smem);
+        DF* sX = sT + BNB * BPAD;
+        const int r = ti;
+        const int kb = k * BNB, r0 = r * BNB;
+        const int nb = min(BNB, q.n - kb), nr = min(BNB, q.n - r0);
+        double* Vb = Vec + q.offX;
+        if (!trans) {
+          stage_block_cg(sT, Ab + r0 + (long long)kb * lda, lda, nr, nb);
+        } else {
+          for (int e = tid; e < BNB * BNB; e += BT) {
+            const int kk = e & 63, row = e >> 6;
+            DF v;
+            v.h = 0.f;
+            v.l = 0.f;
+            if (kk < nb && row < nr) v = ld_df_cg(Ab + (long long)(kb + kk) + (long long)(r0 + row) * lda);
+            sT[kk * BPAD + row] = v;
+          }
+        }
+        for (int e = tid; e < BNB * nrhs; e += BT) {
+          const int i = e % BNB, rr = e / BNB;
+          sX[e] = to_df((i < nb) ? __ldcg(Vb + (long long)(kb + i) + (long long)rr * q.n) : 0.0);
+        }
+        __syncthreads();
+        for (int e = tid; e < BNB * nrhs; e += BT) {
+          const int row = e % BNB, rr = e / BNB;
+          if (row >= nr) continue;
+          float sh = 0.f, sl = 0.f;
+#pragma unroll 4
+          for (int kk = 0; kk < BNB; ++kk) {
+            const DF a = sT[kk * BPAD + row], b = sX[rr * BNB + kk];
+            const float ph = a.h * b.h;
+            float pl = fmaf(a.h, b.h, -ph);
+            pl = fmaf(a.h, b.l, pl);
+            pl = fmaf(a.l, b.h, pl);
+            const float tt = sh + ph;
+            const float bp = tt - sh;
+            const float er = (sh - (tt - bp)) + (ph - bp);
+            sh = tt;
+            sl += er + pl;
+          }
+          double* pv = Vb + (long long)(r0 + row) + (long long)rr * q.n;
+          *pv = __ldcg(pv) - ((double)sh + (double)sl);
+        }
+        if (!trans) {
+          pub = fw + r;
+          pub_val = k + 1;
+        } else {
+          pub = bw + r;
+          pub_val = nblk - k;
+        }
+        break;
+      }
+      case BT_ADD: {
+        const int r = ti, r0 = r * BNB, nr = min(BNB, q.n - r0);
+        for (int e = tid; e < BNB * nrhs; e += BT) {
+          const int i = e % BNB, c = e / BNB;
+          if (i < nr) {
+            const long long o = q.offX + (long long)(r0 + i) + (long long)c * q.n;
+            X[o] = __ldcg(X + o) + __ldcg(V + o);
+          }
+        }
+        cnt_add = S.done + (long long)f * nsys + s;
+        break;
+      }
+    }
+    // ---- publish
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      if (pub) st_rel(pub, pub_val);
+      if (cnt_add) atomicAdd(cnt_add, 1);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ host side
 
 static const long long* preT_dev(const BatchPlan* p, int k) { return p->d_pre + p->preT_off[k]; }
@@ -843,7 +1385,142 @@ int batch_precond(void* plan, long long n, int K, double* tmp, BatchPcCtx* ctx, 
   return MPDOK_OK;
 }
 
+static void dag_release(BatchPlan* p) {
+  if (p->d_dagpre) cudaFree(p->d_dagpre);
+  if (p->d_secs) cudaFree(p->d_secs);
+  if (p->d_dagstate) cudaFree(p->d_dagstate);
+  p->d_dagpre = nullptr;
+  p->d_secs = nullptr;
+  p->d_dagstate = nullptr;
+  p->dag_refine = -1;
+}
+
+// Host side of the task-graph step: the section table for `refine` refinement
+// phases, the prefix tables it needs beyond the level tables, and the state.
+static int dag_prepare(BatchPlan* p, int refine) {
+  if (p->dag_refine == refine && p->d_secs) return MPDOK_OK;
+  std::vector<long long> pre;  // appended prefix arrays; offsets into d_dagpre
+  std::vector<DagSec> secs;
+  long long begin = 0;
+  auto add_prefix = [&](const std::vector<long long>& v) {
+    const long long off = (long long)pre.size();
+    pre.insert(pre.end(), v.begin(), v.end());
+    return off;
+  };
+  auto prefix_of = [&](int cnt, auto count) {
+    std::vector<long long> v(1, 0);
+    for (int i = 0; i < cnt; ++i) v.push_back(v.back() + count(i));
+    return v;
+  };
+  auto add_sec = [&](int kind, int k, int phase, int cnt, const std::vector<long long>& v) {
+    if (v.back() == 0) return;
+    DagSec d{};
+    d.begin = begin;
+    d.kind = kind;
+    d.k = k;
+    d.phase = phase;
+    d.pre_off = add_prefix(v);
+    d.cnt = cnt;
+    secs.push_back(d);
+    begin += v.back();
+  };
+  const int ns = p->nsys;
+  const auto rows = prefix_of(ns, [&](int i) { return (long long)p->sys[i].nblk; });
+  add_sec(BT_COPY, 0, 0, ns, rows);
+  add_sec(BT_ASM, 0, 0, ns, prefix_of(ns, [&](int i) { return (long long)p->sys[i].nblk * p->sys[i].nblk; }));
+  for (int k = 0; k < p->maxblk; ++k) {
+    const int cnt = p->act[k];
+    add_sec(BT_POTRF, k, 0, cnt, prefix_of(cnt, [](int) { return 1LL; }));
+    add_sec(BT_TRSM, k, 0, cnt, prefix_of(cnt, [&](int i) { return (long long)(p->sys[i].nblk - k - 1); }));
+    add_sec(BT_SYRK, k, 0, cnt, prefix_of(cnt, [&](int i) {
+      const long long T = p->sys[i].nblk - k - 1;
+      return T * (T + 1) / 2;
+    }));
+  }
+  for (int f = 0; f <= refine; ++f) {
+    if (f > 0) add_sec(BT_RES, 0, f, ns, rows);
+    for (int k = 0; k < p->maxblk; ++k) {
+      const int cnt = p->act[k];
+      add_sec(BT_DIAGF, k, f, cnt, prefix_of(cnt, [](int) { return 1LL; }));
+      add_sec(BT_UPDF, k, f, cnt, prefix_of(cnt, [&](int i) { return (long long)(p->sys[i].nblk - k - 1); }));
+    }
+    for (int k = p->maxblk - 1; k >= 0; --k) {
+      const int cnt = p->act[k];
+      add_sec(BT_DIAGB, k, f, cnt, prefix_of(cnt, [](int) { return 1LL; }));
+      add_sec(BT_UPDB, k, f, cnt, prefix_of(cnt, [&](int) { return (long long)k; }));
+    }
+    if (f > 0) add_sec(BT_ADD, 0, f, ns, rows);
+  }
+  // per-system offsets of the tile states and of the vector blocks
+  std::vector<long long> st_off(ns), v_off(ns);
+  long long ast = 0, av = 0;
+  for (int i = 0; i < ns; ++i) {
+    st_off[i] = ast;
+    v_off[i] = av;
+    ast += (long long)p->sys[i].nblk * (p->sys[i].nblk + 1) / 2;
+    av += p->sys[i].nblk;
+  }
+  const long long off_st = add_prefix(st_off), off_v = add_prefix(v_off);
+  dag_release(p);
+  MPDOK_CUDA_TRY(cudaMalloc(&p->d_dagpre, pre.size() * sizeof(long long)));
+  MPDOK_CUDA_TRY(cudaMemcpy(p->d_dagpre, pre.data(), pre.size() * sizeof(long long), cudaMemcpyHostToDevice));
+  MPDOK_CUDA_TRY(cudaMalloc(&p->d_secs, secs.size() * sizeof(DagSec)));
+  MPDOK_CUDA_TRY(cudaMemcpy(p->d_secs, secs.data(), secs.size() * sizeof(DagSec), cudaMemcpyHostToDevice));
+  p->dag_nsec = (int)secs.size();
+  p->dag_total = begin;
+  p->dag_st_off = off_st;
+  p->dag_v_off = off_v;
+  p->dag_v_total = av;
+  // states: [st | fw] start at -1, [bw | done | asm_done | head | err] at 0
+  p->dag_n_neg = (size_t)ast + (size_t)(refine + 1) * av;
+  size_t head = p->dag_n_neg + (size_t)(refine + 1) * av + (size_t)(refine + 1) * ns + ns;
+  head = (head + 1) & ~(size_t)1;  // the 8-byte queue counter
+  p->dag_head_idx = head;
+  p->dag_n_zero = head + 4 - p->dag_n_neg;  // head (2 ints), err, spare
+  MPDOK_CUDA_TRY(cudaMalloc(&p->d_dagstate, (p->dag_n_neg + p->dag_n_zero) * sizeof(int)));
+  p->dag_refine = refine;
+  return MPDOK_OK;
+}
+
+static int batch_step_dag(BatchPlan* p, const double* B, double* X, int refine, cudaStream_t s) {
+  MPDOK_TRY(dag_prepare(p, refine));
+  int* base = p->d_dagstate;
+  MPDOK_CUDA_TRY(cudaMemsetAsync(base, 0xff, p->dag_n_neg * sizeof(int), s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(base + p->dag_n_neg, 0, p->dag_n_zero * sizeof(int), s));
+  MPDOK_CUDA_TRY(cudaMemsetAsync(p->d_pert, 0, sizeof(int), s));
+  const long long av = p->dag_v_total;
+  const size_t ast = p->dag_n_neg - (size_t)(refine + 1) * av;
+  DagState S;
+  S.st = base;
+  S.fw = base + ast;
+  S.bw = base + p->dag_n_neg;
+  S.done = S.bw + (refine + 1) * av;
+  S.asm_done = S.done + (refine + 1) * p->nsys;
+  S.head = reinterpret_cast<unsigned long long*>(base + p->dag_head_idx);
+  S.err = base + p->dag_head_idx + 2;
+  const size_t smem = (2 * (size_t)BNB * BPAD + 32) * sizeof(double);
+  const int grid = std::max(1, p->dag_ctas_per_sm) * num_sms();
+  const long long* sto = p->d_dagpre + p->dag_st_off;
+  const long long* vo = p->d_dagpre + p->dag_v_off;
+#define DAG_LAUNCH(KK, DD, AR)                                                                                   \
+  do {                                                                                                           \
+    MPDOK_TRY(set_smem(k_bstep_dag<KK, DD, AR>, smem));                                                          \
+    launch(k_bstep_dag<KK, DD, AR>, dim3(grid), BT, smem, s, (const BSys*)p->d_sys, (const long long*)p->d_dagpre, \
+           (const DagSec*)p->d_secs, p->dag_nsec, p->dag_total, sto, vo, av, p->nsys, p->nrhs,                   \
+           (const double*)p->coords, p->A, p->Linv, B, X, p->V, p->d_pert, S);                                   \
+  } while (0)
+  if (p->arith == 0) {
+    BKIND_DIM_SWITCH(p->kernel, p->dim, DAG_LAUNCH(KK_, DD_, 0));
+  } else {
+    BKIND_DIM_SWITCH(p->kernel, p->dim, DAG_LAUNCH(KK_, DD_, 1));
+  }
+#undef DAG_LAUNCH
+  MPDOK_LAUNCH_CHECK("batch task-graph step");
+  return MPDOK_OK;
+}
+
 static void plan_free(BatchPlan* p) {
+  dag_release(p);
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   if (p->cap) cudaStreamDestroy(p->cap);
@@ -1043,6 +1720,45 @@ extern "C" int mpdok_batch_adjoint(void* plan, const double* X, const double* La
   return MPDOK_OK;
 }
 
+// The adjoint contraction of ONE system (the in-core path's gradients), with
+// the batch kernels on a one-system description kept in the workspace:
+// [BSys | prefix (2) | per-row partials (2 n)].
+extern "C" size_t mpdok_rbf_adjoint_workspace_size(long long n) {
+  if (n < 0) return 0;
+  return 256 + 256 + align_up((size_t)std::max(1LL, n) * 2 * sizeof(double), 256);
+}
+
+extern "C" int mpdok_rbf_adjoint(const double* coords, long long n, int dim, int kernel, double eps, int nrhs,
+                                 const double* X, const double* Lam, double* grad_coords, double* grad_eps,
+                                 double* grad_reg, void* work, size_t work_bytes, cudaStream_t s) {
+  MPDOK_ARG_CHECK(n >= 1 && n <= (1LL << 30), "n out of range");
+  MPDOK_ARG_CHECK(dim >= 1 && dim <= 3, "dim must be 1, 2 or 3");
+  MPDOK_ARG_CHECK(kernel == MPDOK_KERNEL_GAUSSIAN || kernel == MPDOK_KERNEL_MQ, "unknown kernel");
+  MPDOK_ARG_CHECK(nrhs >= 1 && nrhs <= BMAX_RHS, "nrhs must be in [1, 8]");
+  MPDOK_ARG_CHECK(coords && X && Lam && grad_coords && grad_eps && grad_reg && work, "null pointer");
+  MPDOK_ARG_CHECK(work_bytes >= mpdok_rbf_adjoint_workspace_size(n), "adjoint workspace too small");
+  BSys q{};
+  q.n = (int)n;
+  q.nblk = (int)((n + BNB - 1) / BNB);
+  q.eps = eps;
+  q.gamma = eps * eps;
+  char* w = (char*)work;
+  BSys* d_sys = (BSys*)w;
+  long long* d_pre = (long long*)(w + 256);
+  double* rows = (double*)(w + 512);
+  const long long pre[2] = {0, q.nblk};
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(d_sys, &q, sizeof(BSys), cudaMemcpyHostToDevice, s));
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(d_pre, pre, sizeof(pre), cudaMemcpyHostToDevice, s));
+  BKIND_DIM_SWITCH(kernel, dim,
+                   launch(k_badjoint<KK_, DD_>, dim3((unsigned)q.nblk), BT, 0, s, (const BSys*)d_sys,
+                          (const long long*)d_pre, 1, nrhs, coords, X, Lam, grad_coords, rows));
+  launch(k_badj_reduce, dim3(1), BT, 0, s, (const BSys*)d_sys, (const double*)rows, grad_eps, grad_reg);
+  MPDOK_LAUNCH_CHECK("rbf adjoint");
+  // the host copies above read stack memory: finish them before returning
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  return MPDOK_OK;
+}
+
 extern "C" int mpdok_batch_perturbed(void* plan, cudaStream_t s) {
   if (!plan) return MPDOK_ERR_INVALID_ARG;
   BatchPlan* p = (BatchPlan*)plan;
@@ -1065,9 +1781,15 @@ extern "C" int mpdok_batch_graph_build(void* plan, const double* B, double* X, i
     cudaGraphDestroy(p->graph);
     p->graph = nullptr;
   }
+  if (p->schedule == 1) MPDOK_TRY(dag_prepare(p, refine));  // (allocates: before the capture)
   MPDOK_CUDA_TRY(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
-  int st = batch_factor(p, p->cap);
-  if (st == MPDOK_OK) st = batch_solve(p, B, X, refine, p->cap);
+  int st;
+  if (p->schedule == 1) {
+    st = batch_step_dag(p, B, X, refine, p->cap);
+  } else {
+    st = batch_factor(p, p->cap);
+    if (st == MPDOK_OK) st = batch_solve(p, B, X, refine, p->cap);
+  }
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(p->cap, &g);
   if (st != MPDOK_OK) {
@@ -1092,6 +1814,40 @@ extern "C" int mpdok_batch_graph_launch(void* plan, cudaStream_t s) {
   }
   MPDOK_CUDA_TRY(cudaGraphLaunch(p->exec, s));
   count_launch();
+  return MPDOK_OK;
+}
+
+extern "C" int mpdok_batch_schedule(void* plan, int schedule, int ctas_per_sm) {
+  MPDOK_ARG_CHECK(plan, "null plan");
+  MPDOK_ARG_CHECK(schedule == 0 || schedule == 1, "schedule must be 0 (levels) or 1 (task graph)");
+  MPDOK_ARG_CHECK(ctas_per_sm >= 1 && ctas_per_sm <= 3, "ctas_per_sm must be in [1, 3]");
+  BatchPlan* p = (BatchPlan*)plan;
+  p->schedule = schedule;
+  p->dag_ctas_per_sm = ctas_per_sm;
+  return MPDOK_OK;
+}
+
+extern "C" int mpdok_batch_step(void* plan, const double* B, double* X, int refine, cudaStream_t s) {
+  MPDOK_ARG_CHECK(plan && B && X, "null pointer");
+  MPDOK_ARG_CHECK(refine >= 0 && refine <= 16, "refine must be in [0, 16]");
+  BatchPlan* p = (BatchPlan*)plan;
+  if (p->schedule == 1) return batch_step_dag(p, B, X, refine, s);
+  MPDOK_TRY(batch_factor(p, s));
+  return batch_solve(p, B, X, refine, s);
+}
+
+extern "C" int mpdok_batch_dag_status(void* plan, cudaStream_t s) {
+  MPDOK_ARG_CHECK(plan, "null plan");
+  BatchPlan* p = (BatchPlan*)plan;
+  if (!p->d_dagstate) return MPDOK_OK;
+  int h = 0;
+  const int* err = p->d_dagstate + p->dag_head_idx + 2;
+  MPDOK_CUDA_TRY(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MPDOK_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h) {
+    set_error("batch task graph: a task's wait on its inputs ran out");
+    return MPDOK_ERR_TIMEOUT;
+  }
   return MPDOK_OK;
 }
 

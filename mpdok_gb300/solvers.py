@@ -59,14 +59,19 @@ class MixedSolver:
         """x, info for A x = b.  A may live on the host: then it is uploaded
         straight into its device buffer, and for the LU method its FP32 copy
         is made block by block while the rest of A is still in flight."""
+        t_host = time.perf_counter()
         b64 = as_vector(b, torch.float64)
         n = int(A.shape[0])
         if self._a32 is None or self._a32.shape[0] != n:
             self._a32 = fortran_empty(n, n, torch.float32)
         a32_ready = False
+        up = None
         if isinstance(A, torch.Tensor) and not A.is_cuda and A.dtype == torch.float64 and A.dim() == 2 \
                 and self.method != "gmres-ir":
+            up = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
+            up[0].record()
             A64 = upload_fortran(A, out32=self._a32)
+            up[1].record()
             a32_ready = True
         else:
             A64 = as_fortran(A, torch.float64)
@@ -93,7 +98,10 @@ class MixedSolver:
         d["factor_ms"] = ev[0].elapsed_time(ev[1])
         d["refine_ms"] = ev[1].elapsed_time(ev[2])
         d["perturbed_pivots"] = lu.n_perturbed
-        self.last_timing = {"factor_ms": d["factor_ms"], "refine_ms": d["refine_ms"]}
+        self.last_timing = {"factor_ms": d["factor_ms"], "refine_ms": d["refine_ms"],
+                            "host_ms": (time.perf_counter() - t_host) * 1e3}
+        if up is not None:
+            self.last_timing["upload_ms"] = up[0].elapsed_time(up[1])
         if not d["converged"]:
             why = ("the FP64 residual diverged; the best iterate is returned" if d["diverged"]
                    else f"not converged in {self.maxiter_outer} outer steps")

@@ -165,10 +165,11 @@ def test_batch_autotune_picks_and_caches(tmp_path, monkeypatch):
     Xs, eps, Bs = _batch(sizes, 2, 2, seed=1)
     s = Bt.BatchedRBFSolver(sizes, dim=2, nrhs=2)
     s.load(Xs, eps, 1e-6)
-    rec = s.autotune(candidates=(1, 2), reps=1)
-    assert rec["grid_mult"] in (1, 2) and s.grid_mult == rec["grid_mult"]
+    rec = s.autotune(candidates=("levels:1", "levels:2", "dag:2", "dag:3"), reps=1)
+    assert rec["config"] in ("levels:1", "levels:2", "dag:2", "dag:3") and s.config == rec["config"]
+    assert set(rec["seconds"]) == {"levels:1", "levels:2", "dag:2", "dag:3"} and rec["tile"] == 64
     s2 = Bt.BatchedRBFSolver(sizes, dim=2, nrhs=2)
-    assert s2.tuned is not None and s2.grid_mult == rec["grid_mult"]
+    assert s2.tuned is not None and s2.config == rec["config"]
     s2.load(Xs, eps, 1e-6).factor()
     X = s2.solve(Bs)
     rel = s2.relres(Bs, X).cpu().numpy()
@@ -222,3 +223,46 @@ def test_c2_family_reaches_the_fp64_floor_with_four_rhs():
     rel = np.max(np.linalg.norm(B - A @ X, axis=0) / np.linalg.norm(B, axis=0))
     assert rel <= 10 * rel_ref, (rel, rel_ref)
     assert np.linalg.norm(X - x_ref) / np.linalg.norm(x_ref) < 1e-3
+
+
+@pytest.mark.parametrize("arith", ["df32", "f64"])
+def test_task_graph_step_is_bit_identical_to_level_schedule(arith):
+    """The persistent task-graph step (one launch: assembly, Cholesky, solve and
+    two FP64 refinements of every system) runs each tile task with the
+    arithmetic and the update order of the level-scheduled launches, so X is
+    bit-identical; and it reaches the FP64 Cholesky oracle's floor."""
+    from mpdok_gb300.batch import BatchedRBFSolver, unpack_rhs
+    sizes = [700, 129, 64, 300, 5, 1000, 77]
+    Xs, eps, Bs = _batch(sizes, 2, 3, seed=21)
+    s = BatchedRBFSolver(sizes, dim=2, nrhs=3, arith=arith, grid_mult=2)
+    s.load(Xs, eps, 1e-8)
+    X_lev = s.step(Bs, refine=2).clone()
+    for ctas in (1, 3):
+        s.configure(f"dag:{ctas}")
+        X_dag = s.step(Bs, refine=2)
+        torch.cuda.synchronize()
+        s.dag_status()
+        assert torch.equal(X_dag, X_lev), ctas
+    for i, (Xc, B, xg) in enumerate(zip(Xs, Bs, unpack_rhs(X_dag, sizes, 3))):
+        _, rel_ref = R.solve(Xc, eps[i], 1e-8, B)
+        A = R.rbf(Xc, eps[i], 1e-8)
+        rel = np.max(np.linalg.norm(B - A @ xg.cpu().numpy(), axis=0) / np.linalg.norm(B, axis=0))
+        assert rel <= 10 * rel_ref + 1e-14, (i, rel, rel_ref)
+
+
+def test_task_graph_is_one_kernel_in_the_captured_graph():
+    from mpdok_gb300.batch import BatchedRBFSolver
+    sizes = [300, 129, 64, 700, 5]
+    Xs, eps, Bs = _batch(sizes, 2, 4, seed=9)
+    s = BatchedRBFSolver(sizes, dim=2, nrhs=4, grid_mult=1)
+    s.load(Xs, eps, 1e-6)
+    X_ref = s.step(Bs, refine=2).clone()
+    s.configure("dag:3")
+    Bbuf, Xbuf = s.build_graph(Bs, refine=2)
+    assert s.graph_nodes <= 4  # the state resets (memsets) and ONE kernel node
+    for _ in range(2):
+        Xbuf.zero_()
+        s.run_graph()
+        torch.cuda.synchronize()
+        s.dag_status()
+        assert torch.equal(Xbuf, X_ref)
