@@ -228,11 +228,13 @@ MPDOK_API int mpdok_mf_cg_ir(const double* coords, long long n, int dim, int ker
  * a batch plan (below) of one system of size n with nrhs equal to this
  * solve's nrhs, loaded and factored (mpdok_batch_factor).  For SPD systems
  * too ill-conditioned for any FP32 CG body (kappa * 6e-8 > 1, the C2
- * family), the preconditioned FP32 CG converges in a few steps and the FP64
- * refinement reaches the FP64 floor.  mode 0: FP32 copy of A64 in opbuf
- * (mpdok_cg_ir_operator_size(n, 0)) + native FP64 residual; 1: split A64
- * (mpdok_cg_ir_operator_size(n, 1)) for the FP32 products and the residual;
- * 2: matrix-free from coords (dim, kernel, gamma, reg; A64 / opbuf unused).
+ * family) the inner PCG keeps FP64 vectors (an FP32 correction would move the
+ * residual by up to kappa * 6e-8), converges in a few steps and the FP64
+ * refinement reaches the FP64 floor.  mode 0: stored FP64 A64 (opbuf
+ * unused); 1: split A64 (two FP32 slices in opbuf,
+ * mpdok_cg_ir_operator_size(n, 1); error-free FP32 products, FP64-level
+ * accuracy on the FP32 pipe); 2: matrix-free from coords (dim, kernel, gamma,
+ * reg; A64 / opbuf unused).
  * The reference's cg (dense_krylov.py:119-205) with its FP64 residual check,
  * made convergent on this family by the preconditioner. */
 MPDOK_API size_t mpdok_chol_cg_ir_workspace_size(long long n, int nrhs, int mode);

@@ -1371,6 +1371,14 @@ static int bpc_apply_cols(void* ctx, const float* v, float* z, int K, long long 
   return MPDOK_OK;
 }
 
+int batch_apply_f64(void* plan, long long n, int K, double* V, cudaStream_t s) {
+  MPDOK_ARG_CHECK(plan && V, "null pointer");
+  BatchPlan* p = (BatchPlan*)plan;
+  MPDOK_ARG_CHECK(p->nsys == 1 && p->sys[0].n == n, "the preconditioner plan must hold one system of size n");
+  MPDOK_ARG_CHECK(p->nrhs == K, "the preconditioner plan's nrhs must equal the solve's nrhs");
+  return batch_solve_inplace(p, V, s);
+}
+
 int batch_precond(void* plan, long long n, int K, double* tmp, BatchPcCtx* ctx, Precond* pc) {
   MPDOK_ARG_CHECK(plan && tmp && ctx && pc, "null pointer");
   BatchPlan* p = (BatchPlan*)plan;

@@ -99,6 +99,9 @@ struct BatchPcCtx {
   long long n = 0;
 };
 int batch_precond(void* plan, long long n, int K, double* tmp, BatchPcCtx* ctx, Precond* pc);
+// V := A^-1 V in FP64 with the Cholesky factor of a batch plan of one system
+// (V: n x K column-major, ld n, K = the plan's nrhs).  Defined in batch.cu.
+int batch_apply_f64(void* plan, long long n, int K, double* V, cudaStream_t s);
 
 // One Arnoldi cycle (up to m steps) on the FP32 operator A32 with the
 // unnormalised start vector already in V[:,0] and ws.sc->nrm2 = ||V[:,0]||^2

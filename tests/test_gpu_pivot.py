@@ -52,7 +52,7 @@ def test_factor_matches_lapack_getrf(n, kind):
     # candidates' exact (FP64) Schur-complement magnitudes agree to FP32 rounding
     diff = np.nonzero(ipiv != piv_ref)[0]
     if diff.size == 0:
-        assert np.linalg.norm(LU - lu_ref) / np.linalg.norm(lu_ref) < 1e-5
+        assert np.linalg.norm(LU - lu_ref) / np.linalg.norm(lu_ref) < 1e-4
         return
     d = int(diff[0])
     Wd = W.copy()
