@@ -231,10 +231,10 @@ MPDOK_API int mpdok_mf_cg_ir(const double* coords, long long n, int dim, int ker
  * family) the inner PCG keeps FP64 vectors (an FP32 correction would move the
  * residual by up to kappa * 6e-8), converges in a few steps and the FP64
  * refinement reaches the FP64 floor.  mode 0: stored FP64 A64 (opbuf
- * unused); 1: split A64 (two FP32 slices in opbuf,
- * mpdok_cg_ir_operator_size(n, 1); error-free FP32 products, FP64-level
- * accuracy on the FP32 pipe); 2: matrix-free from coords (dim, kernel, gamma,
- * reg; A64 / opbuf unused).
+ * unused); 1: the inner products from split A64 (two FP32 slices in opbuf,
+ * mpdok_cg_ir_operator_size(n, 1); error-free FP32 products, about 2^-48 on
+ * the FP32 pipe), the FP64 residual from A64; 2: matrix-free from coords
+ * (dim, kernel, gamma, reg; A64 / opbuf unused).
  * The reference's cg (dense_krylov.py:119-205) with its FP64 residual check,
  * made convergent on this family by the preconditioner. */
 MPDOK_API size_t mpdok_chol_cg_ir_workspace_size(long long n, int nrhs, int mode);

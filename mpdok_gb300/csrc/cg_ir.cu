@@ -137,10 +137,11 @@ extern "C" int mpdok_mf_cg_ir(const double* coords, long long n, int dim, int ke
 // inner recurrence keeps its vectors in FP64, because a correction rounded to
 // FP32 changes the residual by up to kappa * 6e-8 relative, more than it
 // removes.  The products come from the operator of `mode`: 0 the stored FP64
-// matrix (FP64 pipe), 1 the split matrix (two FP32 slices, error-free FP32
-// products and double-float sums: FP64-level accuracy on the FP32 pipe, the
-// Ozaki-style split matvec), 2 matrix-free (FP64 evaluate-and-multiply from
-// the coordinates).  Every column runs its own PCG; the host reads the K dot
+// matrix (FP64 pipe), 1 the split matrix for the inner products (two FP32
+// slices, error-free FP32 products and double-float sums: about 2^-48 on the
+// FP32 pipe, the Ozaki-style split matvec) with the outer residual from the
+// FP64 matrix, 2 matrix-free (FP64 evaluate-and-multiply from the
+// coordinates).  Every column runs its own PCG; the host reads the K dot
 // products per step.
 namespace mpdok {
 
@@ -228,7 +229,7 @@ static CholPcgWs chol_layout(long long n, int K, void* base) {
 
 static size_t chol_op_bytes(long long n, int K, int mode) {
   if (mode == 0) return gemv_workspace_bytes(MPDOK_F64, n, n, K, false);
-  if (mode == 1) return split_gemv_work_bytes(n, n, K);
+  if (mode == 1) return align_up(gemv_workspace_bytes(MPDOK_F64, n, n, K, false), 256) + split_gemv_work_bytes(n, n, K);
   return matfree_work_bytes(n, n, K, MPDOK_F64);
 }
 
@@ -249,7 +250,8 @@ static int set_coef(const CholPcgWs& w, const double* host, int K, cudaStream_t 
   return MPDOK_OK;
 }
 
-static int chol_pcg_ir_core(void* plan, const Residual64& R, long long n, int K, const double* B, long long ldb,
+static int chol_pcg_ir_core(void* plan, const Residual64& R, const Residual64& Ain, long long n, int K,
+                            const double* B, long long ldb,
                             double* Xout, long long ldx, double tol, int maxiter_outer, double inner_tol,
                             int inner_maxiter, const CholPcgWs& w, mpdok_solve_info* info, cudaStream_t s) {
   const unsigned g = (unsigned)std::max(1LL, std::min<long long>((n * K + 255) / 256, (long long)num_sms() * 8));
@@ -288,8 +290,8 @@ static int chol_pcg_ir_core(void* plan, const Residual64& R, long long n, int K,
     std::vector<double> r0(rn);
     std::vector<char> live(K, 1);
     for (int it = 0; it < inner_maxiter; ++it) {
-      // q = -(A p): the residual operator with a zero right-hand side
-      MPDOK_TRY(R.apply(R.ctx, w.zero, w.p, w.q, w.parts, K, n, s));
+      // q = -(A p): the inner operator with a zero right-hand side
+      MPDOK_TRY(Ain.apply(Ain.ctx, w.zero, w.p, w.q, w.parts, K, n, s));
       MPDOK_TRY(cdots(w, w.p, w.q, n, K, pq.data(), s));
       for (int c = 0; c < K; ++c) cf[c] = (live[c] && pq[c] != 0.0) ? -rz[c] / pq[c] : 0.0;  // alpha = rz / (p.Ap)
       MPDOK_TRY(set_coef(w, cf.data(), K, s));
@@ -362,23 +364,34 @@ extern "C" int mpdok_chol_cg_ir(void* plan, const double* A64, long long lda, co
     c.n = n;
     c.gw = gw;
     c.gbytes = gbytes;
-    return chol_pcg_ir_core(plan, stored_res64(&c), n, nrhs, B, ldb, X, ldx, tol, maxiter_outer, inner_tol,
-                            inner_maxiter, w, info, s);
+    const Residual64 R = stored_res64(&c);
+    return chol_pcg_ir_core(plan, R, R, n, nrhs, B, ldb, X, ldx, tol, maxiter_outer, inner_tol, inner_maxiter, w,
+                            info, s);
   }
   if (mode == 1) {
     const long long ld = (long long)align_up((size_t)n, 4);
     float* hi = (float*)opbuf;
     float* lo = (float*)((char*)opbuf + align_up((size_t)ld * n * sizeof(float), 256));
     if (!op_ready) MPDOK_TRY(split_matrix(A64, lda, n, n, hi, lo, ld, s));
+    // the inner products come from the split slices (FP32 pipe, 2^-48 products), the outer
+    // residual from the FP64 matrix: the split form represents A to about 2^-48, which would
+    // hold the attainable relres some 30x above the FP64 floor
+    const size_t gb = gemv_workspace_bytes(MPDOK_F64, n, n, nrhs, false);
+    StoredCtx r;
+    r.A64 = A64;
+    r.lda64 = lda;
+    r.n = n;
+    r.gw = gw;
+    r.gbytes = gb;
     SplitCtx c;
     c.hi = hi;
     c.lo = lo;
     c.ld = ld;
     c.n = n;
-    c.work = gw;
-    c.work_bytes = gbytes;
-    return chol_pcg_ir_core(plan, split_res64(&c), n, nrhs, B, ldb, X, ldx, tol, maxiter_outer, inner_tol,
-                            inner_maxiter, w, info, s);
+    c.work = gw + align_up(gb, 256);
+    c.work_bytes = gbytes - align_up(gb, 256);
+    return chol_pcg_ir_core(plan, stored_res64(&r), split_res64(&c), n, nrhs, B, ldb, X, ldx, tol, maxiter_outer,
+                            inner_tol, inner_maxiter, w, info, s);
   }
   MfCtx c;
   c.op.rows = coords;
@@ -391,6 +404,7 @@ extern "C" int mpdok_chol_cg_ir(void* plan, const double* A64, long long lda, co
   c.op.reg = reg;
   c.w64 = gw;
   c.w64_bytes = gbytes;
-  return chol_pcg_ir_core(plan, mf_res64(&c), n, nrhs, B, ldb, X, ldx, tol, maxiter_outer, inner_tol, inner_maxiter,
-                          w, info, s);
+  const Residual64 R = mf_res64(&c);
+  return chol_pcg_ir_core(plan, R, R, n, nrhs, B, ldb, X, ldx, tol, maxiter_outer, inner_tol, inner_maxiter, w, info,
+                          s);
 }
