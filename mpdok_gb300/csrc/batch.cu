@@ -738,7 +738,7 @@ __global__ void __launch_bounds__(BT) k_badj_reduce(const BSys* __restrict__ sys
 // Reads of data other tasks wrote bypass L1 (ld.global.cg); the arithmetic of
 // every task is that of the level-scheduled kernels.
 enum BTaskKind : int { BT_COPY = 0, BT_ASM, BT_POTRF, BT_TRSM, BT_SYRK, BT_RES, BT_DIAGF, BT_UPDF, BT_DIAGB, BT_UPDB,
-                       BT_ADD };
+                       BT_ADD, BT_SYRKC, BT_SYRKR };
 
 struct DagSec {         // one contiguous run of tasks of one kind
   long long begin;      // first global task index
@@ -804,6 +804,26 @@ __device__ __forceinline__ void stage_block_cg(T* sT, const double* __restrict__
 
 __device__ __forceinline__ int tri_idx(int i, int j) { return i * (i + 1) / 2 + j; }
 
+// Tiles (ti, tj), tj <= ti, of a level-k trailing-update task u.  BT_SYRK: all
+// lower tiles right of the panel in triangular order; BT_SYRKC: the next
+// panel column tj = k + 1 only; BT_SYRKR: the rest (tj >= k + 2).  The split
+// lets the queue put the next column's updates, and the next panel's factor
+// and solve, ahead of the bulk of the level (a look-ahead of one panel).
+__device__ __forceinline__ void syrk_tiles(int kind, int k, long long u, int& ti, int& tj) {
+  if (kind == BT_SYRKC) {
+    ti = k + 1 + (int)u;
+    tj = k + 1;
+    return;
+  }
+  int a = (int)((sqrt(8.0 * (double)u + 1.0) - 1.0) * 0.5);
+  while ((long long)(a + 1) * (a + 2) / 2 <= u) ++a;
+  while ((long long)a * (a + 1) / 2 > u) --a;
+  const int b = (int)(u - (long long)a * (a + 1) / 2);
+  const int sh = kind == BT_SYRKR ? 2 : 1;
+  ti = k + sh + a;
+  tj = k + sh + b;
+}
+
 template <int KIND, int D, int ARITH>
 __global__ void __launch_bounds__(BT) k_bstep_dag(const BSys* __restrict__ sys, const long long* __restrict__ pre,
                                                   const DagSec* __restrict__ secs, int nsec, long long total,
@@ -853,16 +873,13 @@ __global__ void __launch_bounds__(BT) k_bstep_dag(const BSys* __restrict__ sys, 
           ti = k + 1 + (int)u;
           ok = dag_wait(st + tri_idx(k, k), k + 1, S.err) && dag_wait(st + tri_idx(ti, k), k, S.err);
           break;
-        case BT_SYRK: {
-          int a = (int)((sqrt(8.0 * (double)u + 1.0) - 1.0) * 0.5);
-          while ((long long)(a + 1) * (a + 2) / 2 <= u) ++a;
-          while ((long long)a * (a + 1) / 2 > u) --a;
-          ti = k + 1 + a;
-          tj = k + 1 + (int)(u - (long long)a * (a + 1) / 2);
+        case BT_SYRK:
+        case BT_SYRKC:
+        case BT_SYRKR:
+          syrk_tiles(sec.kind, k, u, ti, tj);
           ok = dag_wait(st + tri_idx(ti, k), k + 1, S.err) && dag_wait(st + tri_idx(tj, k), k + 1, S.err) &&
                dag_wait(st + tri_idx(ti, tj), k, S.err);
           break;
-        }
         case BT_RES:
           ok = dag_wait(S.done + (long long)(f - 1) * nsys + s, nblk, S.err) &&
                dag_wait(S.asm_done + s, nblk * nblk, S.err);
@@ -888,12 +905,8 @@ __global__ void __launch_bounds__(BT) k_bstep_dag(const BSys* __restrict__ sys, 
     if (!s_ok) return;
     if (sec.kind == BT_TRSM || sec.kind == BT_UPDF || sec.kind == BT_UPDB || sec.kind == BT_ADD) {
       ti = (sec.kind == BT_TRSM || sec.kind == BT_UPDF) ? k + 1 + (int)u : (int)u;
-    } else if (sec.kind == BT_SYRK) {
-      int a = (int)((sqrt(8.0 * (double)u + 1.0) - 1.0) * 0.5);
-      while ((long long)(a + 1) * (a + 2) / 2 <= u) ++a;
-      while ((long long)a * (a + 1) / 2 > u) --a;
-      ti = k + 1 + a;
-      tj = k + 1 + (int)(u - (long long)a * (a + 1) / 2);
+    } else if (sec.kind == BT_SYRK || sec.kind == BT_SYRKC || sec.kind == BT_SYRKR) {
+      syrk_tiles(sec.kind, k, u, ti, tj);
     }
     // ---- the task
     int* pub = nullptr;  // state word set to pub_val when the task is done
@@ -1031,7 +1044,9 @@ __global__ void __launch_bounds__(BT) k_bstep_dag(const BSys* __restrict__ sys, 
         pub_val = k + 1;
         break;
       }
-      case BT_SYRK: {
+      case BT_SYRK:
+      case BT_SYRKC:
+      case BT_SYRKR: {
         using STT = typename std::conditional<ARITH == 0, double, DF>::type;
         STT* sA = reinterpret_cast<STT*>(smem);
         STT* sB = sA + BNB * BPAD;
@@ -1436,13 +1451,21 @@ static int dag_prepare(BatchPlan* p, int refine) {
   const auto rows = prefix_of(ns, [&](int i) { return (long long)p->sys[i].nblk; });
   add_sec(BT_COPY, 0, 0, ns, rows);
   add_sec(BT_ASM, 0, 0, ns, prefix_of(ns, [&](int i) { return (long long)p->sys[i].nblk * p->sys[i].nblk; }));
-  for (int k = 0; k < p->maxblk; ++k) {
+  // factor, with a look-ahead of one panel in the queue order:
+  //   POTRF(0) TRSM(0) | per k: SYRK(k, column k+1) POTRF(k+1) TRSM(k+1) SYRK(k, columns >= k+2)
+  auto panel = [&](int k) {
     const int cnt = p->act[k];
     add_sec(BT_POTRF, k, 0, cnt, prefix_of(cnt, [](int) { return 1LL; }));
     add_sec(BT_TRSM, k, 0, cnt, prefix_of(cnt, [&](int i) { return (long long)(p->sys[i].nblk - k - 1); }));
-    add_sec(BT_SYRK, k, 0, cnt, prefix_of(cnt, [&](int i) {
-      const long long T = p->sys[i].nblk - k - 1;
-      return T * (T + 1) / 2;
+  };
+  panel(0);
+  for (int k = 0; k < p->maxblk; ++k) {
+    const int cnt = p->act[k];
+    add_sec(BT_SYRKC, k, 0, cnt, prefix_of(cnt, [&](int i) { return (long long)(p->sys[i].nblk - k - 1); }));
+    if (k + 1 < p->maxblk) panel(k + 1);
+    add_sec(BT_SYRKR, k, 0, cnt, prefix_of(cnt, [&](int i) {
+      const long long T = p->sys[i].nblk - k - 2;
+      return T > 0 ? T * (T + 1) / 2 : 0LL;
     }));
   }
   for (int f = 0; f <= refine; ++f) {
