@@ -1054,7 +1054,7 @@ def main():
         del hb, db, A_host
         e2e = {"value": sum(times) / len(times), "unit": UNIT, "h2d_bytes_per_step": 8 * n * n + 8 * n,
                "d2h_bytes_per_step": 8 * n, "api": "mpdok_gb300.solvers.MixedSolver.solve(host A, host b)",
-               "breakdown_ms": parts[-1] if parts else None,
+               "steps_seconds": times, "breakdown_ms": parts,
                "upload_seconds": up_s, "upload_GBs": 8.0 * n * n / up_s / 1e9, "pinned_h2d_GBs": link,
                "upload_frac_of_pinned_copy": 8.0 * n * n / up_s / 1e9 / link}
 

@@ -260,210 +260,219 @@ __device__ __forceinline__ void inverse_doubling(const float* T, float* XL, floa
 //   [X11 0; L21 X22]^-1 off-diagonal block = -X22 L21 X11,
 //   [X11 U12; 0 X22]^-1 off-diagonal block = -X11 U12 X22,
 // for block sizes 32 and 64, each product spread over all 256 threads.
+// The 32 x 32 diagonal blocks of L^-1 (unit lower) and U^-1 from the factored
+// block T (shared memory, pitch DP): warps 0-3 invert L's four blocks, warps
+// 4-7 U's, each with its column j in lane j's registers (fully unrolled
+// substitution; the block's rows are shared-memory broadcasts).  The terms
+// outside a column's triangle are exact zeros, so every entry gets the same
+// operations in the same order as a column-by-column substitution.  Entry
+// (r, c) of an inverse goes to dst[r * rs + c * cs].
+__device__ __forceinline__ void diag32_inverses(const float* T, float* XL, float* XU, int rs, int cs) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = warp & 3;
+  const int o = b * 32;
+  const float* Tb = T + o * DP + o;
+  if (warp >= 8) {
+    // idle during the 32 x 32 substitutions
+  } else if (warp < 4) {
+    float x[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      float acc = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+      for (int k = 0; k < i; ++k) acc = fmaf(-Tb[i * DP + k], x[k], acc);
+      x[i] = (i < lane) ? 0.f : acc;
+    }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) XL[(o + i) * rs + (o + lane) * cs] = x[i];
+  } else {
+    float x[32];
+#pragma unroll
+    for (int i = 31; i >= 0; --i) {
+      float acc = 0.f;
+#pragma unroll
+      for (int k = i + 1; k < 32; ++k) acc = fmaf(Tb[i * DP + k], x[k], acc);
+      const float d = Tb[i * DP + i];
+      x[i] = (i > lane) ? 0.f : (i == lane ? 1.f / d : -acc / d);
+    }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) XU[(o + i) * rs + (o + lane) * cs] = x[i];
+  }
+}
+
+// Inverses by recursive doubling: the 32 x 32 diagonal blocks by substitution,
+// then
+//   [X11 0; L21 X22]^-1 off-diagonal block = -X22 L21 X11,
+//   [X11 U12; 0 X22]^-1 off-diagonal block = -X11 U12 X22,
+// for block sizes 32 and 64, each product spread over all 1024 threads.
 __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x;
   for (int idx = tid; idx < LNB * DP; idx += blockDim.x) { XL[idx] = 0.f; XU[idx] = 0.f; }
   __syncthreads();
-  {
-    // Each 32 x 32 diagonal block is inverted by one warp with its column j in
-    // lane j's registers (fully unrolled substitution; the block's rows are
-    // shared-memory broadcasts).  The terms outside a column's triangle are
-    // exact zeros, so every entry gets the same operations in the same order
-    // as a column-by-column substitution.
-    const int b = warp & 3;
-    const int o = b * 32;
-    const float* Tb = T + o * DP + o;
-    if (warp >= 8) {
-      // idle during the 32 x 32 substitutions
-    } else if (warp < 4) {
-      float x[32];
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        float acc = (i == lane) ? 1.f : 0.f;
-#pragma unroll
-        for (int k = 0; k < i; ++k) acc = fmaf(-Tb[i * DP + k], x[k], acc);
-        x[i] = (i < lane) ? 0.f : acc;
-      }
-#pragma unroll
-      for (int i = 0; i < 32; ++i) XL[(o + i) * DP + o + lane] = x[i];
-    } else {
-      float x[32];
-#pragma unroll
-      for (int i = 31; i >= 0; --i) {
-        float acc = 0.f;
-#pragma unroll
-        for (int k = i + 1; k < 32; ++k) acc = fmaf(Tb[i * DP + k], x[k], acc);
-        const float d = Tb[i * DP + i];
-        x[i] = (i > lane) ? 0.f : (i == lane ? 1.f / d : -acc / d);
-      }
-#pragma unroll
-      for (int i = 0; i < 32; ++i) XU[(o + i) * DP + o + lane] = x[i];
-    }
-  }
+  diag32_inverses(T, XL, XU, DP, 1);
   __syncthreads();
   inverse_doubling<32>(T, XL, XU, Tmp);
   inverse_doubling<64>(T, XL, XU, Tmp);
 }
 
 
-// Blocked LU of the 128 x 128 diagonal block in four 32-column sub-panels.
-// The kernel is issue-bound on its single SM, so the work is arranged for
-// few instructions per flop:
-//   A  the sub-panel (rows >= c0, 32 columns) is factored by 4 warps; thread
-//      r keeps row r of it in registers, the pivot row goes through shared
-//      memory (double-buffered) with one 128-thread barrier per column;
-//   B  U12 = L11^-1 A12 by column-parallel forward substitution (one thread
-//      per trailing column, the column in registers);
-//   C  A22 -= L21 U12 (K = 32) by all 1024 threads.
-// Elimination step K of a 32 x 32 block held one row per lane (the warp's
-// rows in registers): the pivot row is read by shuffle from lane K, a pivot
-// below tau in magnitude is replaced by +-tau (counted), and steps K >=
-// active are skipped.  Recursion over K keeps every register index static.
-template <int K>
-__device__ __forceinline__ void top_block_step(float (&row)[32], int lane, int active, float tau, int* nperturb) {
-  if (K < active) {  // uniform across the warp
-    if (lane == K && !(fabsf(row[K]) >= tau)) {
-      row[K] = (row[K] < 0.f) ? -tau : tau;
-      atomicAdd(nperturb, 1);
-    }
-    const float pinv = __frcp_rn(__shfl_sync(0xffffffffu, row[K], K));
-    const float l = row[K] * pinv;  // within 1.5 ulp of row[K] / pivot
-#pragma unroll
-    for (int c = K + 1; c < 32; ++c) {
-      const float u = __shfl_sync(0xffffffffu, row[c], K);
-      if (lane > K) row[c] = fmaf(-l, u, row[c]);
-    }
-    if (lane > K) row[K] = l;
-  }
-  if constexpr (K + 1 < 32) top_block_step<K + 1>(row, lane, active, tau, nperturb);
-}
+// Unpivoted LU of the 128 x 128 diagonal block, held in registers: thread
+// (r = tid % 128, g = tid / 128) keeps row r, columns [16 g, 16 g + 16).
+// Elimination step k reads the pivot row k and the column k; both are final
+// after step k - 1, so their owners publish them into double-buffered shared
+// rows right after their own step k - 1 update, and a step costs one barrier.
+// Every thread forms the pivot's reciprocal and its row's multiplier itself:
+//   u_kk <- +-tau when |u_kk| < tau (counted once),
+//   l_r = a_rk * rcp_rn(u_kk),   a_rj <- fma(-l_r, u_kj, a_rj)  (j > k),
+// the operations and order of a step-by-step elimination.  The kernel then
+// writes L\U into the factor and back into W's diagonal block (FP32, for the
+// panel solves and the inverses), and the inverses of its 32 x 32 diagonal
+// blocks of L and U into the diagonal positions of Linv / Uinv; the panel
+// solves need only those, and k_tri_inv_complete fills in the rest of the
+// 128 x 128 inverses once the factorization is done.
+constexpr size_t DIAG_RR_SMEM = (size_t)(LNB * DP + 4 * LNB) * sizeof(float);
 
 template <typename F>
 __global__ void __launch_bounds__(DIAG_THREADS, 1)
 k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __restrict__ LU, long long ldf,
           float* __restrict__ Linv, float* __restrict__ Uinv, int* nperturb, float tau) {
   extern __shared__ float sm[];
+  float* T = sm;                      // [128][DP]: the factored block, for the 32 x 32 inverses
+  float* prow = sm + LNB * DP;        // [2][128]: pivot row k
+  float* pcol = prow + 2 * LNB;       // [2][128]: column k before division
+  static_assert((LNB * DP) % 4 == 0, "the pivot rows must be 16-byte aligned");
+  const int tid = threadIdx.x, r = tid & (LNB - 1), g = tid >> 7;
+  float a[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int c = 16 * g + i;
+    a[i] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
+  }
+  // the inputs of step 0
+  if (r == 0) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) prow[16 * g + i] = a[i];
+  }
+  if (g == 0) pcol[r] = a[0];
+  __syncthreads();
+  for (int gk = 0; 16 * gk < nbk; ++gk) {
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      const int k = 16 * gk + kk;
+      if (k >= nbk) break;  // uniform
+      const float* pr = prow + (k & 1) * LNB;
+      const float* pc = pcol + (k & 1) * LNB;
+      float piv = pr[k];
+      const bool small = !(fabsf(piv) >= tau);
+      if (small) piv = (piv < 0.f) ? -tau : tau;
+      const float pinv = __frcp_rn(piv);
+      if (small && r == k && g == gk) {
+        a[kk] = piv;
+        atomicAdd(nperturb, 1);
+      }
+      if (r > k && g >= gk) {
+        const float l = pc[r] * pinv;
+        float u[16];
+#pragma unroll
+        for (int i = 0; i < 16; i += 4) {
+          const float4 v = *reinterpret_cast<const float4*>(pr + 16 * g + i);
+          u[i] = v.x; u[i + 1] = v.y; u[i + 2] = v.z; u[i + 3] = v.w;
+        }
+        if (g == gk) {
+          a[kk] = l;
+#pragma unroll
+          for (int i = kk + 1; i < 16; ++i) a[i] = fmaf(-l, u[i], a[i]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) a[i] = fmaf(-l, u[i], a[i]);
+        }
+      }
+      // publish the inputs of step k + 1 (row k + 1 and column k + 1)
+      const int k1 = k + 1;
+      if (k1 < nbk) {
+        float* nr = prow + (k1 & 1) * LNB;
+        float* nc = pcol + (k1 & 1) * LNB;
+        if (r == k1) {
+#pragma unroll
+          for (int i = 0; i < 16; i += 4)
+            *reinterpret_cast<float4*>(nr + 16 * g + i) = make_float4(a[i], a[i + 1], a[i + 2], a[i + 3]);
+        }
+        const int c1 = (kk + 1) & 15;  // column k + 1 within its group
+        const int g1 = gk + (kk == 15 ? 1 : 0);
+        if (g == g1 && r >= k1) nc[r] = a[c1];
+      }
+      __syncthreads();
+    }
+  }
+  // L\U out: the factor (F), W's diagonal block (FP32) and shared memory
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int c = 16 * g + i;
+    T[r * DP + c] = a[i];
+    if (r < nbk && c < nbk) {
+      LU[(j0 + r) + (j0 + c) * ldf] = from_f32<F>(a[i]);
+      W[(j0 + r) + (j0 + c) * ldw] = a[i];
+    }
+  }
+  __syncthreads();
+  diag32_inverses(T, Linv, Uinv, 1, LNB);
+}
+
+// The full 128 x 128 inverses of every diagonal block (for the triangular
+// solves of the preconditioner) from W's factored diagonal blocks and the
+// 32 x 32 diagonal-block inverses that k_lu_diag left in Linv / Uinv: the
+// doubling steps of tri_inverses, one CTA per block.
+__global__ void __launch_bounds__(DIAG_THREADS, 1)
+k_tri_inv_complete(const float* __restrict__ W, long long ldw, long long n, float* __restrict__ Linv,
+                   float* __restrict__ Uinv) {
+  extern __shared__ float sm[];
   float* T = sm;
   float* XL = sm + LNB * DP;
   float* XU = sm + 2 * LNB * DP;
   float* Tmp = sm + 3 * LNB * DP;
-  // phase A's copy of the top block's U rows (pitch UBP, 16-byte aligned) and
-  // pivot reciprocals (row 32), in Tmp, which is free until the inverses
-  constexpr int UBP = 36;
-  float* Ub = Tmp;
-  static_assert(33 * UBP <= 64 * 65, "the U copy must fit in Tmp");
-  static_assert((3 * LNB * DP) % 4 == 0, "Tmp must be 16-byte aligned");
   const int tid = threadIdx.x;
+  const long long j0 = (long long)blockIdx.x * LNB;
+  const int nbk = (int)min((long long)LNB, n - j0);
+  float* Li = Linv + (long long)blockIdx.x * LNB * LNB;
+  float* Ui = Uinv + (long long)blockIdx.x * LNB * LNB;
   for (int idx = tid; idx < LNB * LNB; idx += DIAG_THREADS) {
     const int r = idx % LNB, c = idx / LNB;
     T[r * DP + c] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
+    const bool diag = (r >> 5) == (c >> 5);
+    XL[r * DP + c] = diag ? Li[c * LNB + r] : 0.f;
+    XU[r * DP + c] = diag ? Ui[c * LNB + r] : 0.f;
   }
   __syncthreads();
-  for (int c0 = 0; c0 < nbk; c0 += 32) {
-    // ---- A: sub-panel columns [c0, c0 + 32), rows [c0, 128).  The 32 x 32
-    // top block lives in warp c0 / 32, one row per lane, and is factored
-    // warp-synchronously (pivot rows by shuffle).  The rows below then take
-    // eight threads each (four columns per thread, warps 4 and up) and apply
-    // the block's U rows from an aligned copy.  Every entry sees the same
-    // operations in the same order as a step-by-step elimination.
-    if ((tid >> 5) == (c0 >> 5)) {
-      const int r = tid, lane = tid & 31;
-      float row[32];
-#pragma unroll
-      for (int c = 0; c < 32; ++c) row[c] = T[r * DP + c0 + c];
-      top_block_step<0>(row, lane, nbk - c0, tau, nperturb);
-#pragma unroll
-      for (int c = 0; c < 32; ++c) T[r * DP + c0 + c] = row[c];
-      // U rows again at a 16-byte-aligned pitch, and the pivot reciprocals
-#pragma unroll
-      for (int c = 0; c < 32; c += 4)
-        *reinterpret_cast<float4*>(Ub + lane * UBP + c) = make_float4(row[c], row[c + 1], row[c + 2], row[c + 3]);
-      Ub[32 * UBP + lane] = __frcp_rn(T[r * DP + c0 + lane]);  // the pivot, as the steps above used it
-    }
-    __syncthreads();
-    {
-      const int u = tid - LNB;  // whole warps: the rows below come in multiples of four
-      const int r = c0 + 32 + (u >> 3), g = u & 7;
-      if (u >= 0 && r < LNB) {
-        float v[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) v[i] = T[r * DP + c0 + 4 * g + i];
-        const int src = (tid & 31) & ~7;  // lane of this row's columns 0..3
-#pragma unroll
-        for (int k = 0; k < 32; ++k) {
-          if (c0 + k < nbk) {  // uniform
-            const float l = __shfl_sync(0xffffffffu, v[k & 3], src | (k >> 2)) * Ub[32 * UBP + k];
-            if (g == (k >> 2)) v[k & 3] = l;
-            const float4 uu = *reinterpret_cast<const float4*>(Ub + k * UBP + 4 * g);
-            if (4 * g + 0 > k) v[0] = fmaf(-l, uu.x, v[0]);
-            if (4 * g + 1 > k) v[1] = fmaf(-l, uu.y, v[1]);
-            if (4 * g + 2 > k) v[2] = fmaf(-l, uu.z, v[2]);
-            if (4 * g + 3 > k) v[3] = fmaf(-l, uu.w, v[3]);
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) T[r * DP + c0 + 4 * g + i] = v[i];
-      }
-    }
-    __syncthreads();
-    const int c1 = c0 + 32;
-    if (c1 >= LNB) break;
-    // ---- B: U12 = L11^-1 A12, rows [c0, c1), columns [c1, 128): one column per thread
-    if (tid < LNB - c1) {
-      const int c = c1 + tid;
-      float u[32];
-#pragma unroll
-      for (int i = 0; i < 32; ++i) u[i] = T[(c0 + i) * DP + c];
-#pragma unroll
-      for (int i = 1; i < 32; ++i) {
-        float acc = u[i];
-#pragma unroll
-        for (int k = 0; k < i; ++k) acc = fmaf(-T[(c0 + i) * DP + c0 + k], u[k], acc);
-        u[i] = acc;
-      }
-#pragma unroll
-      for (int i = 1; i < 32; ++i) T[(c0 + i) * DP + c] = u[i];
-    }
-    __syncthreads();
-    // ---- C: A22 -= L21 U12 over rows and columns [c1, 128), K = 32
-    const int m = LNB - c1;
-    for (int e = tid; e < m * m; e += blockDim.x) {
-      const int i = c1 + e / m, c = c1 + e % m;
-      float acc = T[i * DP + c];
-#pragma unroll
-      for (int k = 0; k < 32; ++k) acc = fmaf(-T[i * DP + c0 + k], T[(c0 + k) * DP + c], acc);
-      T[i * DP + c] = acc;
-    }
-    __syncthreads();
-  }
-  __syncthreads();
-  for (int idx = tid; idx < nbk * nbk; idx += blockDim.x) {
-    const int r = idx % nbk, c = idx / nbk;
-    LU[(j0 + r) + (j0 + c) * ldf] = from_f32<F>(T[r * DP + c]);
-  }
-  tri_inverses(T, XL, XU, Tmp);
-  for (int idx = tid; idx < LNB * LNB; idx += blockDim.x) {
+  inverse_doubling<32>(T, XL, XU, Tmp);
+  inverse_doubling<64>(T, XL, XU, Tmp);
+  for (int idx = tid; idx < LNB * LNB; idx += DIAG_THREADS) {
     const int r = idx % LNB, c = idx / LNB;
-    Linv[c * LNB + r] = XL[r * DP + c];
-    Uinv[c * LNB + r] = XU[r * DP + c];
+    Li[c * LNB + r] = XL[r * DP + c];
+    Ui[c * LNB + r] = XU[r * DP + c];
   }
 }
 
 // --------------------------------------------------------------- TRSMs
-// L21 = W21 * Uinv.  Block: RB rows x 128 columns; thread RB / 16 rows x 8 columns.
+// Both panel solves work block column by block column (block row by block
+// row) with the 32 x 32 diagonal-block inverses that k_lu_diag leaves in
+// Linv / Uinv and the off-diagonal blocks of the factored diagonal block in W:
+//   L21 = W21 U^-1:  X_b = (W_b - sum_{a<b} X_a U_ab) Uinv_bb,
+//   U12 = L^-1 W12:  Z_b = Linv_bb (W_b - sum_{a<b} L_ba Z_a),  b = 0..3.
+
+// L21 = W21 U^-1 for RB rows x 128 columns; thread: column j of the current
+// block column, rows tid / 32 + 8 u.
 template <typename F, int RB>
 __device__ __forceinline__ void trsm_right_body(const float* __restrict__ W, long long ldw, long long j0,
                                                 long long r_begin, long long n, const float* __restrict__ Uinv,
                                                 F* __restrict__ Lp, long long lp_pitch, long long lp_row0, int koff,
                                                 F* __restrict__ LU, long long ldf, int bid) {
   static_assert(RB % 16 == 0 && RB <= 64, "rows per block: a multiple of 16, at most 64");
-  constexpr int TR = RB / 16;     // rows per thread
+  constexpr int RU = RB / 8;      // rows per thread
   extern __shared__ float sm[];
   constexpr int XP = LNB + 1;     // odd pitch: the row-fastest staging writes hit distinct banks
-  constexpr int TSP = LNB + 4;    // keeps the float4 reads of Ts aligned; staging writes 4-way at most
-  static_assert((RB * XP) % 4 == 0, "Ts must be 16-byte aligned");
-  float* Xs = sm;                 // [RB][XP]   rows of W21 (then the output tile)
-  float* Ts = sm + RB * XP;       // [128][TSP] Uinv row-major [k][c]
+  constexpr int TSP = LNB + 4;
+  float* Xs = sm;                 // [RB][XP]   rows of W21, solved in place
+  float* Ts = sm + RB * XP;       // [128][TSP] U row-major [k][c], diagonal 32 x 32 blocks = their inverses
   const int tid = threadIdx.x;
   const long long r0 = r_begin + (long long)bid * RB;
   const int rows = (int)min((long long)RB, n - r0);
@@ -474,35 +483,44 @@ __device__ __forceinline__ void trsm_right_body(const float* __restrict__ W, lon
         return (r < rows) ? W[(r0 + r) + (j0 + c) * ldw] : 0.f;
       },
       [&](int idx, float v) { Xs[(idx % RB) * XP + idx / RB] = v; });
-  // Uinv column-major: [c*128 + k]
   stage_tile<LNB * LNB, TRSM_THREADS, 32>(
-      tid, [&](int idx) { return Uinv[idx]; }, [&](int idx, float v) { Ts[(idx % LNB) * TSP + idx / LNB] = v; });
+      tid,
+      [&](int idx) {
+        const int k = idx % LNB, c = idx / LNB;
+        if ((k >> 5) == (c >> 5)) return Uinv[idx];
+        return k < c ? W[(j0 + k) + (j0 + c) * ldw] : 0.f;
+      },
+      [&](int idx, float v) { Ts[(idx % LNB) * TSP + idx / LNB] = v; });
   __syncthreads();
-  const int ty = tid / 16, tx = tid % 16;
-  float acc[TR][8];
+  const int j = tid & 31, i0 = tid >> 5;
+  for (int cb = 0; cb < 4; ++cb) {
+    const int c = 32 * cb + j;
+    float y[RU];
 #pragma unroll
-  for (int i = 0; i < TR; ++i)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    for (int u = 0; u < RU; ++u) y[u] = Xs[(i0 + 8 * u) * XP + c];
 #pragma unroll 4
-  for (int k = 0; k < LNB; ++k) {
-    float a[TR], b[8];
+    for (int k = 0; k < 32 * cb; ++k) {
+      const float t = Ts[k * TSP + c];
 #pragma unroll
-    for (int i = 0; i < TR; ++i) a[i] = Xs[(ty * TR + i) * XP + k];
-    const float4 b0 = *reinterpret_cast<const float4*>(&Ts[k * TSP + tx * 8]);
-    const float4 b1 = *reinterpret_cast<const float4*>(&Ts[k * TSP + tx * 8 + 4]);
-    b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w; b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
+      for (int u = 0; u < RU; ++u) y[u] = fmaf(-Xs[(i0 + 8 * u) * XP + k], t, y[u]);
+    }
 #pragma unroll
-    for (int i = 0; i < TR; ++i)
+    for (int u = 0; u < RU; ++u) Xs[(i0 + 8 * u) * XP + c] = y[u];
+    __syncthreads();
+    float x[RU];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    for (int u = 0; u < RU; ++u) x[u] = 0.f;
+#pragma unroll 8
+    for (int m = 0; m < 32; ++m) {
+      const float t = Ts[(32 * cb + m) * TSP + c];
+#pragma unroll
+      for (int u = 0; u < RU; ++u) x[u] = fmaf(Xs[(i0 + 8 * u) * XP + 32 * cb + m], t, x[u]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < RU; ++u) Xs[(i0 + 8 * u) * XP + c] = x[u];
+    __syncthreads();
   }
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < TR; ++i)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) Xs[(ty * TR + i) * XP + tx * 8 + j] = acc[i][j];
-  __syncthreads();
   // K-major operand for the trailing GEMM: Lp[row][k]
   for (int idx = tid; idx < RB * LNB; idx += TRSM_THREADS) {
     const int r = idx / LNB, c = idx % LNB;
@@ -515,18 +533,20 @@ __device__ __forceinline__ void trsm_right_body(const float* __restrict__ W, lon
   }
 }
 
-// U12 = Linv * W12.  Block: 128 rows x RB columns; thread 8 rows x RB / 16 columns.
+// U12 = L^-1 W12 for 128 rows x RB columns; thread: column tid % RB, rows
+// tid / RB + (256 / RB) u of the current block row.
 template <typename F, int RB>
 __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long long ldw, long long j0,
                                                long long c_begin, long long n, const float* __restrict__ Linv,
                                                F* __restrict__ Up, long long up_pitch, long long up_col0, int koff,
                                                F* __restrict__ LU, long long ldf, int bid) {
   static_assert(RB % 16 == 0 && RB <= 64, "columns per block: a multiple of 16, at most 64");
-  constexpr int TC = RB / 16;       // columns per thread
+  constexpr int RS = TRSM_THREADS / RB;  // row stride between a thread's rows
+  constexpr int RU = 32 / RS;            // rows per thread in a block row
   extern __shared__ float sm[];
   constexpr int XP = RB + 4;
-  float* Xs = sm;                   // [128][XP]  W12 tile [k][c]
-  float* Ts = sm + LNB * XP;        // [128][LNB+1] Linv row-major [r][k]
+  float* Xs = sm;                   // [128][XP]  W12 tile [k][c], solved in place
+  float* Ts = sm + LNB * XP;        // [128][LNB+1] L row-major [r][k], diagonal 32 x 32 blocks = their inverses
   constexpr int TP = LNB + 1;
   const int tid = threadIdx.x;
   const long long c0 = c_begin + (long long)bid * RB;
@@ -538,39 +558,43 @@ __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long
         return (c < cols) ? W[(j0 + k) + (c0 + c) * ldw] : 0.f;
       },
       [&](int idx, float v) { Xs[(idx % LNB) * XP + idx / LNB] = v; });
-  // Linv column-major [k*128 + r]
   stage_tile<LNB * LNB, TRSM_THREADS, 32>(
-      tid, [&](int idx) { return Linv[idx]; }, [&](int idx, float v) { Ts[(idx % LNB) * TP + idx / LNB] = v; });
+      tid,
+      [&](int idx) {
+        const int r = idx % LNB, k = idx / LNB;
+        if ((r >> 5) == (k >> 5)) return Linv[idx];
+        return r > k ? W[(j0 + r) + (j0 + k) * ldw] : 0.f;
+      },
+      [&](int idx, float v) { Ts[(idx % LNB) * TP + idx / LNB] = v; });
   __syncthreads();
-  const int ty = tid / 16, tx = tid % 16;
-  float acc[8][TC];
+  const int cc = tid % RB, i0 = tid / RB;
+  for (int rb = 0; rb < 4; ++rb) {
+    float y[RU];
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
-#pragma unroll
-    for (int j = 0; j < TC; ++j) acc[i][j] = 0.f;
+    for (int u = 0; u < RU; ++u) y[u] = Xs[(32 * rb + i0 + RS * u) * XP + cc];
 #pragma unroll 4
-  for (int k = 0; k < LNB; ++k) {
-    float a[8], bb[TC];
+    for (int k = 0; k < 32 * rb; ++k) {
+      const float z = Xs[k * XP + cc];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) a[i] = Ts[(ty * 8 + i) * TP + k];
-    if constexpr (TC == 4) {
-      const float4 b = *reinterpret_cast<const float4*>(&Xs[k * XP + tx * 4]);
-      bb[0] = b.x; bb[1] = b.y; bb[2] = b.z; bb[3] = b.w;
-    } else {
-#pragma unroll
-      for (int j = 0; j < TC; ++j) bb[j] = Xs[k * XP + tx * TC + j];
+      for (int u = 0; u < RU; ++u) y[u] = fmaf(-Ts[(32 * rb + i0 + RS * u) * TP + k], z, y[u]);
     }
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+    for (int u = 0; u < RU; ++u) Xs[(32 * rb + i0 + RS * u) * XP + cc] = y[u];
+    __syncthreads();
+    float x[RU];
 #pragma unroll
-      for (int j = 0; j < TC; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
+    for (int u = 0; u < RU; ++u) x[u] = 0.f;
+#pragma unroll 8
+    for (int m = 0; m < 32; ++m) {
+      const float z = Xs[(32 * rb + m) * XP + cc];
+#pragma unroll
+      for (int u = 0; u < RU; ++u) x[u] = fmaf(Ts[(32 * rb + i0 + RS * u) * TP + 32 * rb + m], z, x[u]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < RU; ++u) Xs[(32 * rb + i0 + RS * u) * XP + cc] = x[u];
+    __syncthreads();
   }
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < 8; ++i)
-#pragma unroll
-    for (int j = 0; j < TC; ++j) Xs[(ty * 8 + i) * XP + tx * TC + j] = acc[i][j];
-  __syncthreads();
   for (int idx = tid; idx < LNB * RB; idx += TRSM_THREADS) {
     const int r = idx % LNB, c = idx / LNB;
     if (c < cols) {
@@ -589,7 +613,7 @@ constexpr size_t trsm_pair_smem(int rb) {
 }
 
 // Both panel solves of one inner panel in one launch: blocks [0, nb) form
-// L21 = W21 Uinv (RB rows each), the rest U12 = Linv W12 (RB columns each);
+// L21 = W21 U^-1 (RB rows each), the rest U12 = L^-1 W12 (RB columns each);
 // they write disjoint outputs, so they run side by side.  RB = 64 for the
 // strips; RB = 16 for the 128 rows and columns of the next panel, which sit
 // on the chain: four times the CTAs, a quarter of the work each.
@@ -1551,10 +1575,10 @@ static int lu_apply_t(const void* fbuf, long long n, int fdtype, const float* v,
   MPDOK_TRY(reset_tickets(tk, s));
   const int slot = prof_start(MPDOK_PROF_TRSV, s);
   const size_t smem = (size_t)LNB * LNB * sizeof(float);
-  MPDOK_TRY(set_smem(k_trsv<F, true>, smem));
-  MPDOK_TRY(set_smem(k_trsv<F, false>, smem));
   const float* dr = (const float*)(fb + L.off_dr);
   const int* perm = (const int*)(fb + L.off_perm);
+  MPDOK_TRY(set_smem(k_trsv<F, true>, smem));
+  MPDOK_TRY(set_smem(k_trsv<F, false>, smem));
   launch(k_trsv<F, true>, L.nblk, 256, smem, s, LU, L.ldf, Linv, Ml, n, L.nblk, v, dr, perm, y, tk, err, skip);
   launch(k_trsv<F, false>, L.nblk, 256, smem, s, LU, L.ldf, Uinv, Mu, n, L.nblk, (const float*)y, d, perm, zz,
          tk + 1, err, skip);
@@ -1761,7 +1785,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   launch(k_scaled_copy, g2, 256, 0, s, A, lda, n, (const float*)d, W, w.ldw);
   MPDOK_LAUNCH_CHECK("lu scale");
 
-  const size_t smem_diag = DIAG_SMEM;
+  const size_t smem_diag = DIAG_RR_SMEM;
   constexpr size_t smem_tp = trsm_pair_smem(64), smem_tp16 = trsm_pair_smem(16);
   MPDOK_TRY(set_smem(k_lu_diag<F>, smem_diag));
   MPDOK_TRY(set_smem(k_trsm_pair<F, 64>, smem_tp));
@@ -1879,6 +1903,10 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   }
   if (bst < 0) return bst;
   {
+    // the full diagonal-block inverses of the triangular solves, then their chain tiles
+    MPDOK_TRY(set_smem(k_tri_inv_complete, DIAG_SMEM));
+    launch(k_tri_inv_complete, L.nblk, DIAG_THREADS, DIAG_SMEM, s, (const float*)W, w.ldw, n, Linv, Uinv);
+    MPDOK_LAUNCH_CHECK("lu diagonal-block inverses");
     const size_t smem_ct = 2 * (size_t)LNB * LNB * sizeof(float);
     MPDOK_TRY(set_smem(k_trsv_chain_tiles<F>, smem_ct));
     launch(k_trsv_chain_tiles<F>, dim3(L.nblk, 2), 256, smem_ct, s, (const F*)LU, L.ldf, (const float*)Linv,

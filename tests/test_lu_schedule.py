@@ -64,13 +64,14 @@ def _accesses(op, n, spw):
         return [("W", (0, n, 0, n), True)]
     _, _, J, jp, a, b, m, nn, K, koff, rb, _ = (int(x) for x in op["row"])
     buf = (J // spw) & 1
+    nbk = min(LNB, n - jp)
+    blk = (jp, jp + nbk, jp, jp + nbk)
     if op["kind"] == DIAG:
-        nbk = min(LNB, n - jp)
-        blk = (jp, jp + nbk, jp, jp + nbk)
-        return [("W", blk, False), ("LU", blk, True), (("inv", jp // LNB), (0, 1, 0, 1), True)]
+        # factors the block in place (W keeps L\\U in FP32 for the panel solves)
+        return [("W", blk, True), ("LU", blk, True), (("inv", jp // LNB), (0, 1, 0, 1), True)]
     if op["kind"] == SOLVE:
         slot = jp - J
-        return [("W", (a, b, jp, jp + LNB), False), ("W", (jp, jp + LNB, a, b), False),
+        return [("W", blk, False), ("W", (a, b, jp, jp + LNB), False), ("W", (jp, jp + LNB, a, b), False),
                 (("inv", jp // LNB), (0, 1, 0, 1), False),
                 (("Lp", buf), (a - J, b - J, slot, slot + LNB), True),
                 (("Up", buf), (a - J, b - J, slot, slot + LNB), True),
