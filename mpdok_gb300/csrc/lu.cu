@@ -469,7 +469,7 @@ __device__ __forceinline__ void trsm_right_body(const float* __restrict__ W, lon
   static_assert(RB % 16 == 0 && RB <= 64, "rows per block: a multiple of 16, at most 64");
   constexpr int RU = RB / 8;      // rows per thread
   extern __shared__ float sm[];
-  constexpr int XP = LNB + 1;     // odd pitch: the row-fastest staging writes hit distinct banks
+  constexpr int XP = LNB + 4;     // rows read as float4 runs along k
   constexpr int TSP = LNB + 4;
   float* Xs = sm;                 // [RB][XP]   rows of W21, solved in place
   float* Ts = sm + RB * XP;       // [128][TSP] U row-major [k][c], diagonal 32 x 32 blocks = their inverses
@@ -498,11 +498,18 @@ __device__ __forceinline__ void trsm_right_body(const float* __restrict__ W, lon
     float y[RU];
 #pragma unroll
     for (int u = 0; u < RU; ++u) y[u] = Xs[(i0 + 8 * u) * XP + c];
-#pragma unroll 4
-    for (int k = 0; k < 32 * cb; ++k) {
-      const float t = Ts[k * TSP + c];
+    for (int k = 0; k < 32 * cb; k += 4) {
+      float t[4];
 #pragma unroll
-      for (int u = 0; u < RU; ++u) y[u] = fmaf(-Xs[(i0 + 8 * u) * XP + k], t, y[u]);
+      for (int q = 0; q < 4; ++q) t[q] = Ts[(k + q) * TSP + c];
+#pragma unroll
+      for (int u = 0; u < RU; ++u) {
+        const float4 xv = *reinterpret_cast<const float4*>(&Xs[(i0 + 8 * u) * XP + k]);
+        y[u] = fmaf(-xv.x, t[0], y[u]);
+        y[u] = fmaf(-xv.y, t[1], y[u]);
+        y[u] = fmaf(-xv.z, t[2], y[u]);
+        y[u] = fmaf(-xv.w, t[3], y[u]);
+      }
     }
 #pragma unroll
     for (int u = 0; u < RU; ++u) Xs[(i0 + 8 * u) * XP + c] = y[u];
@@ -510,11 +517,19 @@ __device__ __forceinline__ void trsm_right_body(const float* __restrict__ W, lon
     float x[RU];
 #pragma unroll
     for (int u = 0; u < RU; ++u) x[u] = 0.f;
-#pragma unroll 8
-    for (int m = 0; m < 32; ++m) {
-      const float t = Ts[(32 * cb + m) * TSP + c];
+#pragma unroll 2
+    for (int m = 0; m < 32; m += 4) {
+      float t[4];
 #pragma unroll
-      for (int u = 0; u < RU; ++u) x[u] = fmaf(Xs[(i0 + 8 * u) * XP + 32 * cb + m], t, x[u]);
+      for (int q = 0; q < 4; ++q) t[q] = Ts[(32 * cb + m + q) * TSP + c];
+#pragma unroll
+      for (int u = 0; u < RU; ++u) {
+        const float4 xv = *reinterpret_cast<const float4*>(&Xs[(i0 + 8 * u) * XP + 32 * cb + m]);
+        x[u] = fmaf(xv.x, t[0], x[u]);
+        x[u] = fmaf(xv.y, t[1], x[u]);
+        x[u] = fmaf(xv.z, t[2], x[u]);
+        x[u] = fmaf(xv.w, t[3], x[u]);
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -546,8 +561,8 @@ __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long
   extern __shared__ float sm[];
   constexpr int XP = RB + 4;
   float* Xs = sm;                   // [128][XP]  W12 tile [k][c], solved in place
-  float* Ts = sm + LNB * XP;        // [128][LNB+1] L row-major [r][k], diagonal 32 x 32 blocks = their inverses
-  constexpr int TP = LNB + 1;
+  float* Ts = sm + LNB * XP;        // [128][TP] L row-major [r][k], diagonal 32 x 32 blocks = their inverses
+  constexpr int TP = LNB + 4;       // rows read as float4 runs along k
   const int tid = threadIdx.x;
   const long long c0 = c_begin + (long long)bid * RB;
   const int cols = (int)min((long long)RB, n - c0);
@@ -572,11 +587,18 @@ __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long
     float y[RU];
 #pragma unroll
     for (int u = 0; u < RU; ++u) y[u] = Xs[(32 * rb + i0 + RS * u) * XP + cc];
-#pragma unroll 4
-    for (int k = 0; k < 32 * rb; ++k) {
-      const float z = Xs[k * XP + cc];
+    for (int k = 0; k < 32 * rb; k += 4) {
+      float z[4];
 #pragma unroll
-      for (int u = 0; u < RU; ++u) y[u] = fmaf(-Ts[(32 * rb + i0 + RS * u) * TP + k], z, y[u]);
+      for (int q = 0; q < 4; ++q) z[q] = Xs[(k + q) * XP + cc];
+#pragma unroll
+      for (int u = 0; u < RU; ++u) {
+        const float4 lv = *reinterpret_cast<const float4*>(&Ts[(32 * rb + i0 + RS * u) * TP + k]);
+        y[u] = fmaf(-lv.x, z[0], y[u]);
+        y[u] = fmaf(-lv.y, z[1], y[u]);
+        y[u] = fmaf(-lv.z, z[2], y[u]);
+        y[u] = fmaf(-lv.w, z[3], y[u]);
+      }
     }
 #pragma unroll
     for (int u = 0; u < RU; ++u) Xs[(32 * rb + i0 + RS * u) * XP + cc] = y[u];
@@ -584,11 +606,19 @@ __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long
     float x[RU];
 #pragma unroll
     for (int u = 0; u < RU; ++u) x[u] = 0.f;
-#pragma unroll 8
-    for (int m = 0; m < 32; ++m) {
-      const float z = Xs[(32 * rb + m) * XP + cc];
+#pragma unroll 2
+    for (int m = 0; m < 32; m += 4) {
+      float z[4];
 #pragma unroll
-      for (int u = 0; u < RU; ++u) x[u] = fmaf(Ts[(32 * rb + i0 + RS * u) * TP + 32 * rb + m], z, x[u]);
+      for (int q = 0; q < 4; ++q) z[q] = Xs[(32 * rb + m + q) * XP + cc];
+#pragma unroll
+      for (int u = 0; u < RU; ++u) {
+        const float4 lv = *reinterpret_cast<const float4*>(&Ts[(32 * rb + i0 + RS * u) * TP + 32 * rb + m]);
+        x[u] = fmaf(lv.x, z[0], x[u]);
+        x[u] = fmaf(lv.y, z[1], x[u]);
+        x[u] = fmaf(lv.z, z[2], x[u]);
+        x[u] = fmaf(lv.w, z[3], x[u]);
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -607,8 +637,8 @@ __device__ __forceinline__ void trsm_left_body(const float* __restrict__ W, long
 
 // Shared memory of k_trsm_pair<F, RB>: the larger of its two bodies.
 constexpr size_t trsm_pair_smem(int rb) {
-  const size_t right = (size_t)(rb * (LNB + 1) + LNB * (LNB + 4)) * sizeof(float);
-  const size_t left = (size_t)(LNB * (rb + 4) + LNB * (LNB + 1)) * sizeof(float);
+  const size_t right = (size_t)(rb * (LNB + 4) + LNB * (LNB + 4)) * sizeof(float);
+  const size_t left = (size_t)(LNB * (rb + 4) + LNB * (LNB + 4)) * sizeof(float);
   return right > left ? right : left;
 }
 
@@ -1614,28 +1644,36 @@ int lu_apply_any(const void* fbuf, long long n, int fdtype, const float* v, floa
 // of J + 1 writes rows < Jn or columns < Jn only.  Operands alternate between
 // two buffers, so (b) of J still reads its own while J + 1 writes the other.
 //
-// Inside a super-panel the panels are pipelined over two more high-priority
-// streams.  The chain stream (sa) runs, per panel p with columns
-// [jp, r1 = jp + 128): the diagonal-block LU; the panel solve of the next
-// panel's own block rows and columns [r1, nxt); the update of the next
-// diagonal block [r1, nxt)^2 by panel p; then the next diagonal LU.  The
-// strip stream (sb) runs the rest of panel p's solve (rows and columns >=
-// nxt) and its updates outside that diagonal block:
-//   rows [r1, nxt) x columns [nxt, n), rows [nxt, Jend) x columns [r1, n),
-//   rows [Jend, n) x columns [r1, Jend).
-// The chain stream waits for the strips of panel p - 1 before its solve of
-// panel p's next block (that solve reads rows and columns the strips
-// update), so the diagonal LU of panel p + 1 overlaps the strips of p.
+// Inside a super-panel the panels are pipelined over three more streams.
+// The chain stream (sa) runs, per panel p with columns [jp, r1 = jp + 128):
+// the diagonal-block LU; the panel solve of the next panel's own block rows
+// and columns [r1, nxt); the update of the next diagonal block [r1, nxt)^2 by
+// panel p; then the next diagonal LU.  The strip stream (sb) runs the rest of
+// panel p's solve inside the super-panel (rows and columns [nxt, Jend)) and
+// its updates there:
+//   rows [r1, nxt) x columns [nxt, Jend), rows [nxt, Jend) x columns [r1, Jend).
+// The below stream (sc, lower priority) handles the rows and columns past the
+// super-panel left-looking: for panel p it first applies every earlier panel
+// of the super-panel to p's own column block rows >= Jend and row block
+// columns >= Jend (one update each, K = jp - J, instead of a K = 128 update of
+// the whole row and column strips per panel: 1/4.5 of the FP32 traffic), then
+// solves p's panel there.  Only later panels' below work and the far update
+// read what it writes.  The chain stream waits for the strip of panel p - 1 before its solve
+// of panel p's next block (that solve reads blocks the strip updates), so the
+// diagonal LU of panel p + 1 overlaps the strip of p, and neither waits for
+// the bulk below.  Without a super-panel below (the last one), the strip
+// stream runs the whole solve and both strips as one.
 //
 // The schedule is data: lu_schedule lists every launch, event record and
 // event wait of one factorization in issue order, lu_factor_t executes the
 // list, and mpdok_lu_schedule exports it, so that a host-only check can verify
 // that every pair of launches touching the same data is ordered by the
 // streams and events.
-enum LuStream : int { LU_MAIN = 0, LU_CHAIN = 1, LU_STRIP = 2 };
+enum LuStream : int { LU_MAIN = 0, LU_CHAIN = 1, LU_STRIP = 2, LU_BELOW = 3 };
 enum LuKind : int { LU_DIAG = 0, LU_SOLVE = 1, LU_UPDATE = 2, LU_RECORD = 3, LU_WAIT = 4, LU_PROF_START = 5,
                     LU_PROF_STOP = 6 };
-enum LuEvent : int { LU_EV_READY = 0, LU_EV_PANEL = 1, LU_EV_A = 2, LU_EV_B = 3 };
+enum LuEvent : int { LU_EV_READY = 0, LU_EV_PANEL = 1, LU_EV_A = 2, LU_EV_B = 3, LU_EV_C = 4 };
+constexpr int LU_NEVENTS = 5;
 struct LuStep {
   int kind = 0, stream = 0;
   long long J = 0;           // super-panel start (operand buffer (J / spw) & 1)
@@ -1693,6 +1731,8 @@ static std::vector<LuStep> lu_schedule(long long n, long long spw) {
     const long long Jend = std::min<long long>(n, J + spw);
     const int sa = lookahead ? LU_CHAIN : LU_MAIN;
     const int sb = split ? LU_STRIP : sa;
+    const int sc = LU_BELOW;
+    const bool below = lookahead && Jend < n;  // rows and columns past the super-panel
     for (long long jp = J; jp < Jend; jp += LNB) {
       const long long r1 = jp + LNB;                              // first row / column after the panel
       const long long nxt = std::min<long long>(r1 + LNB, Jend);  // end of the next panel of J
@@ -1712,20 +1752,42 @@ static std::vector<LuStep> lu_schedule(long long n, long long spw) {
       prof(sa, 0, false, 2.0 * 2.0 * (double)(nxt - std::min(r1, nxt)) * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
       if (split) record(sa, LU_EV_A);
       if (has_next) update(sa, J, koff, LNB, r1, r1, nxt - r1, nxt - r1);
-      // strips: the rest of the panel solve and of panel p's updates
+      // below, left-looking: panel p's own column and row blocks past the
+      // super-panel receive the updates of every earlier panel of J at once
+      // (K = jp - J), then the panel solve there; off the chain's path
+      if (below) {
+        if (jp > J) {
+          // issued before this panel's strip, so the event is still that of
+          // panel p - 1: the strips (and the chain's solves) of panels J .. p - 1
+          wait(sc, LU_EV_B);
+          update(sc, J, 0, jp - J, Jend, jp, n - Jend, std::min<long long>(LNB, Jend - jp));
+          update(sc, J, 0, jp - J, jp, Jend, std::min<long long>(LNB, Jend - jp), n - Jend);
+        }
+        wait(sc, LU_EV_A);
+        prof(sc, 2, true, 0.0);
+        solve(sc, J, jp, Jend, n, 64);
+        prof(sc, 2, false, 2.0 * 2.0 * (double)(n - Jend) * LNB * LNB);
+      }
+      // strip: the rest of the panel solve and of panel p's updates inside
+      // the super-panel (what the chain's next solve reads)
       if (split) wait(sb, LU_EV_A);
       const long long begin = has_next ? nxt : r1;
-      if (begin < n) {
+      const long long inner_end = below ? Jend : n;
+      if (begin < inner_end) {
         prof(sb, 1, true, 0.0);
-        solve(sb, J, jp, begin, n, 64);
-        prof(sb, 1, false, 2.0 * 2.0 * (double)(n - begin) * LNB * LNB);
+        solve(sb, J, jp, begin, inner_end, 64);
+        prof(sb, 1, false, 2.0 * 2.0 * (double)(inner_end - begin) * LNB * LNB);
       }
       if (has_next) {
-        update(sb, J, koff, LNB, r1, nxt, nxt - r1, n - nxt);
-        update(sb, J, koff, LNB, nxt, r1, Jend - nxt, n - r1);
-        update(sb, J, koff, LNB, Jend, r1, n - Jend, Jend - r1);
+        update(sb, J, koff, LNB, r1, nxt, nxt - r1, inner_end - nxt);
+        update(sb, J, koff, LNB, nxt, r1, Jend - nxt, inner_end - r1);
+        if (!below) update(sb, J, koff, LNB, Jend, r1, n - Jend, Jend - r1);
       }
       if (split) record(sb, LU_EV_B);
+    }
+    if (below) {  // join the below stream
+      record(sc, LU_EV_C);
+      wait(sa, LU_EV_C);
     }
     if (split) wait(sa, LU_EV_B);  // join the strips
     if (lookahead) {
@@ -1810,19 +1872,23 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   };
   const bool lookahead = n > spw;
   const bool split = n > LNB;
-  cudaStream_t side = nullptr, strip = nullptr;
-  cudaEvent_t evs[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t side = nullptr, strip = nullptr, below = nullptr;
+  cudaEvent_t evs[LU_NEVENTS] = {};
   auto cleanup = [&]() {
     for (cudaEvent_t& e : evs)
       if (e) cudaEventDestroy(e);
     if (side) cudaStreamDestroy(side);
     if (strip) cudaStreamDestroy(strip);
+    if (below) cudaStreamDestroy(below);
   };
   if (split) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    // the chain and the strip first; the bulk below the super-panel next; the far update last
+    const int mid = hi < lo ? hi + 1 : hi;
     cudaError_t e = cudaStreamCreateWithPriority(&strip, cudaStreamNonBlocking, hi);
     if (e == cudaSuccess && lookahead) e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi);
+    if (e == cudaSuccess && lookahead) e = cudaStreamCreateWithPriority(&below, cudaStreamNonBlocking, mid);
     for (cudaEvent_t& ev : evs)
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -1831,8 +1897,8 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     }
   }
   const std::vector<LuStep> sched = lu_schedule(n, spw);
-  const cudaStream_t streams[3] = {s, side, strip};  // LU_MAIN, LU_CHAIN, LU_STRIP
-  int prof_window[2] = {-1, -1};
+  const cudaStream_t streams[4] = {s, side, strip, below};  // LU_MAIN, LU_CHAIN, LU_STRIP, LU_BELOW
+  int prof_window[3] = {-1, -1, -1};
   auto body = [&]() -> int {
     for (const LuStep& st : sched) {
       if (st.stream != LU_MAIN && streams[st.stream] == nullptr) {
@@ -1898,6 +1964,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     if (bst != MPDOK_OK) {
       cudaStreamSynchronize(strip);
       if (side) cudaStreamSynchronize(side);
+      if (below) cudaStreamSynchronize(below);
     }
     cleanup();
   }
