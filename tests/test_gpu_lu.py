@@ -116,6 +116,36 @@ def test_mixed_solver_headline_family_small():
     assert O.relres(A64, x.cpu().numpy(), s.b) < 1e-12
 
 
+def test_hard_family_fp32_factors_reach_the_fp64_floor():
+    """The hard family (the headline's centres, C5's nugget 1e-6, smooth
+    right-hand side) at N = 4096, with eps scaled to the point density,
+    100 * sqrt(4096 / 32768): kappa ~ 1.5e7.  FP32 factors precondition the
+    GMRES-IR to <= max(1e-12, 10 x) the FP64 LU oracle's relres, and the
+    solution agrees with the oracle's to within kappa times the residual floor.
+    FP16 factors have kappa * u > 1 here; their outcome is only reported."""
+    import math
+    import warnings
+    from mpdok_gb300 import configs
+    from mpdok_gb300.rbf_kernel import assemble
+    from mpdok_gb300.solvers import MixedSolver
+    n = 4096
+    s = configs.hard_headline(n=n, eps=configs.HARD_EPS * math.sqrt(n / 32768))
+    A64 = O.rbf_matrix(s.coords, gamma=s.gamma, reg=s.reg)
+    x_ref = O.fp64_solve(A64, s.b)
+    floor = O.relres(A64, x_ref, s.b)
+    A = assemble(s.coords, gamma=s.gamma, reg=s.reg, dtype=torch.float64)
+    b = torch.from_numpy(s.b).cuda()
+    x, info = MixedSolver(factor_dtype="fp32").solve(A, b, tol=1e-12)
+    assert info["converged"]
+    xs = x.cpu().numpy()
+    assert O.relres(A64, xs, s.b) <= max(1e-12, 10 * floor)
+    assert np.linalg.norm(xs - x_ref) / np.linalg.norm(x_ref) < 1e-6
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        x16, info16 = MixedSolver(factor_dtype="fp16").solve(A, b, tol=1e-12)
+    assert torch.isfinite(x16).all() and info16["relres"] <= 1.0 + 1e-12
+
+
 def test_lu_not_factored_status():
     import ctypes
     from mpdok_gb300 import _native as N
