@@ -677,13 +677,46 @@ static int cycle_start_from_f32(const KWs& ws, const float* src32, cudaStream_t 
   return MPDOK_OK;
 }
 
+// Host copies of a cycle's done flag, two slots per host thread and device
+// (pinned, so the copy is asynchronous) with the events that mark them written.
+struct DoneProbe {
+  int* flag = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  bool ok = false;
+  DoneProbe() {
+    ok = cudaMallocHost(reinterpret_cast<void**>(&flag), 2 * sizeof(int)) == cudaSuccess &&
+         cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) cudaGetLastError();
+  }
+};
+
 int arnoldi_cycle(const KWs& ws, const Operator32& A, int m, int reorth, double tol_rel, const Precond* pc,
                   float* x32, double* x64, cudaStream_t s) {
   const long long n = ws.n;
   const ArnState st = arn_state(ws);
   const size_t smem_dots = (size_t)ws.ch * sizeof(float);
   const size_t smem_apply = (size_t)(KMAX_RESTART + 1 + ws.ch) * sizeof(float);
+  // Every kernel of an iteration is predicated on the device done flag, so
+  // the cycle may be queued whole; but a predicated-off iteration still costs
+  // its launches (~75 us at N = 32768, a preconditioned cycle converges in a
+  // few of its 30).  So the host reads the flag two iterations behind the
+  // queue (the GPU always has the next iteration queued) and stops queueing
+  // once it is set.  Not while the stream is being captured.
+  constexpr int MAX_DEV = 64;
+  thread_local DoneProbe* probes[MAX_DEV] = {};
+  int dev = 0;
+  MPDOK_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < MAX_DEV && probes[dev] == nullptr) probes[dev] = new DoneProbe();
+  DoneProbe* pp = (dev >= 0 && dev < MAX_DEV) ? probes[dev] : nullptr;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  const bool poll = pp != nullptr && pp->ok && cudaStreamIsCapturing(s, &cap) == cudaSuccess &&
+                    cap == cudaStreamCaptureStatusNone;
   for (int k = 0; k < m; ++k) {
+    if (poll && k >= 2) {
+      MPDOK_CUDA_TRY(cudaEventSynchronize(pp->ev[k & 1]));  // the flag after iteration k - 2
+      if (pp->flag[k & 1]) break;
+    }
     const float* vk = ws.V + (long long)k * ws.ldv;
     const float* opnd = vk;
     if (pc && pc->apply) {
@@ -704,6 +737,10 @@ int arnoldi_cycle(const KWs& ws, const Operator32& A, int m, int reorth, double 
     }
     launch(k_normalize, vec_blocks(n), KT, 0, s, ws.w, ws.V + (long long)(k + 1) * ws.ldv, n, ws.sc);
     MPDOK_LAUNCH_CHECK("arnoldi step");
+    if (poll) {
+      MPDOK_CUDA_TRY(cudaMemcpyAsync(&pp->flag[k & 1], &ws.sc->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+      MPDOK_CUDA_TRY(cudaEventRecord(pp->ev[k & 1], s));
+    }
   }
   launch(k_backsub, 1, 32, 0, s, ws.sc, st);
   if (pc && pc->apply) {
