@@ -720,8 +720,9 @@ int arnoldi_cycle(const KWs& ws, const Operator32& A, int m, int reorth, double 
     const float* vk = ws.V + (long long)k * ws.ldv;
     const float* opnd = vk;
     if (pc && pc->apply) {
-      MPDOK_TRY(pc->apply(pc->ctx, vk, pc->z, s, &ws.sc->done));
-      opnd = pc->z;
+      float* zk = pc->Z ? pc->Z + (long long)k * pc->ldz : pc->z;
+      MPDOK_TRY(pc->apply(pc->ctx, vk, zk, s, &ws.sc->done));
+      opnd = zk;
     }
     MPDOK_TRY(A.apply(A.ctx, opnd, ws.w, 1, ws.ldv, s, &ws.sc->done));
     double* Hcol = ws.H + (long long)k * st.ldh;
@@ -743,7 +744,11 @@ int arnoldi_cycle(const KWs& ws, const Operator32& A, int m, int reorth, double 
     }
   }
   launch(k_backsub, 1, 32, 0, s, ws.sc, st);
-  if (pc && pc->apply) {
+  if (pc && pc->apply && pc->Z) {
+    // x += M^{-1} V y = Z y
+    if (x64) launch(k_update<double>, vec_blocks(n), KT, 0, s, (const float*)pc->Z, pc->ldz, ws.y, ws.sc, n, x64, nullptr);
+    else launch(k_update<float>, vec_blocks(n), KT, 0, s, (const float*)pc->Z, pc->ldz, ws.y, ws.sc, n, x32, nullptr);
+  } else if (pc && pc->apply) {
     // x += M^{-1} (V y): t = V y into w, z = M^{-1} t, x += z.
     launch(k_update<float>, vec_blocks(n), KT, 0, s, ws.V, ws.ldv, ws.y, ws.sc, n, nullptr, ws.w);
     MPDOK_TRY(pc->apply(pc->ctx, ws.w, pc->z, s, nullptr));

@@ -85,6 +85,11 @@ struct Precond {
   int (*apply)(void* ctx, const float* v, float* z, cudaStream_t s, const int* skip) = nullptr;
   void* ctx = nullptr;
   float* z = nullptr;  // n floats of scratch for M^{-1} v
+  // optional: m columns (leading dimension ldz) that keep z_k = M^{-1} v_k of
+  // every Arnoldi step, so that the cycle's update x += M^{-1} V y is Z y and
+  // needs no further application of M^{-1}
+  float* Z = nullptr;
+  long long ldz = 0;
   // optional: all K columns (leading dimension ld) in one call; CG-IR uses it
   // when set (a factorization applied to K right-hand sides at once)
   int (*apply_cols)(void* ctx, const float* v, float* z, int K, long long ld, cudaStream_t s) = nullptr;

@@ -2610,10 +2610,14 @@ extern "C" int mpdok_lu_ir_solve_multi(const double* A, long long lda, long long
   return err_finish(merr, body(), s);
 }
 
+// Leading dimension of the preconditioned directions Z kept by the LU-GMRES-IR.
+static long long zcols_ld(long long n) { return (std::max(1LL, n) + 63) / 64 * 64; }
+
 extern "C" size_t mpdok_lu_gmres_ir_work_size(long long n, int restart) {
   if (n < 0 || restart < 1) return 0;
   return align_up(apply_layout(n).total, 256) + align_up((size_t)std::max(1LL, n) * sizeof(float), 256) +
-         align_up(krylov_layout(n, restart, nullptr).total, 256) + align_up((size_t)std::max(1LL, n) * 8, 256) + 256;
+         align_up(krylov_layout(n, restart, nullptr).total, 256) + align_up((size_t)std::max(1LL, n) * 8, 256) +
+         align_up((size_t)restart * zcols_ld(n) * sizeof(float), 256) + 256;
 }
 
 extern "C" int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* A32, long long lda32, long long n,
@@ -2655,6 +2659,10 @@ extern "C" int mpdok_lu_gmres_ir(const double* A64, long long lda, const float* 
   // the mixed solve is guarded: on a singular or badly scaled system it returns
   // the best iterate with info->stagnated = 2 instead of diverging
   double* xbest = (double*)(wb + a_bytes + align_up((size_t)n * sizeof(float), 256) + align_up(ws.total, 256));
+  // z_k = M^-1 v_k of every Arnoldi step: the cycle's update needs no extra
+  // application of the triangular solves
+  pc.Z = (float*)((char*)xbest + align_up((size_t)n * 8, 256));
+  pc.ldz = zcols_ld(n);
   return err_finish(aerr, gmres_ir_core(ws, stored_op32(&c), stored_res64(&c), b, x, tol, maxiter_outer, restart,
                                         inner_tol, &pc, info, s, xbest), s);
 }
