@@ -1646,11 +1646,10 @@ int lu_apply_any(const void* fbuf, long long n, int fdtype, const float* v, floa
 //
 // Inside a super-panel the panels are pipelined over three more streams.
 // The chain stream (sa) runs, per panel p with columns [jp, r1 = jp + 128):
-// the diagonal-block LU; the panel solve of the next panel's own block rows
-// and columns [r1, nxt); the update of the next diagonal block [r1, nxt)^2 by
-// panel p; then the next diagonal LU.  The strip stream (sb) runs the rest of
-// panel p's solve inside the super-panel (rows and columns [nxt, Jend)) and
-// its updates there:
+// the diagonal-block LU; the panel solve for the rest of the super-panel
+// (rows and columns [r1, Jend), in 16-row blocks, one launch); the update of
+// the next diagonal block [r1, nxt)^2 by panel p; then the next diagonal LU.
+// The strip stream (sb) runs panel p's other updates inside the super-panel:
 //   rows [r1, nxt) x columns [nxt, Jend), rows [nxt, Jend) x columns [r1, Jend).
 // The below stream (sc, lower priority) handles the rows and columns past the
 // super-panel left-looking: for panel p it first applies every earlier panel
@@ -1747,9 +1746,11 @@ static std::vector<LuStep> lu_schedule(long long n, long long spw) {
       }
       if (has_next) {
         if (split && jp > J) wait(sa, LU_EV_B);  // strips of panel p - 1
-        solve(sa, J, jp, r1, nxt, 16);
+        // the panel's solve for the rest of the super-panel, the next panel's
+        // own block first in line, in 16-row blocks: one launch on the chain
+        solve(sa, J, jp, r1, Jend, 16);
       }
-      prof(sa, 0, false, 2.0 * 2.0 * (double)(nxt - std::min(r1, nxt)) * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
+      prof(sa, 0, false, 2.0 * 2.0 * (double)(Jend - std::min(r1, Jend)) * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
       if (split) record(sa, LU_EV_A);
       if (has_next) update(sa, J, koff, LNB, r1, r1, nxt - r1, nxt - r1);
       // below, left-looking: panel p's own column and row blocks past the
@@ -1768,16 +1769,10 @@ static std::vector<LuStep> lu_schedule(long long n, long long spw) {
         solve(sc, J, jp, Jend, n, 64);
         prof(sc, 2, false, 2.0 * 2.0 * (double)(n - Jend) * LNB * LNB);
       }
-      // strip: the rest of the panel solve and of panel p's updates inside
-      // the super-panel (what the chain's next solve reads)
+      // strip: the rest of panel p's updates inside the super-panel (what the
+      // chain's next solve reads)
       if (split) wait(sb, LU_EV_A);
-      const long long begin = has_next ? nxt : r1;
       const long long inner_end = below ? Jend : n;
-      if (begin < inner_end) {
-        prof(sb, 1, true, 0.0);
-        solve(sb, J, jp, begin, inner_end, 64);
-        prof(sb, 1, false, 2.0 * 2.0 * (double)(inner_end - begin) * LNB * LNB);
-      }
       if (has_next) {
         update(sb, J, koff, LNB, r1, nxt, nxt - r1, inner_end - nxt);
         update(sb, J, koff, LNB, nxt, r1, Jend - nxt, inner_end - r1);

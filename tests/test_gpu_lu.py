@@ -254,14 +254,11 @@ def test_profile_timeline_matches_class_totals():
         assert len(rows) == cnt > 0
         assert np.isclose(rows[:, 3].sum(), work, rtol=1e-12)
         assert np.isclose((rows[:, 2] - rows[:, 1]).sum(), ms, rtol=1e-3, atol=1e-3)
-    # a record per 128-column panel on the chain stream, one on the strip
-    # stream where rows of the super-panel remain below the panel's next block,
-    # and one on the below stream while super-panels follow (widths of 1024)
+    # a record per 128-column panel on the chain stream (its diagonal LU and
+    # its solve inside the super-panel), and one on the below stream while
+    # super-panels follow (widths of 1024)
     n, spw, expect = 3000, 1024, 0
     for jp in range(0, n, 128):
         jend = min(n, (jp // spw + 1) * spw)
-        below = n > spw and jend < n
-        r1 = jp + 128
-        begin = min(r1 + 128, jend) if r1 < jend else r1
-        expect += 1 + (begin < (jend if below else n)) + below
+        expect += 1 + (n > spw and jend < n)
     assert len(tl[tl[:, 0] == N.PROF_LU_PANEL]) == expect
