@@ -658,49 +658,100 @@ k_trsm_pair(const float* __restrict__ W, long long ldw, long long j0, long long 
     trsm_left_body<F, RB>(W, ldw, j0, begin, n, Linv, Up, pitch, base0, koff, LU, ldf, (int)blockIdx.x - nb);
 }
 
-// CUDA-core trailing update for FP32 factors: C -= A B^T, A (M x 128), B (N x 128) K-major FP32.
+// CUDA-core trailing update for FP32 factors: C -= A B^T, A (M x K) and B
+// (N x K) K-major FP32 with row pitch ldk.  CTA tile 128 x 128; K in slabs
+// of 16 staged transposed in shared memory, double-buffered (the next slab's
+// global loads sit in registers while the current slab is used, one barrier
+// per slab); thread tile 8 x 8 = rows {4 ty .. +3, 64 + 4 ty .. +3} x columns
+// {4 tx .. +3, 64 + 4 tx .. +3}, read as float4 (conflict-free).  Every
+// output accumulates its products in ascending k, one FMA each.
+constexpr int SG_BK = 16;
+constexpr int SG_P = 128 + 4;
+
+// Eight consecutive K-values of one operand row (zero past M or K).
+__device__ __forceinline__ void sg_load8(const float* __restrict__ X, int row, int rows, int k, int K, long long ldk,
+                                         float (&r)[8]) {
+  const float* p = X + (long long)row * ldk + k;
+  if (row < rows && k + 8 <= K && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+    const float4 u = __ldg(reinterpret_cast<const float4*>(p));
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p) + 1);
+    r[0] = u.x; r[1] = u.y; r[2] = u.z; r[3] = u.w; r[4] = v.x; r[5] = v.y; r[6] = v.z; r[7] = v.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) r[i] = (row < rows && k + i < K) ? __ldg(p + i) : 0.f;
+  }
+}
+
 __global__ void __launch_bounds__(256)
 k_gemm_update_f32(float* __restrict__ C, long long ldc, const float* __restrict__ A, const float* __restrict__ B,
                   long long ldk, int M, int N, int K) {
-  __shared__ float As[16][128 + 4];
-  __shared__ float Bs[16][128 + 4];
+  __shared__ __align__(16) float As[2][SG_BK][SG_P];
+  __shared__ __align__(16) float Bs[2][SG_BK][SG_P];
   const int tid = threadIdx.x;
   const int m0 = blockIdx.x * 128, n0 = blockIdx.y * 128;
   const int ty = tid / 16, tx = tid % 16;
+  const int lr = tid >> 1, lk = (tid & 1) * 8;  // staging: row lr, K-values lk .. lk + 7 of the slab
+  float ra[8], rb[8];
+  auto stage = [&](int buf) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      As[buf][lk + i][lr] = ra[i];
+      Bs[buf][lk + i][lr] = rb[i];
+    }
+  };
   float acc[8][8];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-  for (int kb = 0; kb < K; kb += 16) {
-    for (int idx = tid; idx < 16 * 128; idx += 256) {
-      const int k = idx % 16, r = idx / 16;
-      As[k][r] = (m0 + r < M && kb + k < K) ? A[(long long)(m0 + r) * ldk + kb + k] : 0.f;
-      Bs[k][r] = (n0 + r < N && kb + k < K) ? B[(long long)(n0 + r) * ldk + kb + k] : 0.f;
+  sg_load8(A, m0 + lr, M, lk, K, ldk, ra);
+  sg_load8(B, n0 + lr, N, lk, K, ldk, rb);
+  stage(0);
+  __syncthreads();
+  for (int kb = 0; kb < K; kb += SG_BK) {
+    const int cur = (kb / SG_BK) & 1;
+    const bool more = kb + SG_BK < K;
+    if (more) {
+      sg_load8(A, m0 + lr, M, kb + SG_BK + lk, K, ldk, ra);
+      sg_load8(B, n0 + lr, N, kb + SG_BK + lk, K, ldk, rb);
     }
-    __syncthreads();
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      float a[8], b[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) a[i] = As[k][ty * 8 + i];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) b[j] = Bs[k][tx * 8 + j];
+    for (int k = 0; k < SG_BK; ++k) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[cur][k][4 * ty]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[cur][k][64 + 4 * ty]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[cur][k][4 * tx]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[cur][k][64 + 4 * tx]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
     }
+    if (more) stage(cur ^ 1);  // the other buffer was last read before the previous barrier
     __syncthreads();
   }
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const int col = n0 + tx * 8 + j;
+    const int col = n0 + (j < 4 ? 4 * tx + j : 64 + 4 * tx + j - 4);
     if (col >= N) continue;
+    float* c = C + (long long)col * ldc;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int row = m0 + ty * 8 + i;
-      if (row < M) C[row + (long long)col * ldc] -= acc[i][j];
+    for (int h = 0; h < 2; ++h) {
+      const int row = m0 + h * 64 + 4 * ty;
+      float* cp = c + row;
+      if (row + 4 <= M && (reinterpret_cast<uintptr_t>(cp) & 15) == 0) {
+        float4 v = *reinterpret_cast<float4*>(cp);
+        v.x -= acc[4 * h + 0][j];
+        v.y -= acc[4 * h + 1][j];
+        v.z -= acc[4 * h + 2][j];
+        v.w -= acc[4 * h + 3][j];
+        *reinterpret_cast<float4*>(cp) = v;
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (row + i < M) cp[i] -= acc[4 * h + i][j];
+      }
     }
   }
 }
