@@ -109,15 +109,18 @@ k_matfree_f32(const __grid_constant__ CUtensorMap tmC, const __grid_constant__ C
     if (ntiles > 0) issue(0);
     if (ntiles > 1) issue(1);
   }
+  static_assert(MF_RPT == 2, "a thread's rows are one packed pair");
   float4 rc[MF_RPT];
-  float acc[MF_RPT][K];
+  float2 accp[K];  // (row 0, row 1) per right-hand side
 #pragma unroll
   for (int t = 0; t < MF_RPT; ++t) {
     const long long r = r0 + tid + (long long)t * MF_THREADS;
     rc[t] = (r < nrows) ? rowpack[r] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int kk = 0; kk < K; ++kk) acc[t][kk] = 0.f;
   }
+#pragma unroll
+  for (int kk = 0; kk < K; ++kk) accp[kk] = make_float2(0.f, 0.f);
+  const float2 rx = make_float2(rc[0].x, rc[1].x), ry = make_float2(rc[0].y, rc[1].y),
+               rz = make_float2(rc[0].z, rc[1].z);
   for (int t = 0; t < ntiles; ++t) {
     const int st = t & 1;
     // every thread observes the completed phase (acquire of the TMA writes)
@@ -132,19 +135,25 @@ k_matfree_f32(const __grid_constant__ CUtensorMap tmC, const __grid_constant__ C
 #pragma unroll 4
     for (int j = 0; j < nb; ++j) {
       const float4 c = sC[st][j];
+      // the thread's two rows as packed pairs (FP32x2 pipe): per lane the
+      // same IEEE operations, in the same order, as
+      //   d2 = fma(dx, dx, fma(dy, dy, dz * dz)),  acc = fma(v, x_j, acc)
+      const float2 dx = __fadd2_rn(rx, make_float2(-c.x, -c.x));
+      const float2 dy = __fadd2_rn(ry, make_float2(-c.y, -c.y));
+      const float2 dz = __fadd2_rn(rz, make_float2(-c.z, -c.z));
+      const float2 d2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+      float2 v;
+      if (KIND == MPDOK_KERNEL_GAUSSIAN) {
+        const float2 e = __fmul2_rn(make_float2(g, g), d2);  // g = -gamma * log2(e)
+        v = make_float2(ex2_approx(e.x), ex2_approx(e.y));
+      } else {
+        const float2 a = __ffma2_rn(make_float2(g, g), d2, make_float2(1.f, 1.f));  // g = gamma
+        v = __fmul2_rn(a, make_float2(rsqrt_approx(a.x), rsqrt_approx(a.y)));
+      }
 #pragma unroll
-      for (int u = 0; u < MF_RPT; ++u) {
-        const float dx = rc[u].x - c.x, dy = rc[u].y - c.y, dz = rc[u].z - c.z;
-        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        float v;
-        if (KIND == MPDOK_KERNEL_GAUSSIAN) {
-          v = ex2_approx(g * d2);  // g = -gamma * log2(e)
-        } else {
-          const float a = fmaf(g, d2, 1.f);  // g = gamma
-          v = a * rsqrt_approx(a);
-        }
-#pragma unroll
-        for (int kk = 0; kk < K; ++kk) acc[u][kk] = fmaf(v, sX[st][kk][j], acc[u][kk]);
+      for (int kk = 0; kk < K; ++kk) {
+        const float xj = sX[st][kk][j];
+        accp[kk] = __ffma2_rn(v, make_float2(xj, xj), accp[kk]);
       }
     }
     __syncthreads();
@@ -159,7 +168,7 @@ k_matfree_f32(const __grid_constant__ CUtensorMap tmC, const __grid_constant__ C
     const long long r = r0 + tid + (long long)u * MF_THREADS;
     if (r < nrows) {
 #pragma unroll
-      for (int kk = 0; kk < K; ++kk) P[((long long)sidx * K + kk) * nrows + r] = acc[u][kk];
+      for (int kk = 0; kk < K; ++kk) P[((long long)sidx * K + kk) * nrows + r] = u == 0 ? accp[kk].x : accp[kk].y;
     }
   }
 }
