@@ -321,8 +321,9 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
 // Elimination step k reads the pivot row k and the column k; both are final
 // after step k - 1, so their owners publish them into double-buffered shared
 // rows right after their own step k - 1 update, and a step costs one barrier.
-// Every thread forms the pivot's reciprocal and its row's multiplier itself:
-//   u_kk <- +-tau when |u_kk| < tau (counted once),
+// The owner of the pivot also replaces a pivot below tau in magnitude by
+// +-tau (counted) and publishes its reciprocal; every thread then forms its
+// row's multiplier:
 //   l_r = a_rk * rcp_rn(u_kk),   a_rj <- fma(-l_r, u_kj, a_rj)  (j > k),
 // the operations and order of a step-by-step elimination.  The kernel then
 // writes L\U into the factor and back into W's diagonal block (FP32, for the
@@ -331,74 +332,82 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
 // solves need only those, and k_tri_inv_complete fills in the rest of the
 // 128 x 128 inverses once the factorization is done.
 constexpr size_t DIAG_RR_SMEM = (size_t)(LNB * DP + 4 * LNB) * sizeof(float);
+// Columns per thread: 512 threads of 32 columns hold half an SM's registers,
+// so the kernel finds room next to other streams' CTAs instead of waiting for
+// a whole SM to drain.
+constexpr int DIAG_CPT = 16;
+constexpr int DIAG_LU_THREADS = LNB * (LNB / DIAG_CPT);
+
+// The pivot of a step, as its owner hands it on: |u_kk| < tau becomes +-tau
+// (counted), and the reciprocal every thread multiplies by.
+__device__ __forceinline__ float pivot_fix(float& piv, float tau, int* nperturb) {
+  if (!(fabsf(piv) >= tau)) {
+    piv = (piv < 0.f) ? -tau : tau;
+    atomicAdd(nperturb, 1);
+  }
+  return __frcp_rn(piv);
+}
 
 template <typename F>
-__global__ void __launch_bounds__(DIAG_THREADS, 1)
+__global__ void __launch_bounds__(DIAG_LU_THREADS, 1)
 k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __restrict__ LU, long long ldf,
           float* __restrict__ Linv, float* __restrict__ Uinv, int* nperturb, float tau) {
   extern __shared__ float sm[];
   float* T = sm;                      // [128][DP]: the factored block, for the 32 x 32 inverses
   float* prow = sm + LNB * DP;        // [2][128]: pivot row k
   float* pcol = prow + 2 * LNB;       // [2][128]: column k before division
+  __shared__ float s_pinv[2];         // the reciprocal of pivot k
   static_assert((LNB * DP) % 4 == 0, "the pivot rows must be 16-byte aligned");
   const int tid = threadIdx.x, r = tid & (LNB - 1), g = tid >> 7;
-  float a[16];
+  float a[DIAG_CPT];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const int c = 16 * g + i;
+  for (int i = 0; i < DIAG_CPT; ++i) {
+    const int c = DIAG_CPT * g + i;
     a[i] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
   }
   // the inputs of step 0
+  if (r == 0 && g == 0) s_pinv[0] = pivot_fix(a[0], tau, nperturb);
   if (r == 0) {
 #pragma unroll
-    for (int i = 0; i < 16; ++i) prow[16 * g + i] = a[i];
+    for (int i = 0; i < DIAG_CPT; ++i) prow[DIAG_CPT * g + i] = a[i];
   }
   if (g == 0) pcol[r] = a[0];
   __syncthreads();
-  for (int gk = 0; 16 * gk < nbk; ++gk) {
+  for (int gk = 0; DIAG_CPT * gk < nbk; ++gk) {
 #pragma unroll
-    for (int kk = 0; kk < 16; ++kk) {
-      const int k = 16 * gk + kk;
+    for (int kk = 0; kk < DIAG_CPT; ++kk) {
+      const int k = DIAG_CPT * gk + kk;
       if (k >= nbk) break;  // uniform
       const float* pr = prow + (k & 1) * LNB;
       const float* pc = pcol + (k & 1) * LNB;
-      float piv = pr[k];
-      const bool small = !(fabsf(piv) >= tau);
-      if (small) piv = (piv < 0.f) ? -tau : tau;
-      const float pinv = __frcp_rn(piv);
-      if (small && r == k && g == gk) {
-        a[kk] = piv;
-        atomicAdd(nperturb, 1);
-      }
       if (r > k && g >= gk) {
-        const float l = pc[r] * pinv;
-        float u[16];
+        const float l = pc[r] * s_pinv[k & 1];
+        const bool own = g == gk;  // this thread's group holds column k
+        if (own) a[kk] = l;
 #pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          const float4 v = *reinterpret_cast<const float4*>(pr + 16 * g + i);
-          u[i] = v.x; u[i + 1] = v.y; u[i + 2] = v.z; u[i + 3] = v.w;
-        }
-        if (g == gk) {
-          a[kk] = l;
+        for (int i4 = 0; i4 < DIAG_CPT; i4 += 4) {
+          if (own && i4 + 3 <= kk) continue;  // columns <= k of the pivot's own group
+          const float4 v = *reinterpret_cast<const float4*>(pr + DIAG_CPT * g + i4);
+          const float u[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-          for (int i = kk + 1; i < 16; ++i) a[i] = fmaf(-l, u[i], a[i]);
-        } else {
-#pragma unroll
-          for (int i = 0; i < 16; ++i) a[i] = fmaf(-l, u[i], a[i]);
+          for (int q = 0; q < 4; ++q)
+            if (!own || i4 + q > kk) a[i4 + q] = fmaf(-l, u[q], a[i4 + q]);
         }
       }
-      // publish the inputs of step k + 1 (row k + 1 and column k + 1)
+      // publish the inputs of step k + 1: row k + 1 (its pivot fixed and
+      // inverted once, by its owner) and column k + 1
       const int k1 = k + 1;
       if (k1 < nbk) {
         float* nr = prow + (k1 & 1) * LNB;
         float* nc = pcol + (k1 & 1) * LNB;
+        const int c1 = (kk + 1) & (DIAG_CPT - 1);  // column k + 1 within its group
+        const int g1 = gk + (kk == DIAG_CPT - 1 ? 1 : 0);
+        if (r == k1 && g == g1) s_pinv[k1 & 1] = pivot_fix(a[c1], tau, nperturb);
         if (r == k1) {
 #pragma unroll
-          for (int i = 0; i < 16; i += 4)
-            *reinterpret_cast<float4*>(nr + 16 * g + i) = make_float4(a[i], a[i + 1], a[i + 2], a[i + 3]);
+          for (int i = 0; i < DIAG_CPT; i += 4)
+            *reinterpret_cast<float4*>(nr + DIAG_CPT * g + i) = make_float4(a[i], a[i + 1], a[i + 2], a[i + 3]);
         }
-        const int c1 = (kk + 1) & 15;  // column k + 1 within its group
-        const int g1 = gk + (kk == 15 ? 1 : 0);
         if (g == g1 && r >= k1) nc[r] = a[c1];
       }
       __syncthreads();
@@ -406,8 +415,8 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
   }
   // L\U out: the factor (F), W's diagonal block (FP32) and shared memory
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const int c = 16 * g + i;
+  for (int i = 0; i < DIAG_CPT; ++i) {
+    const int c = DIAG_CPT * g + i;
     T[r * DP + c] = a[i];
     if (r < nbk && c < nbk) {
       LU[(j0 + r) + (j0 + c) * ldf] = from_f32<F>(a[i]);
@@ -1695,35 +1704,31 @@ int lu_apply_any(const void* fbuf, long long n, int fdtype, const float* v, floa
 // of J + 1 writes rows < Jn or columns < Jn only.  Operands alternate between
 // two buffers, so (b) of J still reads its own while J + 1 writes the other.
 //
-// Inside a super-panel the panels are pipelined over three more streams.
-// The chain stream (sa) runs, per panel p with columns [jp, r1 = jp + 128):
-// the diagonal-block LU; the panel solve for the rest of the super-panel
-// (rows and columns [r1, Jend), in 16-row blocks, one launch); the update of
-// the next diagonal block [r1, nxt)^2 by panel p; then the next diagonal LU.
-// The strip stream (sb) runs panel p's other updates inside the super-panel:
-//   rows [r1, nxt) x columns [nxt, Jend), rows [nxt, Jend) x columns [r1, Jend).
-// The below stream (sc, lower priority) handles the rows and columns past the
-// super-panel left-looking: for panel p it first applies every earlier panel
-// of the super-panel to p's own column block rows >= Jend and row block
-// columns >= Jend (one update each, K = jp - J, instead of a K = 128 update of
-// the whole row and column strips per panel: 1/4.5 of the FP32 traffic), then
-// solves p's panel there.  Only later panels' below work and the far update
-// read what it writes.  The chain stream waits for the strip of panel p - 1 before its solve
-// of panel p's next block (that solve reads blocks the strip updates), so the
-// diagonal LU of panel p + 1 overlaps the strip of p, and neither waits for
-// the bulk below.  Without a super-panel below (the last one), the strip
-// stream runs the whole solve and both strips as one.
+// Inside a super-panel the panels run on two more streams.  The chain stream
+// (sa) runs, per panel p with columns [jp, r1 = jp + 128): the diagonal-block
+// LU; the panel solve for the rest of the super-panel (rows and columns
+// [r1, Jend), 16-row blocks, one launch); the update of the rest of the
+// super-panel, rows and columns [r1, Jend) (one launch); then the next
+// diagonal LU.  A panel therefore costs three dependent launches on one
+// stream and no cross-stream hand-off.  The below stream (sc, lower priority)
+// handles the rows and columns past the super-panel left-looking: for panel p
+// it first applies every earlier panel of the super-panel to p's own column
+// block rows >= Jend and row block columns >= Jend (one update each, K = jp -
+// J, instead of a K = 128 update of the whole row and column strips per
+// panel: 1/4.5 of the FP32 traffic), then solves p's panel there.  Only later
+// panels' below work and the far update read what it writes, so the chain
+// never waits for it.
 //
 // The schedule is data: lu_schedule lists every launch, event record and
 // event wait of one factorization in issue order, lu_factor_t executes the
 // list, and mpdok_lu_schedule exports it, so that a host-only check can verify
 // that every pair of launches touching the same data is ordered by the
 // streams and events.
-enum LuStream : int { LU_MAIN = 0, LU_CHAIN = 1, LU_STRIP = 2, LU_BELOW = 3 };
+enum LuStream : int { LU_MAIN = 0, LU_CHAIN = 1, LU_BELOW = 2 };
 enum LuKind : int { LU_DIAG = 0, LU_SOLVE = 1, LU_UPDATE = 2, LU_RECORD = 3, LU_WAIT = 4, LU_PROF_START = 5,
                     LU_PROF_STOP = 6 };
-enum LuEvent : int { LU_EV_READY = 0, LU_EV_PANEL = 1, LU_EV_A = 2, LU_EV_B = 3, LU_EV_C = 4 };
-constexpr int LU_NEVENTS = 5;
+enum LuEvent : int { LU_EV_READY = 0, LU_EV_PANEL = 1, LU_EV_A = 2, LU_EV_C = 3 };
+constexpr int LU_NEVENTS = 4;
 struct LuStep {
   int kind = 0, stream = 0;
   long long J = 0;           // super-panel start (operand buffer (J / spw) & 1)
@@ -1738,7 +1743,7 @@ struct LuStep {
 
 static std::vector<LuStep> lu_schedule(long long n, long long spw) {
   std::vector<LuStep> v;
-  const bool lookahead = n > spw, split = n > LNB;
+  const bool lookahead = n > spw;
   auto add = [&](int kind, int stream) {
     LuStep st;
     st.kind = kind;
@@ -1780,62 +1785,44 @@ static std::vector<LuStep> lu_schedule(long long n, long long spw) {
   for (long long J = 0; J < n; J += spw) {
     const long long Jend = std::min<long long>(n, J + spw);
     const int sa = lookahead ? LU_CHAIN : LU_MAIN;
-    const int sb = split ? LU_STRIP : sa;
     const int sc = LU_BELOW;
     const bool below = lookahead && Jend < n;  // rows and columns past the super-panel
     for (long long jp = J; jp < Jend; jp += LNB) {
-      const long long r1 = jp + LNB;                              // first row / column after the panel
-      const long long nxt = std::min<long long>(r1 + LNB, Jend);  // end of the next panel of J
+      const long long r1 = jp + LNB;  // first row / column after the panel
       const bool has_next = r1 < Jend;
-      const long long koff = jp - J;                              // the panel's K-slot in the operands
-      // chain: diagonal LU, then the next panel's own block rows / columns
+      const long long koff = jp - J;  // the panel's K-slot in the operands
+      // chain: the diagonal LU, the panel's solve for the rest of the
+      // super-panel (16-row blocks, one launch), then its update of the rest
+      // of the super-panel (one launch); every update a later panel of J needs
+      // is issued on this stream before it
       prof(sa, 0, true, 0.0);
       {
         LuStep& st = v[add(LU_DIAG, sa)];
         st.J = J;
         st.jp = jp;
       }
-      if (has_next) {
-        if (split && jp > J) wait(sa, LU_EV_B);  // strips of panel p - 1
-        // the panel's solve for the rest of the super-panel, the next panel's
-        // own block first in line, in 16-row blocks: one launch on the chain
-        solve(sa, J, jp, r1, Jend, 16);
-      }
+      if (has_next) solve(sa, J, jp, r1, Jend, 16);
       prof(sa, 0, false, 2.0 * 2.0 * (double)(Jend - std::min(r1, Jend)) * LNB * LNB + (2.0 / 3.0) * LNB * LNB * LNB);
-      if (split) record(sa, LU_EV_A);
-      if (has_next) update(sa, J, koff, LNB, r1, r1, nxt - r1, nxt - r1);
+      if (below) record(sa, LU_EV_A);
+      if (has_next) update(sa, J, koff, LNB, r1, r1, Jend - r1, Jend - r1);
       // below, left-looking: panel p's own column and row blocks past the
       // super-panel receive the updates of every earlier panel of J at once
       // (K = jp - J), then the panel solve there; off the chain's path
       if (below) {
+        wait(sc, LU_EV_A);  // the chain's solves of panels J .. p, and p's diagonal LU
         if (jp > J) {
-          // issued before this panel's strip, so the event is still that of
-          // panel p - 1: the strips (and the chain's solves) of panels J .. p - 1
-          wait(sc, LU_EV_B);
           update(sc, J, 0, jp - J, Jend, jp, n - Jend, std::min<long long>(LNB, Jend - jp));
           update(sc, J, 0, jp - J, jp, Jend, std::min<long long>(LNB, Jend - jp), n - Jend);
         }
-        wait(sc, LU_EV_A);
         prof(sc, 2, true, 0.0);
         solve(sc, J, jp, Jend, n, 64);
         prof(sc, 2, false, 2.0 * 2.0 * (double)(n - Jend) * LNB * LNB);
       }
-      // strip: the rest of panel p's updates inside the super-panel (what the
-      // chain's next solve reads)
-      if (split) wait(sb, LU_EV_A);
-      const long long inner_end = below ? Jend : n;
-      if (has_next) {
-        update(sb, J, koff, LNB, r1, nxt, nxt - r1, inner_end - nxt);
-        update(sb, J, koff, LNB, nxt, r1, Jend - nxt, inner_end - r1);
-        if (!below) update(sb, J, koff, LNB, Jend, r1, n - Jend, Jend - r1);
-      }
-      if (split) record(sb, LU_EV_B);
     }
     if (below) {  // join the below stream
       record(sc, LU_EV_C);
       wait(sa, LU_EV_C);
     }
-    if (split) wait(sa, LU_EV_B);  // join the strips
     if (lookahead) {
       record(LU_CHAIN, LU_EV_PANEL);
       wait(LU_MAIN, LU_EV_PANEL);
@@ -1917,24 +1904,21 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     return gemm_update(C, w.ldw, Ab, Bb, spw, (int)m, (int)nn, K, fdtype, MPDOK_ENGINE_TENSOR, errw, st);
   };
   const bool lookahead = n > spw;
-  const bool split = n > LNB;
-  cudaStream_t side = nullptr, strip = nullptr, below = nullptr;
+  cudaStream_t side = nullptr, below = nullptr;
   cudaEvent_t evs[LU_NEVENTS] = {};
   auto cleanup = [&]() {
     for (cudaEvent_t& e : evs)
       if (e) cudaEventDestroy(e);
     if (side) cudaStreamDestroy(side);
-    if (strip) cudaStreamDestroy(strip);
     if (below) cudaStreamDestroy(below);
   };
-  if (split) {
+  if (lookahead) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    // the chain and the strip first; the bulk below the super-panel next; the far update last
+    // the chain first; the panel work below the super-panel next; the far update last
     const int mid = hi < lo ? hi + 1 : hi;
-    cudaError_t e = cudaStreamCreateWithPriority(&strip, cudaStreamNonBlocking, hi);
-    if (e == cudaSuccess && lookahead) e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi);
-    if (e == cudaSuccess && lookahead) e = cudaStreamCreateWithPriority(&below, cudaStreamNonBlocking, mid);
+    cudaError_t e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&below, cudaStreamNonBlocking, mid);
     for (cudaEvent_t& ev : evs)
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -1943,7 +1927,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     }
   }
   const std::vector<LuStep> sched = lu_schedule(n, spw);
-  const cudaStream_t streams[4] = {s, side, strip, below};  // LU_MAIN, LU_CHAIN, LU_STRIP, LU_BELOW
+  const cudaStream_t streams[3] = {s, side, below};  // LU_MAIN, LU_CHAIN, LU_BELOW
   int prof_window[3] = {-1, -1, -1};
   auto body = [&]() -> int {
     for (const LuStep& st : sched) {
@@ -1959,7 +1943,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
         case LU_DIAG: {
           const int k = (int)(st.jp / LNB);
           const int nbk = (int)std::min<long long>(LNB, n - st.jp);
-          launch(k_lu_diag<F>, 1, DIAG_THREADS, smem_diag, cs, W, w.ldw, st.jp, nbk, LU, L.ldf,
+          launch(k_lu_diag<F>, 1, DIAG_LU_THREADS, smem_diag, cs, W, w.ldw, st.jp, nbk, LU, L.ldf,
                  Linv + (size_t)k * LNB * LNB, Uinv + (size_t)k * LNB * LNB, errw + 1, tau);
           MPDOK_LAUNCH_CHECK("lu diagonal block");
           break;
@@ -2005,12 +1989,11 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     return MPDOK_OK;
   };
   const int bst = body();
-  if (split) {
+  if (lookahead) {
     // on an error the side streams may still hold work: let it finish first
     if (bst != MPDOK_OK) {
-      cudaStreamSynchronize(strip);
-      if (side) cudaStreamSynchronize(side);
-      if (below) cudaStreamSynchronize(below);
+      cudaStreamSynchronize(side);
+      cudaStreamSynchronize(below);
     }
     cleanup();
   }

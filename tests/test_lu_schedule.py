@@ -1,8 +1,8 @@
 """Host-only check of the blocked LU's launch schedule (mpdok_lu_schedule).
 
-The factorization issues its kernels on four streams (the caller's, a chain
-stream, a strip stream and a stream for the rows and columns past the current
-super-panel) that only events order.  This test rebuilds the
+The factorization issues its kernels on three streams (the caller's, a chain
+stream for the work inside the current super-panel, and a stream for the rows
+and columns past it) that only events order.  This test rebuilds the
 happens-before relation of the exported schedule with vector clocks and checks:
 
 * every pair of launches that touch the same data with at least one write is
@@ -35,8 +35,8 @@ def _happens_before(steps):
     """Kernel ops (with a setup op first: the scaling and the working copy on
     the caller's stream) and a predicate hb(i, j): op i completes before op j
     starts on the GPU."""
-    cur = np.zeros((4, 4), dtype=np.int64)   # vector clock of each stream
-    count = [1, 0, 0, 0]                     # the setup op is position 1 of stream 0
+    cur = np.zeros((3, 3), dtype=np.int64)   # vector clock of each stream
+    count = [1, 0, 0]                        # the setup op is position 1 of stream 0
     cur[0, 0] = 1
     recorded = {}
     ops = [dict(kind=SETUP, stream=0, pos=1, clock=cur[0].copy())]
@@ -171,24 +171,23 @@ def test_schedule_orders_every_conflict(n, fdtype):
     check_schedule(N.lu_schedule(n, fdtype), n, fdtype)
 
 
-def test_schedule_has_four_streams_at_look_ahead_sizes():
+def test_schedule_has_three_streams_at_look_ahead_sizes():
     s = N.lu_schedule(4096, N.F16)
     kernels = s[np.isin(s[:, 0], [DIAG, SOLVE, UPDATE])]
-    assert set(np.unique(kernels[:, 1])) == {0, 1, 2, 3}
-    # the chain and the strip stream touch only rows and columns of their own super-panel
+    assert set(np.unique(kernels[:, 1])) == {0, 1, 2}
+    # the chain stream touches only rows and columns of its own super-panel
     spw = _spw(N.F16)
-    for row in kernels[np.isin(kernels[:, 1], [1, 2])]:
+    for row in kernels[kernels[:, 1] == 1]:
         J, a, b, m, nn = (int(row[k]) for k in (2, 4, 5, 6, 7))
         if int(row[0]) == SOLVE:
             assert b <= min(4096, J + spw)
         elif int(row[0]) == UPDATE:
             assert a + m <= min(4096, J + spw) and b + nn <= min(4096, J + spw)
-    s = N.lu_schedule(1000, N.F16)  # one super-panel: caller's stream and strip stream
-    assert set(np.unique(s[np.isin(s[:, 0], [DIAG, SOLVE, UPDATE]), 1])) == {0, 2}
+    s = N.lu_schedule(1000, N.F16)  # one super-panel: the caller's stream alone
+    assert set(np.unique(s[np.isin(s[:, 0], [DIAG, SOLVE, UPDATE]), 1])) == {0}
 
 
-@pytest.mark.parametrize("which", ["strips_before_next_solve", "far_update_before_next_super_panel",
-                                   "chain_before_strips", "chain_before_below_solve",
+@pytest.mark.parametrize("which", ["far_update_before_next_super_panel", "chain_before_below_solve",
                                    "below_before_far_update"])
 def test_checker_catches_a_missing_wait(which):
     """A planted mistake: drop one event wait from the exported schedule."""
@@ -196,16 +195,12 @@ def test_checker_catches_a_missing_wait(which):
     s = N.lu_schedule(n, fd)
     waits = np.nonzero(s[:, 0] == WAIT)[0]
     pick = {
-        # the chain stream's wait for the strips of the previous panel
-        "strips_before_next_solve": [w for w in waits if s[w, 1] == 1 and s[w, 11] == 3],
         # the chain stream's wait for part (a) of the previous far update
         "far_update_before_next_super_panel": [w for w in waits if s[w, 1] == 1 and s[w, 11] == 0][1:],
-        # the strip stream's wait for the chain's panel solve
-        "chain_before_strips": [w for w in waits if s[w, 1] == 2 and s[w, 11] == 2],
-        # the below stream's wait for the panel's diagonal LU before its solve
-        "chain_before_below_solve": [w for w in waits if s[w, 1] == 3 and s[w, 11] == 2],
+        # the below stream's wait for the panel's diagonal LU and solve
+        "chain_before_below_solve": [w for w in waits if s[w, 1] == 2 and s[w, 11] == 2],
         # the chain stream's join of the below stream before the far update
-        "below_before_far_update": [w for w in waits if s[w, 1] == 1 and s[w, 11] == 4],
+        "below_before_far_update": [w for w in waits if s[w, 1] == 1 and s[w, 11] == 3],
     }[which]
     assert pick
     broken = np.delete(s, pick[len(pick) // 2], axis=0)
