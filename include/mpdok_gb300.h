@@ -432,11 +432,14 @@ enum {
   MPDOK_PROF_GEMV_F32 = 0,   /* stored FP32 / 16-bit GEMV stage (bytes)  */
   MPDOK_PROF_GEMV_F64 = 1,   /* stored FP64 GEMV stage (bytes)           */
   MPDOK_PROF_ASSEMBLE = 2,   /* RBF assembly (bytes written)             */
-  MPDOK_PROF_LU_GEMM = 3,    /* LU trailing-update GEMM (flops)          */
+  MPDOK_PROF_LU_GEMM = 3,    /* LU trailing-update GEMM, K < 256, and the
+                                FP32-factor update (flops)               */
   MPDOK_PROF_TRSV = 4,       /* triangular solves (bytes)                */
   MPDOK_PROF_MATFREE = 5,    /* matrix-free evaluate-and-multiply (entries) */
   MPDOK_PROF_OOC_COPY = 6,   /* host -> device tile copies (bytes)       */
-  MPDOK_PROF_LU_PANEL = 7    /* LU panel factorization (flops)           */
+  MPDOK_PROF_LU_PANEL = 7,   /* LU panel factorization (flops)           */
+  MPDOK_PROF_LU_GEMM_DEEP = 8 /* LU trailing-update GEMM with K >= 256: the
+                                warp-specialised tensor-core kernel (flops) */
 };
 MPDOK_API long long mpdok_launch_count(void);
 MPDOK_API int mpdok_profile_enable(int on);
@@ -444,7 +447,7 @@ MPDOK_API int mpdok_profile_query(int kernel_class, double* total_ms, long long*
 /* Launches of the class that a device skip flag turned off (a finished
  * Arnoldi cycle): excluded from mpdok_profile_query's totals. */
 MPDOK_API long long mpdok_profile_skipped(int kernel_class);
-/* Algorithmic bytes of a class whose work counts flops (MPDOK_PROF_LU_GEMM:
+/* Algorithmic bytes of a class whose work counts flops (MPDOK_PROF_LU_GEMM*:
  * the FP32 C tile read and written plus the operands), for its HBM roofline. */
 MPDOK_API double mpdok_profile_bytes(int kernel_class);
 /* Timeline of every timed launch since mpdok_profile_enable, in launch order:

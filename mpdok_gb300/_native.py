@@ -28,7 +28,8 @@ ERR_IO = -7
 ERR_NONFINITE = -8
 
 F64, F32, BF16, F16 = 0, 1, 2, 3
-PROF_GEMV_F32, PROF_GEMV_F64, PROF_ASSEMBLE, PROF_LU_GEMM, PROF_TRSV, PROF_MATFREE, PROF_OOC_COPY, PROF_LU_PANEL = range(8)
+(PROF_GEMV_F32, PROF_GEMV_F64, PROF_ASSEMBLE, PROF_LU_GEMM, PROF_TRSV, PROF_MATFREE, PROF_OOC_COPY, PROF_LU_PANEL,
+ PROF_LU_GEMM_DEEP) = range(9)
 KERNEL_GAUSSIAN, KERNEL_MQ = 0, 1
 ENGINE_TENSOR, ENGINE_SIMT = 0, 1
 HISTORY_MAX = 256

@@ -38,7 +38,7 @@ constexpr int LNB = 128;          // panel width / TRSV block
 // more than that saves).  The FP32 factors' CUDA-core update is compute-bound,
 // so there the narrower width, with twice the super-panels to overlap, is
 // faster.
-inline long long super_panel_width(int fdtype) { return fdtype == MPDOK_F32 ? 512 : 1024; }
+inline long long super_panel_width(int fdtype) { return fdtype == MPDOK_F32 ? 512 : 2048; }
 constexpr long long SPIN_LIMIT = 1LL << 24;
 
 static int fsize(int fdtype) { return fdtype == MPDOK_F32 ? 4 : 2; }
@@ -255,48 +255,55 @@ __device__ __forceinline__ void inverse_doubling(const float* T, float* XL, floa
   __syncthreads();
 }
 
-// Inverses by recursive doubling: the 32 x 32 diagonal blocks are inverted by
-// substitution (one warp per block, one lane per column), then
-//   [X11 0; L21 X22]^-1 off-diagonal block = -X22 L21 X11,
-//   [X11 U12; 0 X22]^-1 off-diagonal block = -X11 U12 X22,
-// for block sizes 32 and 64, each product spread over all 256 threads.
 // The 32 x 32 diagonal blocks of L^-1 (unit lower) and U^-1 from the factored
 // block T (shared memory, pitch DP): warps 0-3 invert L's four blocks, warps
-// 4-7 U's, each with its column j in lane j's registers (fully unrolled
-// substitution; the block's rows are shared-memory broadcasts).  The terms
-// outside a column's triangle are exact zeros, so every entry gets the same
-// operations in the same order as a column-by-column substitution.  Entry
-// (r, c) of an inverse goes to dst[r * rs + c * cs].
-__device__ __forceinline__ void diag32_inverses(const float* T, float* XL, float* XU, int rs, int cs) {
+// 4-7 U's, lane j holding column j in registers.  The substitution is
+// right-looking: once x_i is final its term goes into every later row's
+// accumulator, so a step is one division (U) and independent FMAs, and the
+// block's column i is a shared-memory broadcast.  L's accumulators receive
+// their terms in increasing column order, the order of a row-by-row forward
+// substitution; U's in decreasing order.  Terms outside a column's triangle
+// are exact zeros.  Entry (r, c) of an inverse goes to dst[r * rs + c * cs];
+// with a staging area (32 x 33 floats per warp) and rs == 1 each warp writes
+// its block column by column in 128-byte runs instead of one word per lane.
+__device__ __forceinline__ void diag32_inverses(const float* T, float* XL, float* XU, int rs, int cs,
+                                                float* stage = nullptr) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int b = warp & 3;
-  const int o = b * 32;
+  if (warp >= 8) return;  // idle during the 32 x 32 substitutions
+  const int o = (warp & 3) * 32;
   const float* Tb = T + o * DP + o;
-  if (warp >= 8) {
-    // idle during the 32 x 32 substitutions
-  } else if (warp < 4) {
-    float x[32];
+  float x[32];
+  if (warp < 4) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) x[i] = (i == lane) ? 1.f : 0.f;
 #pragma unroll
     for (int i = 0; i < 32; ++i) {
-      float acc = (i == lane) ? 1.f : 0.f;
+      if (i < lane) x[i] = 0.f;
 #pragma unroll
-      for (int k = 0; k < i; ++k) acc = fmaf(-Tb[i * DP + k], x[k], acc);
-      x[i] = (i < lane) ? 0.f : acc;
+      for (int j = i + 1; j < 32; ++j) x[j] = fmaf(-Tb[j * DP + i], x[i], x[j]);
     }
-#pragma unroll
-    for (int i = 0; i < 32; ++i) XL[(o + i) * rs + (o + lane) * cs] = x[i];
   } else {
-    float x[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) x[i] = 0.f;
 #pragma unroll
     for (int i = 31; i >= 0; --i) {
-      float acc = 0.f;
+      const float num = (i == lane) ? 1.f : -x[i];
+      x[i] = (i > lane) ? 0.f : num / Tb[i * DP + i];
 #pragma unroll
-      for (int k = i + 1; k < 32; ++k) acc = fmaf(Tb[i * DP + k], x[k], acc);
-      const float d = Tb[i * DP + i];
-      x[i] = (i > lane) ? 0.f : (i == lane ? 1.f / d : -acc / d);
+      for (int j = 0; j < i; ++j) x[j] = fmaf(Tb[j * DP + i], x[i], x[j]);
     }
+  }
+  float* X = warp < 4 ? XL : XU;
+  if (stage != nullptr && rs == 1) {
+    float* st = stage + warp * 32 * 33;
 #pragma unroll
-    for (int i = 0; i < 32; ++i) XU[(o + i) * rs + (o + lane) * cs] = x[i];
+    for (int i = 0; i < 32; ++i) st[i * 33 + lane] = x[i];
+    __syncwarp();
+#pragma unroll 8
+    for (int c = 0; c < 32; ++c) X[(o + lane) + (long long)(o + c) * cs] = st[lane * 33 + c];
+  } else {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) X[(o + i) * rs + (o + lane) * cs] = x[i];
   }
 }
 
@@ -316,36 +323,107 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
 }
 
 
-// Unpivoted LU of the 128 x 128 diagonal block, held in registers: thread
-// (r = tid % 128, g = tid / 128) keeps row r, columns [16 g, 16 g + 16).
-// Elimination step k reads the pivot row k and the column k; both are final
-// after step k - 1, so their owners publish them into double-buffered shared
-// rows right after their own step k - 1 update, and a step costs one barrier.
-// The owner of the pivot also replaces a pivot below tau in magnitude by
-// +-tau (counted) and publishes its reciprocal; every thread then forms its
-// row's multiplier:
-//   l_r = a_rk * rcp_rn(u_kk),   a_rj <- fma(-l_r, u_kj, a_rj)  (j > k),
-// the operations and order of a step-by-step elimination.  The kernel then
-// writes L\U into the factor and back into W's diagonal block (FP32, for the
-// panel solves and the inverses), and the inverses of its 32 x 32 diagonal
-// blocks of L and U into the diagonal positions of Linv / Uinv; the panel
-// solves need only those, and k_tri_inv_complete fills in the rest of the
-// 128 x 128 inverses once the factorization is done.
-constexpr size_t DIAG_RR_SMEM = (size_t)(LNB * DP + 4 * LNB) * sizeof(float);
-// Columns per thread: 512 threads of 32 columns hold half an SM's registers,
-// so the kernel finds room next to other streams' CTAs instead of waiting for
-// a whole SM to drain.
-constexpr int DIAG_CPT = 16;
-constexpr int DIAG_LU_THREADS = LNB * (LNB / DIAG_CPT);
+// Unpivoted LU of the 128 x 128 diagonal block, blocked in four 32-column
+// sub-panels with the block in shared memory (T, pitch DP).  For sub-panel p:
+//  (a) one warp per 32-row block of the sub-panel's rows: lane i holds its
+//      row's 32 sub-panel columns, and every warp also holds the sub-panel's
+//      32 x 32 diagonal block, whose elimination it repeats with shuffles, so
+//      the 32 steps need no barrier.  The pivot u_kk is replaced by +-tau
+//      when |u_kk| < tau (counted once) and every multiplier is
+//        l_r = a_rk * rcp_rn(u_kk),   a_rj <- fma(-l_r, u_kj, a_rj);
+//  (b) one thread per column right of the sub-panel: its 32 rows of U by the
+//      same FMAs, the multipliers read from shared memory;
+//  (c) the trailing block: a_rj <- fma(-l_rk, u_kj, a_rj) for the sub-panel's
+//      32 k in increasing order, a register tile per thread.
+// Every entry therefore receives the operations of a step-by-step
+// elimination in the same order, with three barriers per sub-panel instead
+// of one per step.  The kernel then writes L\U into the factor and back into
+// W's diagonal block (FP32, for the panel solves and the inverses), and the
+// inverses of its 32 x 32 diagonal blocks of L and U into the diagonal
+// positions of Linv / Uinv; the panel solves need only those, and
+// k_tri_inv_complete fills in the rest of the 128 x 128 inverses once the
+// factorization is done.
+constexpr int DIAG_LU_THREADS = 256;
+constexpr size_t DIAG_RR_SMEM = (size_t)(LNB * DP + 8 * 32 * 33) * sizeof(float);
+// The launch asks for most of an SM's shared memory, so the block runs on an
+// SM of its own rather than beside the updates' CTAs on the other streams.
+constexpr size_t DIAG_RR_ALLOC = 200 * 1024;
+static_assert(DIAG_RR_SMEM <= DIAG_RR_ALLOC, "the diagonal LU's shared memory");
 
-// The pivot of a step, as its owner hands it on: |u_kk| < tau becomes +-tau
-// (counted), and the reciprocal every thread multiplies by.
-__device__ __forceinline__ float pivot_fix(float& piv, float tau, int* nperturb) {
-  if (!(fabsf(piv) >= tau)) {
-    piv = (piv < 0.f) ? -tau : tau;
-    atomicAdd(nperturb, 1);
+// Four consecutive entries of a factor column (16-byte aligned for FP32,
+// 8-byte for 16-bit factors).
+template <typename F>
+__device__ __forceinline__ void store4(F* p, const float (&v)[4]) {
+  if constexpr (sizeof(F) == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+    union {
+      F h[4];
+      uint2 u;
+    } pk;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) pk.h[e] = from_f32<F>(v[e]);
+    *reinterpret_cast<uint2*>(p) = pk.u;
   }
-  return __frcp_rn(piv);
+}
+static_assert(LNB == 128 && DIAG_LU_THREADS == 256, "the diagonal LU's map: 4 sub-panels, 8 warps, 16 x 16 tiles");
+
+// Step K of a sub-panel's elimination, then the steps after it, for the
+// sub-panel's diagonal block (d: lane i's row) and, with X, one more row
+// block (x: lane i's row).  Recursion over K keeps every register index a
+// constant.
+template <int K, bool X>
+__device__ __forceinline__ void subpanel_steps(float (&d)[32], float (&x)[32], int lane, bool counts, int kmax,
+                                               float tau, int* nperturb) {
+  if constexpr (K < 32) {
+    constexpr unsigned FULL = 0xffffffffu;
+    float piv = __shfl_sync(FULL, d[K], K);
+    const bool fix = K < kmax && !(fabsf(piv) >= tau);
+    if (fix) piv = (piv < 0.f) ? -tau : tau;
+    if (fix && counts && lane == K) atomicAdd(nperturb, 1);
+    if (lane == K) d[K] = piv;
+    const float pinv = __frcp_rn(piv);
+    const float ld = d[K] * pinv;
+    const float lx = X ? x[K] * pinv : 0.f;
+#pragma unroll
+    for (int j = K + 1; j < 32; ++j) {
+      const float u = __shfl_sync(FULL, d[j], K);
+      if (lane > K) d[j] = fmaf(-ld, u, d[j]);
+      if (X) x[j] = fmaf(-lx, u, x[j]);
+    }
+    if (lane > K) d[K] = ld;
+    if (X) x[K] = lx;
+    subpanel_steps<K + 1, X>(d, x, lane, counts, kmax, tau, nperturb);
+  }
+}
+
+// The trailing block of sub-panel p (m = 96 - 32 p rows and columns from
+// q = 32 p + 32): thread (ty, tx) of 16 x 16 owns rows q + ty + 16 i and
+// columns q + tx + 16 j, i, j < TS.
+template <int TS>
+__device__ __forceinline__ void subpanel_trailing(float* T, int P0, int tid) {
+  const int q = P0 + 32, ty = tid >> 4, tx = tid & 15;
+  float acc[TS][TS];
+#pragma unroll
+  for (int i = 0; i < TS; ++i)
+#pragma unroll
+    for (int j = 0; j < TS; ++j) acc[i][j] = T[(q + ty + 16 * i) * DP + q + tx + 16 * j];
+#pragma unroll 4
+  for (int k = 0; k < 32; ++k) {
+    float l[TS], u[TS];
+#pragma unroll
+    for (int i = 0; i < TS; ++i) l[i] = T[(q + ty + 16 * i) * DP + P0 + k];
+#pragma unroll
+    for (int j = 0; j < TS; ++j) u[j] = T[(P0 + k) * DP + q + tx + 16 * j];
+#pragma unroll
+    for (int i = 0; i < TS; ++i)
+#pragma unroll
+      for (int j = 0; j < TS; ++j) acc[i][j] = fmaf(-l[i], u[j], acc[i][j]);
+  }
+#pragma unroll
+  for (int i = 0; i < TS; ++i)
+#pragma unroll
+    for (int j = 0; j < TS; ++j) T[(q + ty + 16 * i) * DP + q + tx + 16 * j] = acc[i][j];
 }
 
 template <typename F>
@@ -353,78 +431,90 @@ __global__ void __launch_bounds__(DIAG_LU_THREADS, 1)
 k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __restrict__ LU, long long ldf,
           float* __restrict__ Linv, float* __restrict__ Uinv, int* nperturb, float tau) {
   extern __shared__ float sm[];
-  float* T = sm;                      // [128][DP]: the factored block, for the 32 x 32 inverses
-  float* prow = sm + LNB * DP;        // [2][128]: pivot row k
-  float* pcol = prow + 2 * LNB;       // [2][128]: column k before division
-  __shared__ float s_pinv[2];         // the reciprocal of pivot k
-  static_assert((LNB * DP) % 4 == 0, "the pivot rows must be 16-byte aligned");
-  const int tid = threadIdx.x, r = tid & (LNB - 1), g = tid >> 7;
-  float a[DIAG_CPT];
+  float* T = sm;                  // [128][DP]: the block
+  float* stage = sm + LNB * DP;   // [8][32][33]: the inverses on their way out
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // 32 threads per column, four rows each (16-byte accesses; W's pitch is a
+  // multiple of 4 and j0 of 128), 8 columns per pass
+  const int r4 = 4 * lane;
+#pragma unroll 4
+  for (int c = warp; c < LNB; c += DIAG_LU_THREADS / 32) {
+    float v[4];
+    if (c < nbk && r4 + 3 < nbk) {
+      const float4 q = *reinterpret_cast<const float4*>(W + (j0 + r4) + (j0 + c) * ldw);
+      v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+    } else {
 #pragma unroll
-  for (int i = 0; i < DIAG_CPT; ++i) {
-    const int c = DIAG_CPT * g + i;
-    a[i] = (r < nbk && c < nbk) ? W[(j0 + r) + (j0 + c) * ldw] : (r == c ? 1.f : 0.f);
-  }
-  // the inputs of step 0
-  if (r == 0 && g == 0) s_pinv[0] = pivot_fix(a[0], tau, nperturb);
-  if (r == 0) {
-#pragma unroll
-    for (int i = 0; i < DIAG_CPT; ++i) prow[DIAG_CPT * g + i] = a[i];
-  }
-  if (g == 0) pcol[r] = a[0];
-  __syncthreads();
-  for (int gk = 0; DIAG_CPT * gk < nbk; ++gk) {
-#pragma unroll
-    for (int kk = 0; kk < DIAG_CPT; ++kk) {
-      const int k = DIAG_CPT * gk + kk;
-      if (k >= nbk) break;  // uniform
-      const float* pr = prow + (k & 1) * LNB;
-      const float* pc = pcol + (k & 1) * LNB;
-      if (r > k && g >= gk) {
-        const float l = pc[r] * s_pinv[k & 1];
-        const bool own = g == gk;  // this thread's group holds column k
-        if (own) a[kk] = l;
-#pragma unroll
-        for (int i4 = 0; i4 < DIAG_CPT; i4 += 4) {
-          if (own && i4 + 3 <= kk) continue;  // columns <= k of the pivot's own group
-          const float4 v = *reinterpret_cast<const float4*>(pr + DIAG_CPT * g + i4);
-          const float u[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-            if (!own || i4 + q > kk) a[i4 + q] = fmaf(-l, u[q], a[i4 + q]);
-        }
-      }
-      // publish the inputs of step k + 1: row k + 1 (its pivot fixed and
-      // inverted once, by its owner) and column k + 1
-      const int k1 = k + 1;
-      if (k1 < nbk) {
-        float* nr = prow + (k1 & 1) * LNB;
-        float* nc = pcol + (k1 & 1) * LNB;
-        const int c1 = (kk + 1) & (DIAG_CPT - 1);  // column k + 1 within its group
-        const int g1 = gk + (kk == DIAG_CPT - 1 ? 1 : 0);
-        if (r == k1 && g == g1) s_pinv[k1 & 1] = pivot_fix(a[c1], tau, nperturb);
-        if (r == k1) {
-#pragma unroll
-          for (int i = 0; i < DIAG_CPT; i += 4)
-            *reinterpret_cast<float4*>(nr + DIAG_CPT * g + i) = make_float4(a[i], a[i + 1], a[i + 2], a[i + 3]);
-        }
-        if (g == g1 && r >= k1) nc[r] = a[c1];
-      }
-      __syncthreads();
+      for (int e = 0; e < 4; ++e)
+        v[e] = (r4 + e < nbk && c < nbk) ? W[(j0 + r4 + e) + (j0 + c) * ldw] : (r4 + e == c ? 1.f : 0.f);
     }
-  }
-  // L\U out: the factor (F), W's diagonal block (FP32) and shared memory
 #pragma unroll
-  for (int i = 0; i < DIAG_CPT; ++i) {
-    const int c = DIAG_CPT * g + i;
-    T[r * DP + c] = a[i];
-    if (r < nbk && c < nbk) {
-      LU[(j0 + r) + (j0 + c) * ldf] = from_f32<F>(a[i]);
-      W[(j0 + r) + (j0 + c) * ldw] = a[i];
-    }
+    for (int e = 0; e < 4; ++e) T[(r4 + e) * DP + c] = v[e];
   }
   __syncthreads();
-  diag32_inverses(T, Linv, Uinv, 1, LNB);
+  for (int p = 0; p < 4 && 32 * p < nbk; ++p) {
+    const int P0 = 32 * p;
+    // (a) the sub-panel: warp w < 4 - p takes rows P0 + 32 w + lane
+    // (warp 0 keeps the diagonal block and carries zero rows, so that every
+    // warp runs the same code: the kernel's instructions are fetched per
+    // launch, often from a busy L2)
+    const int kmax = nbk - P0;  // pivots past the block's edge are the padding's ones
+    if (warp < 4 - p) {
+      float d[32], x[32];
+      const int R = P0 + 32 * warp + lane;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        d[j] = T[(P0 + lane) * DP + P0 + j];
+        x[j] = warp == 0 ? 0.f : T[R * DP + P0 + j];
+      }
+      subpanel_steps<0, true>(d, x, lane, warp == 0, kmax, tau, nperturb);
+      if (warp == 0) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) T[(P0 + lane) * DP + P0 + j] = d[j];
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) T[R * DP + P0 + j] = x[j];
+      }
+    }
+    __syncthreads();
+    if (p == 3) break;
+    // (b) U's rows P0 .. P0 + 31 right of the sub-panel, a column per thread
+    const int c = P0 + 32 + tid;
+    if (c < LNB) {
+      float u[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) u[i] = T[(P0 + i) * DP + c];
+#pragma unroll
+      for (int k = 0; k < 32; ++k)
+#pragma unroll
+        for (int i = k + 1; i < 32; ++i) u[i] = fmaf(-T[(P0 + i) * DP + P0 + k], u[k], u[i]);
+#pragma unroll
+      for (int i = 1; i < 32; ++i) T[(P0 + i) * DP + c] = u[i];
+    }
+    __syncthreads();
+    // (c) the trailing block
+    if (p == 0) subpanel_trailing<6>(T, P0, tid);
+    else if (p == 1) subpanel_trailing<4>(T, P0, tid);
+    else subpanel_trailing<2>(T, P0, tid);
+    __syncthreads();
+  }
+  // L\U out: the factor (F) and W's diagonal block (FP32), in the load's map
+  // (the factor's pitch is a multiple of 8)
+  for (int c = warp; c < nbk; c += DIAG_LU_THREADS / 32) {
+    float v[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) v[e] = T[(r4 + e) * DP + c];
+    if (r4 + 3 < nbk) {
+      *reinterpret_cast<float4*>(W + (j0 + r4) + (j0 + c) * ldw) = make_float4(v[0], v[1], v[2], v[3]);
+      store4(LU + (j0 + r4) + (j0 + c) * ldf, v);
+    } else {
+      for (int e = 0; e < 4 && r4 + e < nbk; ++e) {
+        W[(j0 + r4 + e) + (j0 + c) * ldw] = v[e];
+        LU[(j0 + r4 + e) + (j0 + c) * ldf] = from_f32<F>(v[e]);
+      }
+    }
+  }
+  diag32_inverses(T, Linv, Uinv, 1, LNB, stage);
 }
 
 // The full 128 x 128 inverses of every diagonal block (for the triangular
@@ -1727,8 +1817,8 @@ int lu_apply_any(const void* fbuf, long long n, int fdtype, const float* v, floa
 enum LuStream : int { LU_MAIN = 0, LU_CHAIN = 1, LU_BELOW = 2 };
 enum LuKind : int { LU_DIAG = 0, LU_SOLVE = 1, LU_UPDATE = 2, LU_RECORD = 3, LU_WAIT = 4, LU_PROF_START = 5,
                     LU_PROF_STOP = 6 };
-enum LuEvent : int { LU_EV_READY = 0, LU_EV_PANEL = 1, LU_EV_A = 2, LU_EV_C = 3 };
-constexpr int LU_NEVENTS = 4;
+enum LuEvent : int { LU_EV_READY = 0, LU_EV_PANEL = 1, LU_EV_A = 2, LU_EV_C = 3, LU_EV_B = 4 };
+constexpr int LU_NEVENTS = 5;
 struct LuStep {
   int kind = 0, stream = 0;
   long long J = 0;           // super-panel start (operand buffer (J / spw) & 1)
@@ -1833,18 +1923,20 @@ static std::vector<LuStep> lu_schedule(long long n, long long spw) {
         update(LU_MAIN, J, 0, K, Jend, Jend, n - Jend, n - Jend);
       } else {
         const long long Jn = std::min<long long>(n, Jend + spw);
-        // (a) what super-panel J + 1 reads and writes first
-        update(LU_MAIN, J, 0, K, Jend, Jend, Jn - Jend, n - Jend);
-        update(LU_MAIN, J, 0, K, Jn, Jend, n - Jn, Jn - Jend);
-        record(LU_MAIN, LU_EV_READY);
-        wait(LU_CHAIN, LU_EV_READY);
-        // (b) the rest of the trailing matrix, concurrent with J + 1, in up to
-        // four column chunks: a kernel boundary on this stream drains the
-        // SMs, which lets the panel kernels (one of them needs a whole SM) in
-        // without waiting for the whole update
+        // (a) what super-panel J + 1 reads and writes first, on the chain
+        // stream at its priority, once part (b) of J - 1 (which covers J + 1's
+        // rows and columns too) is done
+        if (J > 0) wait(LU_CHAIN, LU_EV_B);
+        update(LU_CHAIN, J, 0, K, Jend, Jend, Jn - Jend, n - Jend);
+        update(LU_CHAIN, J, 0, K, Jn, Jend, n - Jn, Jn - Jend);
+        // (b) the rest of the trailing matrix on the caller's stream,
+        // concurrent with J + 1, in up to four column chunks: a kernel
+        // boundary on this stream drains the SMs, which lets the panel kernels
+        // (one of them needs a whole SM) in without waiting for the whole update
         const long long rest = n - Jn;
         const long long chunk = std::max<long long>(2048, (rest / 4 + 255) / 256 * 256);
         for (long long c = Jn; c < n; c += chunk) update(LU_MAIN, J, 0, K, Jn, c, n - Jn, std::min(chunk, n - c));
+        if (Jn < n) record(LU_MAIN, LU_EV_B);
       }
     }
   }
@@ -1853,6 +1945,49 @@ static std::vector<LuStep> lu_schedule(long long n, long long spw) {
     wait(LU_MAIN, LU_EV_PANEL);
   }
   return v;
+}
+
+// The look-ahead streams (chain at the highest priority, below-panel work one
+// step lower) and the schedule's events, made once per host thread and device
+// and kept for the life of the process, so a factorization creates none.
+// Every event is recorded before it is waited on in issue order within one
+// factorization, and a factorization ends with the caller's stream joined to
+// both streams and synchronised, so reusing them across calls orders nothing
+// that the schedule did not.
+struct LuStreams {
+  cudaStream_t chain = nullptr, below = nullptr;
+  cudaEvent_t ev[LU_NEVENTS] = {};
+  cudaError_t err = cudaSuccess;
+  LuStreams() {
+    int lo = 0, hi = 0;
+    err = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    const int mid = hi < lo ? hi + 1 : hi;
+    if (err == cudaSuccess) err = cudaStreamCreateWithPriority(&chain, cudaStreamNonBlocking, hi);
+    if (err == cudaSuccess) err = cudaStreamCreateWithPriority(&below, cudaStreamNonBlocking, mid);
+    for (cudaEvent_t& e : ev)
+      if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (err != cudaSuccess) cudaGetLastError();
+  }
+};
+
+static int lu_streams(LuStreams** out) {
+  constexpr int MAX_DEV = 64;
+  thread_local LuStreams* sets[MAX_DEV] = {};
+  int dev = 0;
+  MPDOK_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= MAX_DEV) {
+    set_error("lu look-ahead streams: device ordinal out of range");
+    return MPDOK_ERR_INVALID_ARG;
+  }
+  if (sets[dev] == nullptr) sets[dev] = new LuStreams();
+  if (sets[dev]->err != cudaSuccess) {
+    const cudaError_t e = sets[dev]->err;
+    delete sets[dev];  // a later call tries again
+    sets[dev] = nullptr;
+    return cuda_status(e, "lu look-ahead streams / events");
+  }
+  *out = sets[dev];
+  return MPDOK_OK;
 }
 
 template <typename F>
@@ -1880,7 +2015,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   launch(k_scaled_copy, g2, 256, 0, s, A, lda, n, (const float*)d, W, w.ldw);
   MPDOK_LAUNCH_CHECK("lu scale");
 
-  const size_t smem_diag = DIAG_RR_SMEM;
+  const size_t smem_diag = DIAG_RR_ALLOC;
   constexpr size_t smem_tp = trsm_pair_smem(64), smem_tp16 = trsm_pair_smem(16);
   MPDOK_TRY(set_smem(k_lu_diag<F>, smem_diag));
   MPDOK_TRY(set_smem(k_trsm_pair<F, 64>, smem_tp));
@@ -1904,27 +2039,15 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     return gemm_update(C, w.ldw, Ab, Bb, spw, (int)m, (int)nn, K, fdtype, MPDOK_ENGINE_TENSOR, errw, st);
   };
   const bool lookahead = n > spw;
+  // the chain first; the panel work below the super-panel next; the far update last
   cudaStream_t side = nullptr, below = nullptr;
-  cudaEvent_t evs[LU_NEVENTS] = {};
-  auto cleanup = [&]() {
-    for (cudaEvent_t& e : evs)
-      if (e) cudaEventDestroy(e);
-    if (side) cudaStreamDestroy(side);
-    if (below) cudaStreamDestroy(below);
-  };
+  const cudaEvent_t* evs = nullptr;
   if (lookahead) {
-    int lo = 0, hi = 0;
-    cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    // the chain first; the panel work below the super-panel next; the far update last
-    const int mid = hi < lo ? hi + 1 : hi;
-    cudaError_t e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi);
-    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&below, cudaStreamNonBlocking, mid);
-    for (cudaEvent_t& ev : evs)
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    if (e != cudaSuccess) {
-      cleanup();
-      return cuda_status(e, "lu look-ahead streams / events");
-    }
+    LuStreams* ls = nullptr;
+    MPDOK_TRY(lu_streams(&ls));
+    side = ls->chain;
+    below = ls->below;
+    evs = ls->ev;
   }
   const std::vector<LuStep> sched = lu_schedule(n, spw);
   const cudaStream_t streams[3] = {s, side, below};  // LU_MAIN, LU_CHAIN, LU_BELOW
@@ -1989,13 +2112,10 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     return MPDOK_OK;
   };
   const int bst = body();
-  if (lookahead) {
+  if (lookahead && bst != MPDOK_OK) {
     // on an error the side streams may still hold work: let it finish first
-    if (bst != MPDOK_OK) {
-      cudaStreamSynchronize(side);
-      cudaStreamSynchronize(below);
-    }
-    cleanup();
+    cudaStreamSynchronize(side);
+    cudaStreamSynchronize(below);
   }
   if (bst < 0) return bst;
   {

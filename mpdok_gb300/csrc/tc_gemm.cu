@@ -626,15 +626,35 @@ constexpr int WS_TILES = 4;
 // two-CTA-per-SM kernel, whose set-up is cheaper for two or three K blocks.
 constexpr int WS_MIN_K = 256;
 
+// Streaming multiprocessors of the current device (cached per host thread and
+// device).
+static int sm_count() {
+  constexpr int MAX_DEV = 64;
+  thread_local int cnt[MAX_DEV] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEV) return 1;
+  if (cnt[dev] == 0 && cudaDeviceGetAttribute(&cnt[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return cnt[dev];
+}
+
 static int launch_tc(const CUtensorMap& ma, const CUtensorMap& mb, float* C, long long ldc, int M, int N, int K,
                      int bf16, int* err, cudaStream_t s) {
   if (K >= WS_MIN_K && aligned16(C) && ldc % 4 == 0) {
     CUtensorMap mc;
     MPDOK_TRY(make_map_c(&mc, C, M, N, ldc));
     MPDOK_TRY(set_smem(tc::ws::tc_gemm_update_ws, tc::ws::ALLOC));
+    const int ntm = (M + tc::BM - 1) / tc::BM;
     const int ntn = (N + tc::BN - 1) / tc::BN;
-    dim3 grid((M + tc::BM - 1) / tc::BM, (ntn + WS_TILES - 1) / WS_TILES);
-    tc::ws::tc_gemm_update_ws<<<grid, tc::ws::THREADS, tc::ws::ALLOC, s>>>(ma, mb, mc, M, N, K, WS_TILES, bf16, err);
+    // fewer tiles per CTA while the strips would not fill the GPU once (the
+    // 128-row block updates of the left-looking panels: 4 tiles per CTA
+    // would leave most SMs idle)
+    int T = WS_TILES;
+    while (T > 1 && (long long)ntm * ((ntn + T - 1) / T) < sm_count()) T >>= 1;
+    dim3 grid(ntm, (ntn + T - 1) / T);
+    tc::ws::tc_gemm_update_ws<<<grid, tc::ws::THREADS, tc::ws::ALLOC, s>>>(ma, mb, mc, M, N, K, T, bf16, err);
     count_launch();
     MPDOK_LAUNCH_CHECK("tc_gemm_update_ws");
     return MPDOK_OK;
@@ -655,7 +675,8 @@ int gemm_update(float* C, long long ldc, const void* A, const void* B, long long
   MPDOK_ARG_CHECK(ldc >= M, "ldc < M");
   MPDOK_ARG_CHECK(ldk >= K, "operand pitch < K");
   const int bf16 = fdtype == MPDOK_BF16 ? 1 : 0;
-  const int slot = prof_start(MPDOK_PROF_LU_GEMM, s);
+  const bool deep = engine != MPDOK_ENGINE_SIMT && K >= WS_MIN_K && aligned16(C) && ldc % 4 == 0;
+  const int slot = prof_start(deep ? MPDOK_PROF_LU_GEMM_DEEP : MPDOK_PROF_LU_GEMM, s);
   if (engine == MPDOK_ENGINE_SIMT) {
     dim3 grid((M + 127) / 128, N);
     launch(tc::simt_gemm_update, grid, 128, 0, s, A, B, ldk, bf16, C, ldc, M, N, K);

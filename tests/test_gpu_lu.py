@@ -52,6 +52,25 @@ def test_lu_factor_apply_inverts(dtype, n):
     assert err < max(1e-3, 50 * kappa * u) if dtype != "fp32" else err < 1e-4 * kappa + 1e-5
 
 
+@pytest.mark.parametrize("dtype,tol", [("fp32", 5e-6), ("fp16", 3e-3), ("bf16", 2e-2)])
+@pytest.mark.parametrize("n", [1, 128, 131, 300, 1077, 2100])
+def test_unpivoted_factors_reproduce_the_scaled_matrix(dtype, tol, n):
+    """L U = D A D for the unpivoted factorization (diagonal LU two steps per
+    barrier, block-substitution panel solves, tensor-core or CUDA-core
+    updates), with an odd last block (n = 131, 1077) included."""
+    from mpdok_gb300.lu import LUFactorization
+    X, A, b = _rbf(n, 400.0, 1e-1, seed=n + 11)
+    lu = LUFactorization(A, dtype=dtype)
+    assert lu.n_perturbed == 0
+    LU, ipiv, perm, dr, dc = (t.cpu().numpy() for t in lu.export())
+    np.testing.assert_array_equal(perm, np.arange(n))
+    W = A * dr.astype(np.float64)[:, None] * dc.astype(np.float64)[None, :]
+    L = np.tril(LU.astype(np.float64), -1) + np.eye(n)
+    U = np.triu(LU.astype(np.float64))
+    rel = np.linalg.norm(W - L @ U) / np.linalg.norm(W)
+    assert rel < tol * max(1.0, np.log2(n)), rel
+
+
 def test_lu_apply_is_deterministic():
     from mpdok_gb300.lu import LUFactorization
     X, A, b = _rbf(2000, 900.0, 1e-2, seed=4)
@@ -243,12 +262,12 @@ def test_profile_timeline_matches_class_totals():
         LUFactorization(A, dtype="fp16")
         torch.cuda.synchronize()
         tl = N.profile_timeline()
-        totals = {c: N.profile_query(c) for c in range(8)}
+        totals = {c: N.profile_query(c) for c in range(9)}
     finally:
         N.profile_enable(False)
     assert len(tl) == sum(cnt for _, cnt, _ in totals.values())
     assert np.all(tl[:, 2] >= tl[:, 1]) and np.all(tl[:, 1] >= 0.0)
-    for c in (N.PROF_LU_PANEL, N.PROF_LU_GEMM):
+    for c in (N.PROF_LU_PANEL, N.PROF_LU_GEMM, N.PROF_LU_GEMM_DEEP):
         rows = tl[tl[:, 0] == c]
         ms, cnt, work = totals[c]
         assert len(rows) == cnt > 0
@@ -256,8 +275,10 @@ def test_profile_timeline_matches_class_totals():
         assert np.isclose((rows[:, 2] - rows[:, 1]).sum(), ms, rtol=1e-3, atol=1e-3)
     # a record per 128-column panel on the chain stream (its diagonal LU and
     # its solve inside the super-panel), and one on the below stream while
-    # super-panels follow (widths of 1024)
-    n, spw, expect = 3000, 1024, 0
+    # super-panels follow
+    s = N.lu_schedule(16384, N.F16)
+    spw = sorted({int(j) for j in s[s[:, 0] == 0][:, 2]})[1]
+    n, expect = 3000, 0
     for jp in range(0, n, 128):
         jend = min(n, (jp // spw + 1) * spw)
         expect += 1 + (n > spw and jend < n)

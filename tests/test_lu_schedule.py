@@ -28,7 +28,11 @@ SETUP = -1
 
 
 def _spw(fdtype):
-    return 512 if fdtype == N.F32 else 1024
+    """The library's super-panel width: the start of the second super-panel
+    of a schedule larger than any width."""
+    s = N.lu_schedule(16384, fdtype)
+    js = sorted({int(j) for j in s[s[:, 0] == DIAG][:, 2]})
+    return js[1]
 
 
 def _happens_before(steps):
@@ -162,8 +166,8 @@ def check_schedule(steps, n, fdtype):
                     assert hb(w1, w2), f"operand {res}: write {w2} not after the earlier super-panel's {w1}"
 
 
-CASES = [(4096, N.F16), (3000, N.F16), (1000, N.BF16), (1100, N.F16), (2500, N.F32), (300, N.F16), (129, N.F32),
-         (128, N.F16), (1, N.F16)]
+CASES = [(7000, N.F16), (9000, N.BF16), (4096, N.F16), (3000, N.F16), (1000, N.BF16), (1100, N.F16), (2500, N.F32),
+         (300, N.F16), (129, N.F32), (128, N.F16), (1, N.F16)]
 
 
 @pytest.mark.parametrize("n,fdtype", CASES)
@@ -172,31 +176,37 @@ def test_schedule_orders_every_conflict(n, fdtype):
 
 
 def test_schedule_has_three_streams_at_look_ahead_sizes():
-    s = N.lu_schedule(4096, N.F16)
+    s = N.lu_schedule(7000, N.F16)
     kernels = s[np.isin(s[:, 0], [DIAG, SOLVE, UPDATE])]
     assert set(np.unique(kernels[:, 1])) == {0, 1, 2}
-    # the chain stream touches only rows and columns of its own super-panel
+    # the chain stream touches only rows and columns of its own super-panel,
+    # except for part (a) of its far update: the next super-panel's rows and
+    # columns, with K = the super-panel's width
     spw = _spw(N.F16)
     for row in kernels[kernels[:, 1] == 1]:
-        J, a, b, m, nn = (int(row[k]) for k in (2, 4, 5, 6, 7))
+        J, a, b, m, nn, K = (int(row[k]) for k in (2, 4, 5, 6, 7, 8))
+        Jend = min(7000, J + spw)
         if int(row[0]) == SOLVE:
-            assert b <= min(4096, J + spw)
+            assert b <= Jend
         elif int(row[0]) == UPDATE:
-            assert a + m <= min(4096, J + spw) and b + nn <= min(4096, J + spw)
+            inside = a + m <= Jend and b + nn <= Jend
+            cross = K == Jend - J and a >= Jend and b >= Jend and (a + m <= Jend + spw or b + nn <= Jend + spw)
+            assert inside or cross
     s = N.lu_schedule(1000, N.F16)  # one super-panel: the caller's stream alone
     assert set(np.unique(s[np.isin(s[:, 0], [DIAG, SOLVE, UPDATE]), 1])) == {0}
 
 
-@pytest.mark.parametrize("which", ["far_update_before_next_super_panel", "chain_before_below_solve",
+@pytest.mark.parametrize("which", ["previous_far_update_before_cross_update", "chain_before_below_solve",
                                    "below_before_far_update"])
 def test_checker_catches_a_missing_wait(which):
     """A planted mistake: drop one event wait from the exported schedule."""
-    n, fd = 4096, N.F16
+    n, fd = 7000, N.F16
     s = N.lu_schedule(n, fd)
     waits = np.nonzero(s[:, 0] == WAIT)[0]
     pick = {
-        # the chain stream's wait for part (a) of the previous far update
-        "far_update_before_next_super_panel": [w for w in waits if s[w, 1] == 1 and s[w, 11] == 0][1:],
+        # the chain stream's wait for part (b) of the previous far update
+        # before it updates the next super-panel's rows and columns
+        "previous_far_update_before_cross_update": [w for w in waits if s[w, 1] == 1 and s[w, 11] == 4],
         # the below stream's wait for the panel's diagonal LU and solve
         "chain_before_below_solve": [w for w in waits if s[w, 1] == 2 and s[w, 11] == 2],
         # the chain stream's join of the below stream before the far update
