@@ -330,7 +330,8 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
 //      32 x 32 diagonal block, whose elimination it repeats with shuffles, so
 //      the 32 steps need no barrier.  The pivot u_kk is replaced by +-tau
 //      when |u_kk| < tau (counted once) and every multiplier is
-//        l_r = a_rk * rcp_rn(u_kk),   a_rj <- fma(-l_r, u_kj, a_rj);
+//        l_r = a_rk * rcp(u_kk),   a_rj <- fma(-l_r, u_kj, a_rj)
+//      (rcp: the hardware reciprocal, within 1 ulp);
 //  (b) one thread per column right of the sub-panel: its 32 rows of U by the
 //      same FMAs, the multipliers read from shared memory;
 //  (c) the trailing block: a_rj <- fma(-l_rk, u_kj, a_rj) for the sub-panel's
@@ -368,6 +369,17 @@ __device__ __forceinline__ void store4(F* p, const float (&v)[4]) {
 }
 static_assert(LNB == 128 && DIAG_LU_THREADS == 256, "the diagonal LU's map: 4 sub-panels, 8 warps, 16 x 16 tiles");
 
+// The hardware reciprocal (rcp.approx.ftz.f32: at most 1 ulp from 1 / x).  It
+// sits on the diagonal LU's step-to-step critical path, where the correctly
+// rounded reciprocal costs about 1 us per 32 steps.  A pivot is at least tau
+// in magnitude, and the scaled matrix's entries are of order one, so neither
+// the pivot nor its reciprocal is subnormal.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Step K of a sub-panel's elimination, then the steps after it, for the
 // sub-panel's diagonal block (d: lane i's row) and, with X, one more row
 // block (x: lane i's row).  Recursion over K keeps every register index a
@@ -382,7 +394,7 @@ __device__ __forceinline__ void subpanel_steps(float (&d)[32], float (&x)[32], i
     if (fix) piv = (piv < 0.f) ? -tau : tau;
     if (fix && counts && lane == K) atomicAdd(nperturb, 1);
     if (lane == K) d[K] = piv;
-    const float pinv = __frcp_rn(piv);
+    const float pinv = rcp_approx(piv);
     const float ld = d[K] * pinv;
     const float lx = X ? x[K] * pinv : 0.f;
 #pragma unroll
