@@ -140,6 +140,44 @@ def cpu_lu_sample(n_sample: int, repeats: int, config: str = "HEADLINE", warmup_
     return d
 
 
+def update_standalone(n: int, warmup: int, reps: int) -> dict:
+    """The factorization's first far update alone: C ((n - w) x (n - w), FP32,
+    larger than L2) -= A B^T with K = w, the super-panel width, FP16
+    operands, through the library's tensor-core update; CUDA events on the
+    launching stream."""
+    import torch
+    from mpdok_gb300 import _native as NV
+    from mpdok_gb300.lu import gemm_update
+    s = NV.lu_schedule(16384, NV.F16)
+    w = sorted({int(j) for j in s[s[:, 0] == 0][:, 2]})[1]
+    m = n - w
+    C = torch.zeros((m, m), dtype=torch.float32, device="cuda").t()
+    A = (torch.randn((m, w), device="cuda") * 1e-2).half()
+    B = (torch.randn((m, w), device="cuda") * 1e-2).half()
+    for _ in range(warmup):
+        gemm_update(C, A, B)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        gemm_update(C, A, B)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    hbm, bf16, bf16s, kind = _peaks()
+    flops = 2.0 * m * m * w
+    byts = 8.0 * m * m + 2.0 * w * 2 * m
+    # timed alone: the burst bf16 peak is its denominator (the sustained one beside it)
+    out = {"shape": f"{m}x{m}x{w}", "ms": ms, "TFLOPs": flops / ms / 1e9, "frac_of_burst_bf16": flops / ms / 1e9 / bf16,
+           "frac_of_sustained_bf16": flops / ms / 1e9 / bf16s, "GBs": byts / ms / 1e6,
+           "frac_of_hbm": byts / ms / 1e6 / hbm, "arithmetic_intensity_flop_per_byte": flops / byts,
+           "peak_source": f"{kind}"}
+    del C, A, B
+    torch.cuda.empty_cache()
+    return out
+
+
 def gemv_standalone(n: int, warmup: int, reps: int) -> dict:
     """Stored-matrix GEMV y = A x on (n x n) column-major FP32 / FP64 / BF16
     operands larger than L2, timed with CUDA events on the launching stream."""
@@ -1089,6 +1127,7 @@ def main():
                "upload_frac_of_pinned_copy": 8.0 * n * n / up_s / 1e9 / link}
 
     gemv_sa = gemv_standalone(n, 3, 10) if rank == 0 else None
+    update_sa = update_standalone(n, 1, 3) if rank == 0 else None
 
     # every other configuration once (not per step), so that the driver-run
     # line carries them; each is a complete measurement of its own workload
@@ -1118,6 +1157,7 @@ def main():
         "config": headline_config(n, world), "solver": solver_desc, "assembly_s": t_asm,
         "relres": relres, "solve_info": infos[-1], "fp64_gpu_baseline": fp64,
         "roofline": roof, "gemv_roofline": rooflines.get("gemv_f32"), "gemv_standalone": gemv_sa,
+        "update_standalone": update_sa,
         "rooflines": rooflines,
         "kernel_time_share": share, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": ck, "configs": extras,

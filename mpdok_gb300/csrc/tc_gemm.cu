@@ -620,8 +620,13 @@ static int make_map_c(CUtensorMap* map, float* C, int M, int N, long long ldc) {
 
 constexpr int TC_STAGES = 2;
 
-// Tiles per CTA of the warp-specialised kernel along N (the strip shares A).
-constexpr int WS_TILES = 4;
+// Tiles per CTA of the warp-specialised kernel along N (the strip shares A,
+// and the epilogue of one tile overlaps the MMAs of the next).  Two, not
+// more: a CTA of the far update then holds its SM for about 25 us at K = 2048,
+// so the panel kernels of the other streams find SMs sooner (the 16-bit
+// factorization at N=32768: 45.5 ms with four tiles, 45.0 ms with two, 46.0
+// ms with one).
+constexpr int WS_TILES = 2;
 // K from which the warp-specialised kernel is used; shallower updates keep the
 // two-CTA-per-SM kernel, whose set-up is cheaper for two or three K blocks.
 constexpr int WS_MIN_K = 256;
@@ -649,8 +654,7 @@ static int launch_tc(const CUtensorMap& ma, const CUtensorMap& mb, float* C, lon
     const int ntm = (M + tc::BM - 1) / tc::BM;
     const int ntn = (N + tc::BN - 1) / tc::BN;
     // fewer tiles per CTA while the strips would not fill the GPU once (the
-    // 128-row block updates of the left-looking panels: 4 tiles per CTA
-    // would leave most SMs idle)
+    // 128-row block updates of the left-looking panels)
     int T = WS_TILES;
     while (T > 1 && (long long)ntm * ((ntn + T - 1) / T) < sm_count()) T >>= 1;
     dim3 grid(ntm, (ntn + T - 1) / T);
