@@ -912,8 +912,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", default="headline",
-                    choices=["headline", "gemv", "batch", "ooc", "ooc_solve", "multi_rhs", "c2", "hard"],
+                    choices=["headline", "gemv", "update", "batch", "ooc", "ooc_solve", "multi_rhs", "c2", "hard"],
                     help="gemv: only the standalone stored-matrix GEMV measurement (used for kernel profiles); "
+                         "update: only the standalone first far update of the factorization at --n; "
                          "batch: the batched C4 solve + adjoint line; ooc: the out-of-core C5 streaming line")
     ap.add_argument("--systems", type=int, default=256, help="--only batch: number of C4 systems")
     args = ap.parse_args()
@@ -923,6 +924,11 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         print(json.dumps(gemv_standalone(args.n, max(3, args.warmup), max(5, args.steps))))
+        return 0
+    if args.only == "update":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps(update_standalone(args.n, max(1, args.warmup), max(3, args.steps))))
         return 0
     if args.only == "batch":
         bench_batch(args)
