@@ -331,7 +331,8 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
 //      the 32 steps need no barrier.  The pivot u_kk is replaced by +-tau
 //      when |u_kk| < tau (counted once) and every multiplier is
 //        l_r = a_rk * rcp(u_kk),   a_rj <- fma(-l_r, u_kj, a_rj)
-//      (rcp: the hardware reciprocal, within 1 ulp);
+//      (rcp: the hardware reciprocal, within 1 ulp, for 16-bit factors; the
+//      correctly rounded one for FP32 factors);
 //  (b) one thread per column right of the sub-panel: its 32 rows of U by the
 //      same FMAs, the multipliers read from shared memory;
 //  (c) the trailing block: a_rj <- fma(-l_rk, u_kj, a_rj) for the sub-panel's
@@ -371,9 +372,11 @@ static_assert(LNB == 128 && DIAG_LU_THREADS == 256, "the diagonal LU's map: 4 su
 
 // The hardware reciprocal (rcp.approx.ftz.f32: at most 1 ulp from 1 / x).  It
 // sits on the diagonal LU's step-to-step critical path, where the correctly
-// rounded reciprocal costs about 1 us per 32 steps.  A pivot is at least tau
-// in magnitude, and the scaled matrix's entries are of order one, so neither
-// the pivot nor its reciprocal is subnormal.
+// rounded reciprocal costs about 1 us per 32 steps.  16-bit factors use it (its
+// error is far below their rounding); FP32 factors keep the correctly rounded
+// reciprocal, which near-FP64 refinement tolerances can tell apart.  A pivot
+// is at least tau in magnitude, and the scaled matrix's entries are of order
+// one, so neither the pivot nor its reciprocal is subnormal.
 __device__ __forceinline__ float rcp_approx(float x) {
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
@@ -384,7 +387,7 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // sub-panel's diagonal block (d: lane i's row) and, with X, one more row
 // block (x: lane i's row).  Recursion over K keeps every register index a
 // constant.
-template <int K, bool X>
+template <int K, bool X, bool EXACT>
 __device__ __forceinline__ void subpanel_steps(float (&d)[32], float (&x)[32], int lane, bool counts, int kmax,
                                                float tau, int* nperturb) {
   if constexpr (K < 32) {
@@ -394,7 +397,7 @@ __device__ __forceinline__ void subpanel_steps(float (&d)[32], float (&x)[32], i
     if (fix) piv = (piv < 0.f) ? -tau : tau;
     if (fix && counts && lane == K) atomicAdd(nperturb, 1);
     if (lane == K) d[K] = piv;
-    const float pinv = rcp_approx(piv);
+    const float pinv = EXACT ? __frcp_rn(piv) : rcp_approx(piv);
     const float ld = d[K] * pinv;
     const float lx = X ? x[K] * pinv : 0.f;
 #pragma unroll
@@ -405,7 +408,7 @@ __device__ __forceinline__ void subpanel_steps(float (&d)[32], float (&x)[32], i
     }
     if (lane > K) d[K] = ld;
     if (X) x[K] = lx;
-    subpanel_steps<K + 1, X>(d, x, lane, counts, kmax, tau, nperturb);
+    subpanel_steps<K + 1, X, EXACT>(d, x, lane, counts, kmax, tau, nperturb);
   }
 }
 
@@ -479,7 +482,7 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
         d[j] = T[(P0 + lane) * DP + P0 + j];
         x[j] = warp == 0 ? 0.f : T[R * DP + P0 + j];
       }
-      subpanel_steps<0, true>(d, x, lane, warp == 0, kmax, tau, nperturb);
+      subpanel_steps<0, true, sizeof(F) == 4>(d, x, lane, warp == 0, kmax, tau, nperturb);
       if (warp == 0) {
 #pragma unroll
         for (int j = 0; j < 32; ++j) T[(P0 + lane) * DP + P0 + j] = d[j];
