@@ -1800,40 +1800,43 @@ int lu_apply_any(const void* fbuf, long long n, int fdtype, const float* v, floa
 // column strip (rows >= Jend, columns < Jend); the far trailing matrix
 // (rows, columns >= Jend) then receives all of them at once, K = spw.
 //
-// Look-ahead: super-panels are factored on a high-priority side stream.
-// The far update of super-panel J runs on the caller's stream in two parts:
-// (a) the rows and columns of super-panel J + 1 (rows [Jend, Jn) x columns
-// >= Jend, and rows >= Jn x columns [Jend, Jn)), after which the side
-// stream may factor super-panel J + 1; (b) the rest, rows and columns >= Jn,
-// concurrently with it.  The two touch disjoint parts of W: the inner loop
-// of J + 1 writes rows < Jn or columns < Jn only.  Operands alternate between
-// two buffers, so (b) of J still reads its own while J + 1 writes the other.
+// Look-ahead: super-panels are factored on a high-priority chain stream.  The
+// far update of super-panel J has two parts: (a) the rows and columns of
+// super-panel J + 1 (rows [Jend, Jn) x columns >= Jend, and rows >= Jn x
+// columns [Jend, Jn)), which the chain stream applies itself once the work
+// below J and part (b) of J - 1 are done, and then factors J + 1; (b) the
+// rest, rows and columns >= Jn, on the caller's stream, concurrently with
+// J + 1.  The two touch disjoint parts of W: the inner loop of J + 1 writes
+// rows < Jn or columns < Jn only.  Operands alternate between two buffers, so
+// (b) of J still reads its own while J + 1 writes the other.
 //
-// Inside a super-panel the panels run on two more streams.  The chain stream
-// (sa) runs, per panel p with columns [jp, r1 = jp + 128): the diagonal-block
-// LU; the panel solve for the rest of the super-panel (rows and columns
-// [r1, Jend), 16-row blocks, one launch); the update of the rest of the
-// super-panel, rows and columns [r1, Jend) (one launch); then the next
-// diagonal LU.  A panel therefore costs three dependent launches on one
-// stream and no cross-stream hand-off.  The below stream (sc, lower priority)
-// handles the rows and columns past the super-panel left-looking: for panel p
-// it first applies every earlier panel of the super-panel to p's own column
-// block rows >= Jend and row block columns >= Jend (one update each, K = jp -
-// J, instead of a K = 128 update of the whole row and column strips per
-// panel: 1/4.5 of the FP32 traffic), then solves p's panel there.  Only later
-// panels' below work and the far update read what it writes, so the chain
-// never waits for it.
+// Inside a super-panel the chain stream (sa) runs, per panel p with columns
+// [jp, r1 = jp + 128): the diagonal-block LU; the panel solve for the rest of
+// the super-panel (rows and columns [r1, Jend), 16-row blocks, one launch);
+// the update of the rest of the super-panel, rows and columns [r1, Jend) (one
+// launch); then the next diagonal LU.  A panel therefore costs three dependent
+// launches on one stream and no cross-stream hand-off.  Two below streams (sc,
+// sd, lower priority) handle the rows and columns past the super-panel
+// left-looking: for panel p they apply every earlier panel of the super-panel
+// to p's own column block rows >= Jend (sc) and row block columns >= Jend
+// (sd, concurrently), one update each with K = jp - J instead of a K = 128
+// update of the whole row and column strips per panel (1/4.5 of the FP32
+// traffic); then sc solves p's panel there.  Only later panels' below work and
+// the far update read what they write, so the chain never waits for them
+// until the end of the super-panel.
 //
 // The schedule is data: lu_schedule lists every launch, event record and
 // event wait of one factorization in issue order, lu_factor_t executes the
 // list, and mpdok_lu_schedule exports it, so that a host-only check can verify
 // that every pair of launches touching the same data is ordered by the
 // streams and events.
-enum LuStream : int { LU_MAIN = 0, LU_CHAIN = 1, LU_BELOW = 2 };
+enum LuStream : int { LU_MAIN = 0, LU_CHAIN = 1, LU_BELOW = 2, LU_BELOW2 = 3 };
+constexpr int LU_NSTREAMS = 4;
 enum LuKind : int { LU_DIAG = 0, LU_SOLVE = 1, LU_UPDATE = 2, LU_RECORD = 3, LU_WAIT = 4, LU_PROF_START = 5,
                     LU_PROF_STOP = 6 };
-enum LuEvent : int { LU_EV_READY = 0, LU_EV_PANEL = 1, LU_EV_A = 2, LU_EV_C = 3, LU_EV_B = 4 };
-constexpr int LU_NEVENTS = 5;
+enum LuEvent : int { LU_EV_READY = 0, LU_EV_PANEL = 1, LU_EV_A = 2, LU_EV_C = 3, LU_EV_B = 4, LU_EV_D = 5,
+                     LU_EV_E = 6 };
+constexpr int LU_NEVENTS = 7;
 struct LuStep {
   int kind = 0, stream = 0;
   long long J = 0;           // super-panel start (operand buffer (J / spw) & 1)
@@ -1890,7 +1893,7 @@ static std::vector<LuStep> lu_schedule(long long n, long long spw) {
   for (long long J = 0; J < n; J += spw) {
     const long long Jend = std::min<long long>(n, J + spw);
     const int sa = lookahead ? LU_CHAIN : LU_MAIN;
-    const int sc = LU_BELOW;
+    const int sc = LU_BELOW, sd = LU_BELOW2;
     const bool below = lookahead && Jend < n;  // rows and columns past the super-panel
     for (long long jp = J; jp < Jend; jp += LNB) {
       const long long r1 = jp + LNB;  // first row / column after the panel
@@ -1916,12 +1919,20 @@ static std::vector<LuStep> lu_schedule(long long n, long long spw) {
       if (below) {
         wait(sc, LU_EV_A);  // the chain's solves of panels J .. p, and p's diagonal LU
         if (jp > J) {
+          // the column block here, the row block concurrently on the second
+          // below stream; the row block reads U12 of the earlier panels past
+          // the super-panel, so it waits for the previous panel solve below
+          // (which itself followed the chain's solve of that panel)
+          wait(sd, LU_EV_E);
           update(sc, J, 0, jp - J, Jend, jp, n - Jend, std::min<long long>(LNB, Jend - jp));
-          update(sc, J, 0, jp - J, jp, Jend, std::min<long long>(LNB, Jend - jp), n - Jend);
+          update(sd, J, 0, jp - J, jp, Jend, std::min<long long>(LNB, Jend - jp), n - Jend);
+          record(sd, LU_EV_D);
+          wait(sc, LU_EV_D);
         }
         prof(sc, 2, true, 0.0);
         solve(sc, J, jp, Jend, n, 64);
         prof(sc, 2, false, 2.0 * 2.0 * (double)(n - Jend) * LNB * LNB);
+        record(sc, LU_EV_E);
       }
     }
     if (below) {  // join the below stream
@@ -1962,15 +1973,15 @@ static std::vector<LuStep> lu_schedule(long long n, long long spw) {
   return v;
 }
 
-// The look-ahead streams (chain at the highest priority, below-panel work one
-// step lower) and the schedule's events, made once per host thread and device
+// The look-ahead streams (chain at the highest priority, the two below-panel
+// streams one step lower) and the schedule's events, made once per host thread and device
 // and kept for the life of the process, so a factorization creates none.
 // Every event is recorded before it is waited on in issue order within one
 // factorization, and a factorization ends with the caller's stream joined to
 // both streams and synchronised, so reusing them across calls orders nothing
 // that the schedule did not.
 struct LuStreams {
-  cudaStream_t chain = nullptr, below = nullptr;
+  cudaStream_t chain = nullptr, below = nullptr, below2 = nullptr;
   cudaEvent_t ev[LU_NEVENTS] = {};
   cudaError_t err = cudaSuccess;
   LuStreams() {
@@ -1979,6 +1990,7 @@ struct LuStreams {
     const int mid = hi < lo ? hi + 1 : hi;
     if (err == cudaSuccess) err = cudaStreamCreateWithPriority(&chain, cudaStreamNonBlocking, hi);
     if (err == cudaSuccess) err = cudaStreamCreateWithPriority(&below, cudaStreamNonBlocking, mid);
+    if (err == cudaSuccess) err = cudaStreamCreateWithPriority(&below2, cudaStreamNonBlocking, mid);
     for (cudaEvent_t& e : ev)
       if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     if (err != cudaSuccess) cudaGetLastError();
@@ -2055,17 +2067,18 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
   };
   const bool lookahead = n > spw;
   // the chain first; the panel work below the super-panel next; the far update last
-  cudaStream_t side = nullptr, below = nullptr;
+  cudaStream_t side = nullptr, below = nullptr, below2 = nullptr;
   const cudaEvent_t* evs = nullptr;
   if (lookahead) {
     LuStreams* ls = nullptr;
     MPDOK_TRY(lu_streams(&ls));
     side = ls->chain;
     below = ls->below;
+    below2 = ls->below2;
     evs = ls->ev;
   }
   const std::vector<LuStep> sched = lu_schedule(n, spw);
-  const cudaStream_t streams[3] = {s, side, below};  // LU_MAIN, LU_CHAIN, LU_BELOW
+  const cudaStream_t streams[LU_NSTREAMS] = {s, side, below, below2};  // LU_MAIN, LU_CHAIN, LU_BELOW, LU_BELOW2
   int prof_window[3] = {-1, -1, -1};
   auto body = [&]() -> int {
     for (const LuStep& st : sched) {
@@ -2131,6 +2144,7 @@ static int lu_factor_t(const double* A, long long lda, long long n, int fdtype, 
     // on an error the side streams may still hold work: let it finish first
     cudaStreamSynchronize(side);
     cudaStreamSynchronize(below);
+    cudaStreamSynchronize(below2);
   }
   if (bst < 0) return bst;
   {

@@ -1,8 +1,8 @@
 """Host-only check of the blocked LU's launch schedule (mpdok_lu_schedule).
 
-The factorization issues its kernels on three streams (the caller's, a chain
-stream for the work inside the current super-panel, and a stream for the rows
-and columns past it) that only events order.  This test rebuilds the
+The factorization issues its kernels on four streams (the caller's, a chain
+stream for the work inside the current super-panel, and two streams for the
+rows and columns past it) that only events order.  This test rebuilds the
 happens-before relation of the exported schedule with vector clocks and checks:
 
 * every pair of launches that touch the same data with at least one write is
@@ -39,8 +39,9 @@ def _happens_before(steps):
     """Kernel ops (with a setup op first: the scaling and the working copy on
     the caller's stream) and a predicate hb(i, j): op i completes before op j
     starts on the GPU."""
-    cur = np.zeros((3, 3), dtype=np.int64)   # vector clock of each stream
-    count = [1, 0, 0]                        # the setup op is position 1 of stream 0
+    ns = max(3, int(steps[:, 1].max()) + 1) if len(steps) else 3
+    cur = np.zeros((ns, ns), dtype=np.int64)  # vector clock of each stream
+    count = [1] + [0] * (ns - 1)              # the setup op is position 1 of stream 0
     cur[0, 0] = 1
     recorded = {}
     ops = [dict(kind=SETUP, stream=0, pos=1, clock=cur[0].copy())]
@@ -175,10 +176,10 @@ def test_schedule_orders_every_conflict(n, fdtype):
     check_schedule(N.lu_schedule(n, fdtype), n, fdtype)
 
 
-def test_schedule_has_three_streams_at_look_ahead_sizes():
+def test_schedule_has_four_streams_at_look_ahead_sizes():
     s = N.lu_schedule(7000, N.F16)
     kernels = s[np.isin(s[:, 0], [DIAG, SOLVE, UPDATE])]
-    assert set(np.unique(kernels[:, 1])) == {0, 1, 2}
+    assert set(np.unique(kernels[:, 1])) == {0, 1, 2, 3}
     # the chain stream touches only rows and columns of its own super-panel,
     # except for part (a) of its far update: the next super-panel's rows and
     # columns, with K = the super-panel's width
@@ -197,7 +198,7 @@ def test_schedule_has_three_streams_at_look_ahead_sizes():
 
 
 @pytest.mark.parametrize("which", ["previous_far_update_before_cross_update", "chain_before_below_solve",
-                                   "below_before_far_update"])
+                                   "below_before_far_update", "below_solve_before_row_update"])
 def test_checker_catches_a_missing_wait(which):
     """A planted mistake: drop one event wait from the exported schedule."""
     n, fd = 7000, N.F16
@@ -211,6 +212,9 @@ def test_checker_catches_a_missing_wait(which):
         "chain_before_below_solve": [w for w in waits if s[w, 1] == 2 and s[w, 11] == 2],
         # the chain stream's join of the below stream before the far update
         "below_before_far_update": [w for w in waits if s[w, 1] == 1 and s[w, 11] == 3],
+        # the second below stream's wait for the previous panel solve below
+        # (whose U12 columns its row-block update reads)
+        "below_solve_before_row_update": [w for w in waits if s[w, 1] == 3 and s[w, 11] == 6],
     }[which]
     assert pick
     broken = np.delete(s, pick[len(pick) // 2], axis=0)
