@@ -257,54 +257,98 @@ __device__ __forceinline__ void inverse_doubling(const float* T, float* XL, floa
 
 // The 32 x 32 diagonal blocks of L^-1 (unit lower) and U^-1 from the factored
 // block T (shared memory, pitch DP): warps 0-3 invert L's four blocks, warps
-// 4-7 U's, lane j holding column j in registers.  The substitution is
-// right-looking: once x_i is final its term goes into every later row's
-// accumulator, so a step is one division (U) and independent FMAs, and the
-// block's column i is a shared-memory broadcast.  L's accumulators receive
-// their terms in increasing column order, the order of a row-by-row forward
-// substitution; U's in decreasing order.  Terms outside a column's triangle
-// are exact zeros.  Entry (r, c) of an inverse goes to dst[r * rs + c * cs];
-// with a staging area (32 x 33 floats per warp) and rs == 1 each warp writes
-// its block column by column in 128-byte runs instead of one word per lane.
-__device__ __forceinline__ void diag32_inverses(const float* T, float* XL, float* XU, int rs, int cs,
-                                                float* stage = nullptr) {
+// 4-7 U's, lane j computing column j of its inverse into a shared-memory
+// column w (entry i at w[i * ws]).  Rows are taken in chunks of eight (top
+// down for L, bottom up for U): a rolled loop adds the terms of the finished
+// chunks, a row's accumulators in registers, then an unrolled 8 x 8 step
+// finishes the chunk.  Each entry receives its terms in the order of a
+// right-looking substitution: increasing column for L, decreasing for U; terms
+// outside a column's triangle are exact zeros and are left out.  The loops stay
+// rolled because this runs once per diagonal block, usually on an SM whose
+// instruction cache holds other kernels' code: an unrolled substitution took
+// 5.4 us alone but 15 us inside the factorization, fetching its code from a
+// busy L2.
+template <bool LOWER>
+__device__ __forceinline__ void diag32_column(const float* __restrict__ Tb, float* __restrict__ w, int ws, int lane) {
+  if (LOWER) {
+    for (int c = 0; c < 32; c += 8) {
+      float acc[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) acc[r] = (c + r == lane) ? 1.f : 0.f;
+#pragma unroll 2
+      for (int k = lane; k < c; ++k) {  // x_k = 0 above the diagonal (k < lane)
+        const float xk = w[k * ws];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) acc[r] = fmaf(-Tb[(c + r) * DP + k], xk, acc[r]);
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const float xr = (c + r < lane) ? 0.f : acc[r];
+        acc[r] = xr;
+        if (c + r >= lane) {
+#pragma unroll
+          for (int q = r + 1; q < 8; ++q) acc[q] = fmaf(-Tb[(c + q) * DP + c + r], xr, acc[q]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) w[(c + r) * ws] = acc[r];
+    }
+  } else {
+    for (int c = 24; c >= 0; c -= 8) {
+      float acc[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) acc[r] = 0.f;
+#pragma unroll 2
+      for (int k = lane; k >= c + 8; --k) {  // x_k = 0 below the diagonal (k > lane)
+        const float xk = w[k * ws];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) acc[r] = fmaf(Tb[(c + r) * DP + k], xk, acc[r]);
+      }
+#pragma unroll
+      for (int r = 7; r >= 0; --r) {
+        const int i = c + r;
+        const float num = (i == lane) ? 1.f : -acc[r];
+        const float xr = (i > lane) ? 0.f : num / Tb[i * DP + i];
+        acc[r] = xr;
+        if (i <= lane) {
+#pragma unroll
+          for (int q = 0; q < r; ++q) acc[q] = fmaf(Tb[(c + q) * DP + i], xr, acc[q]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) w[(c + r) * ws] = acc[r];
+    }
+  }
+}
+
+// Into shared memory: entry (r, c) of the inverses at XL / XU[r * DP + c].
+__device__ __forceinline__ void diag32_inverses_smem(const float* T, float* XL, float* XU) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp >= 8) return;  // idle during the 32 x 32 substitutions
   const int o = (warp & 3) * 32;
-  const float* Tb = T + o * DP + o;
-  float x[32];
-  if (warp < 4) {
-#pragma unroll
-    for (int i = 0; i < 32; ++i) x[i] = (i == lane) ? 1.f : 0.f;
-#pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      if (i < lane) x[i] = 0.f;
-#pragma unroll
-      for (int j = i + 1; j < 32; ++j) x[j] = fmaf(-Tb[j * DP + i], x[i], x[j]);
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < 32; ++i) x[i] = 0.f;
-#pragma unroll
-    for (int i = 31; i >= 0; --i) {
-      const float num = (i == lane) ? 1.f : -x[i];
-      x[i] = (i > lane) ? 0.f : num / Tb[i * DP + i];
-#pragma unroll
-      for (int j = 0; j < i; ++j) x[j] = fmaf(Tb[j * DP + i], x[i], x[j]);
-    }
-  }
-  float* X = warp < 4 ? XL : XU;
-  if (stage != nullptr && rs == 1) {
-    float* st = stage + warp * 32 * 33;
-#pragma unroll
-    for (int i = 0; i < 32; ++i) st[i * 33 + lane] = x[i];
-    __syncwarp();
-#pragma unroll 8
-    for (int c = 0; c < 32; ++c) X[(o + lane) + (long long)(o + c) * cs] = st[lane * 33 + c];
-  } else {
-#pragma unroll
-    for (int i = 0; i < 32; ++i) X[(o + i) * rs + (o + lane) * cs] = x[i];
-  }
+  if (warp < 4)
+    diag32_column<true>(T + o * DP + o, XL + o * DP + o + lane, DP, lane);
+  else
+    diag32_column<false>(T + o * DP + o, XU + o * DP + o + lane, DP, lane);
+}
+
+// Into global memory, column-major with pitch ld, through a staging area of
+// 32 x 33 floats per warp: each warp writes its block column by column in
+// 128-byte runs.
+__device__ __forceinline__ void diag32_inverses_global(const float* T, float* Linv, float* Uinv, int ld,
+                                                       float* stage) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp >= 8) return;
+  const int o = (warp & 3) * 32;
+  float* st = stage + warp * 32 * 33;
+  if (warp < 4)
+    diag32_column<true>(T + o * DP + o, st + lane, 33, lane);
+  else
+    diag32_column<false>(T + o * DP + o, st + lane, 33, lane);
+  __syncwarp();
+  float* X = warp < 4 ? Linv : Uinv;
+#pragma unroll 4
+  for (int c = 0; c < 32; ++c) X[(o + lane) + (long long)(o + c) * ld] = st[lane * 33 + c];
 }
 
 // Inverses by recursive doubling: the 32 x 32 diagonal blocks by substitution,
@@ -316,7 +360,7 @@ __device__ void tri_inverses(const float* T, float* XL, float* XU, float* Tmp) {
   const int tid = threadIdx.x;
   for (int idx = tid; idx < LNB * DP; idx += blockDim.x) { XL[idx] = 0.f; XU[idx] = 0.f; }
   __syncthreads();
-  diag32_inverses(T, XL, XU, DP, 1);
+  diag32_inverses_smem(T, XL, XU);
   __syncthreads();
   inverse_doubling<32>(T, XL, XU, Tmp);
   inverse_doubling<64>(T, XL, XU, Tmp);
@@ -529,7 +573,7 @@ k_lu_diag(float* __restrict__ W, long long ldw, long long j0, int nbk, F* __rest
       }
     }
   }
-  diag32_inverses(T, Linv, Uinv, 1, LNB, stage);
+  diag32_inverses_global(T, Linv, Uinv, LNB, stage);
 }
 
 // The full 128 x 128 inverses of every diagonal block (for the triangular
