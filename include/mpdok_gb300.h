@@ -432,13 +432,14 @@ enum {
   MPDOK_PROF_GEMV_F32 = 0,   /* stored FP32 / 16-bit GEMV stage (bytes)  */
   MPDOK_PROF_GEMV_F64 = 1,   /* stored FP64 GEMV stage (bytes)           */
   MPDOK_PROF_ASSEMBLE = 2,   /* RBF assembly (bytes written)             */
-  MPDOK_PROF_LU_GEMM = 3,    /* LU trailing-update GEMM, K < 256, and the
-                                FP32-factor update (flops)               */
+  MPDOK_PROF_LU_GEMM = 3,    /* LU trailing-update GEMM, K < 128 or the
+                                SIMT engine, and the FP32-factor update
+                                (flops)                                  */
   MPDOK_PROF_TRSV = 4,       /* triangular solves (bytes)                */
   MPDOK_PROF_MATFREE = 5,    /* matrix-free evaluate-and-multiply (entries) */
   MPDOK_PROF_OOC_COPY = 6,   /* host -> device tile copies (bytes)       */
   MPDOK_PROF_LU_PANEL = 7,   /* LU panel factorization (flops)           */
-  MPDOK_PROF_LU_GEMM_DEEP = 8 /* LU trailing-update GEMM with K >= 256: the
+  MPDOK_PROF_LU_GEMM_DEEP = 8 /* LU trailing-update GEMM with K >= 128: the
                                 warp-specialised tensor-core kernel (flops) */
 };
 MPDOK_API long long mpdok_launch_count(void);

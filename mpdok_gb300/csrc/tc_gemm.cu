@@ -291,7 +291,7 @@ tc_gemm_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 }
 
 // ------------------------------------------------------------------------
-// Warp-specialised form for deep updates (K >= 256): one CTA per SM walks a
+// Warp-specialised form for the LU's updates (K >= 128): one CTA per SM walks a
 // strip of T tiles (128 x 256) that share their A rows, with
 //   * a 4-stage TMA ring (48 KB per stage: the A and B blocks of one 64-deep
 //     K step), so four loads are in flight while the tensor cores work;
@@ -627,9 +627,12 @@ constexpr int TC_STAGES = 2;
 // factorization at N=32768: 45.5 ms with four tiles, 45.0 ms with two, 46.0
 // ms with one).
 constexpr int WS_TILES = 2;
-// K from which the warp-specialised kernel is used; shallower updates keep the
-// two-CTA-per-SM kernel, whose set-up is cheaper for two or three K blocks.
-constexpr int WS_MIN_K = 256;
+// K from which the warp-specialised kernel is used: every update of the LU
+// (K = 128 inside the super-panel) takes it, since its TMA reduce-add epilogue
+// keeps C out of registers (the 16-bit factorization at N=32768: 44.1 ms with
+// the K = 128 updates on the two-CTA-per-SM kernel, 43.2 ms on this one); the
+// other kernel remains for K = 64.
+constexpr int WS_MIN_K = 128;
 
 // Streaming multiprocessors of the current device (cached per host thread and
 // device).

@@ -267,10 +267,11 @@ def test_profile_timeline_matches_class_totals():
         N.profile_enable(False)
     assert len(tl) == sum(cnt for _, cnt, _ in totals.values())
     assert np.all(tl[:, 2] >= tl[:, 1]) and np.all(tl[:, 1] >= 0.0)
+    assert totals[N.PROF_LU_PANEL][1] > 0 and totals[N.PROF_LU_GEMM_DEEP][1] > 0
     for c in (N.PROF_LU_PANEL, N.PROF_LU_GEMM, N.PROF_LU_GEMM_DEEP):
         rows = tl[tl[:, 0] == c]
         ms, cnt, work = totals[c]
-        assert len(rows) == cnt > 0
+        assert len(rows) == cnt
         assert np.isclose(rows[:, 3].sum(), work, rtol=1e-12)
         assert np.isclose((rows[:, 2] - rows[:, 1]).sum(), ms, rtol=1e-3, atol=1e-3)
     # a record per 128-column panel on the chain stream (its diagonal LU and
