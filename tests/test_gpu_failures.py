@@ -1,4 +1,4 @@
-"""GPU: failure paths, each made on the host (SURVEY §5 failure handling).
+"""GPU: failure paths, each made on the host (the failure handling of the reference's solvers).
 
 * a right-hand side with a NaN gives a clean MPDOK_ERR_NONFINITE status from
   every solver entry point, and the drop-in wrappers' warning names the error;
