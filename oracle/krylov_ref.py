@@ -1,6 +1,6 @@
 """CPU oracle: NumPy/SciPy restatement of MPDOK's dense-operator Krylov path.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker for the sm_103a
+TEST INFRASTRUCTURE ONLY.  This module is the oracle of the sm_103a
 implementation: only tests/, __graft_entry__.smoke() and bench.py's CPU
 baseline / reference arm import it.  The product never routes through it.
 
