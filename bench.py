@@ -1135,7 +1135,7 @@ def main():
     gemv_sa = gemv_standalone(n, 3, 10) if rank == 0 else None
     update_sa = update_standalone(n, 1, 3) if rank == 0 else None
 
-    # every other configuration once (not per step), so that the driver-run
+    # every other configuration once (not per step), so that the default
     # line carries them; each is a complete measurement of its own workload
     extras = {}
     if not args.no_extras and rank == 0 and world == 1:
